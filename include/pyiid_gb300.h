@@ -1,0 +1,195 @@
+/*
+ * pyiid_gb300.h -- C ABI of the GB300 (sm_103a) elastic-scattering library.
+ *
+ * The library evaluates the Debye scattering chain of pyIID on one GPU:
+ *
+ *   pair distances r_ab -> F(Q) = 2 * sum_{a>b} f_a f_b sin(Q r_ab)/r_ab / na(Q)
+ *   F(Q) -> G(r) (the reference's FFT transform, as an exact linear map)
+ *   G(r) -> Rw or chi^2 against an observed G(r), and the position gradient.
+ *
+ * Conventions shared by every entry point
+ *   - All functions return an int status (PYIID_OK == 0).  On failure the
+ *     message is available from pyiid_last_error(ctx) (or pyiid_last_error(NULL)
+ *     when no context exists yet).  Nothing aborts the process.
+ *   - Pointers documented "device" must be CUDA device (or managed) memory of
+ *     the context's device.  Pointers documented "host" are read during the
+ *     call and may be freed afterwards.
+ *   - Work is enqueued on the context's stream (pyiid_set_stream) and is
+ *     asynchronous with respect to the host unless stated otherwise.
+ *   - Q grids are uniform and start at zero: Q_k = k * qbin, k in [0, n_bins).
+ *     Output bins below k_begin are written as zero and never computed.
+ *   - Atoms carry a species id; per-species form factors f_s(Q_k) are given as
+ *     a host table [n_species][n_bins] (the reference's per-atom
+ *     'F(Q) scatter' / 'PDF scatter' arrays have one distinct row per species).
+ *   - Numerical semantics follow the reference: NaN results (coincident atoms,
+ *     fewer than two atoms) become 0 and +-inf become +-FLT_MAX, as numpy's
+ *     nan_to_num does on the reference's float32 arrays.
+ *
+ * One context per host thread / stream.  Contexts are independent; the only
+ * shared state is read-only.
+ */
+#ifndef PYIID_GB300_H
+#define PYIID_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PYIID_OK = 0,
+  PYIID_ERR_INVALID_ARG = 1,
+  PYIID_ERR_CUDA = 2,
+  PYIID_ERR_OOM = 3,
+  PYIID_ERR_DEVICE_FLAG = 4,
+  PYIID_ERR_TIMEOUT = 5
+};
+
+enum { PYIID_POTENTIAL_RW = 0, PYIID_POTENTIAL_CHI_SQ = 1 };
+
+typedef struct pyiid_ctx pyiid_ctx;
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int pyiid_version(void);
+
+/* Create a context bound to CUDA device `device` (the default stream is used
+ * until pyiid_set_stream is called).  Replaces the processor probe of
+ * pyiid/experiments/elasticscatter/__init__.py:29-38 (check_gpu) and the
+ * per-GPU context handling of gpu_wrappers/gpu_wrap.py:287-314. */
+int pyiid_create(pyiid_ctx **out, int device);
+int pyiid_destroy(pyiid_ctx *ctx);
+
+/* Enqueue subsequent work on `stream` (a cudaStream_t; NULL = legacy default). */
+int pyiid_set_stream(pyiid_ctx *ctx, void *stream);
+
+/* Wait for all work enqueued by this context. */
+int pyiid_synchronize(pyiid_ctx *ctx);
+
+/* Last error message of `ctx` (or of the last failed pyiid_create when ctx is
+ * NULL).  The string stays valid until the next call on the same context. */
+const char *pyiid_last_error(const pyiid_ctx *ctx);
+
+/* Number of kernels this context has launched so far (for launch accounting). */
+int64_t pyiid_launch_count(const pyiid_ctx *ctx);
+
+/* ------------------------------------------------------------------------ *
+ * Reduced structure factor.
+ *
+ * fq[k] = 2 * nan_to_num( S_k / na_k ),  k in [k_begin, n_bins)
+ *   S_k  = sum_{a>b} f_a(Q_k) f_b(Q_k) sin(Q_k r_ab) / r_ab
+ *   na_k = n_atoms * mean_{a>b} f_a(Q_k) f_b(Q_k)
+ * Pair sums are accumulated in FP32 (compensated) per tile and reduced in FP64.
+ *
+ * Replaces wrap_fq of cpu_wrappers/flat_multi_cpu_wrap.py:22-60 (same value as
+ * cpu_wrappers/flat_serial_cpu_wrap.py:13-69, cpu_wrappers/nxn_cpu_wrap.py:9-69
+ * and gpu_wrappers/gpu_wrap.py:119-156), i.e. the `self.fq` plug-in of
+ * ElasticScatter (elasticscatter/__init__.py:101, 254, 277).
+ *   positions : device float [n_atoms][3]
+ *   species   : host int32 [n_atoms], values in [0, n_species)
+ *   scatter   : host float [n_species][n_bins]
+ *   fq        : device float [n_bins]
+ * ------------------------------------------------------------------------ */
+int pyiid_fq(pyiid_ctx *ctx, const float *positions, const int32_t *species,
+             int n_atoms, const float *scatter, int n_species, int n_bins,
+             double qbin, int k_begin, float *fq);
+
+/* Gradient of F(Q) in the reference's convention:
+ *   grad[a][c][k] = -(1/na_k) * d S_k / d x_{a,c}  ( = -1/2 * dF_k/dx_{a,c} ),
+ * k in [k_begin, n_bins), NaN -> 0 per element as the reference does.
+ * Replaces wrap_fq_grad of cpu_wrappers/flat_multi_cpu_wrap.py:63-102 (and
+ * flat_serial_cpu_wrap.py:72-133, nxn_cpu_wrap.py:72-137,
+ * gpu_wrappers/gpu_wrap.py:159-194), the `self.grad` plug-in.
+ *   grad : device float [n_atoms][3][n_bins] */
+int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
+                  const int32_t *species, int n_atoms, const float *scatter,
+                  int n_species, int n_bins, double qbin, int k_begin,
+                  float *grad);
+
+/* ------------------------------------------------------------------------ *
+ * F(Q) -> G(r).
+ *
+ * gr[i] = sum_k F'_k T_k(rgrid[i]) where F' is fq with bins below
+ * ceil(qmin/qstep) set to zero and T is the linear map equal to the
+ * reference's zero-padded odd-extension FFT followed by linear interpolation
+ * (kernels/master_kernel.py:39-203, get_pdf_at_qmin / fft_fq_to_gr /
+ * fft_gr_to_fq).  T is built once per (qstep, rstep, qmin, rgrid, n_bins) on
+ * the host in FP64 and cached on the device.
+ *   fq    : device float  [n_configs][n_bins]   (bins from Q = 0)
+ *   rgrid : host double   [n_r]
+ *   gr    : device double [n_configs][n_r]
+ * Replaces get_pdf_at_qmin (kernels/master_kernel.py:39-105). */
+int pyiid_pdf(pyiid_ctx *ctx, const float *fq, int n_configs, int n_bins,
+              double qstep, double rstep, const double *rgrid, int n_r,
+              double qmin, double *gr);
+
+/* Gradient of G(r): the same map applied to each of the 3N rows of a
+ * reference-convention grad_fq.
+ *   grad_fq  : device float  [n_atoms][3][n_bins]
+ *   grad_pdf : device double [n_atoms][3][n_r]
+ * Replaces grad_pdf of kernels/master_kernel.py:276-290 and
+ * gpu_wrappers/gpu_wrap.py:197-284 (the `self.grad_pdf` plug-in). */
+int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
+                   int n_bins, double qstep, double rstep, const double *rgrid,
+                   int n_r, double qmin, double *grad_pdf);
+
+/* ------------------------------------------------------------------------ *
+ * Potentials.
+ *
+ * out[0] = Rw (or chi^2), out[1] = scale, for each of n_configs rows; the
+ * branch for a non-positive scale is the reference's (Rw = 1, scale = 1;
+ * chi^2 uses scale = 1).
+ *   gobs  : device double [n_r] (shared by all configs)
+ *   gcalc : device double [n_configs][n_r]
+ *   out   : device double [n_configs][2]
+ * Replaces get_rw / get_chi_sq / get_scale (kernels/master_kernel.py:206-266,
+ * 388-389) behind wrap_rw / wrap_chi_sq (calc/__init__.py:10-53). */
+int pyiid_potential(pyiid_ctx *ctx, const double *gobs, const double *gcalc,
+                    int n_configs, int n_r, int potential, double *out);
+
+/* Gradient of the potential from an explicit G(r) gradient:
+ *   grad[a][c] = sum_r c_r * grad_pdf[a][c][r]  with the reference's c_r.
+ *   grad_pdf : device double [n_atoms][3][n_r]
+ *   grad     : device double [n_atoms][3]
+ * Replaces get_grad_rw / get_grad_chi_sq / get_grad_scale
+ * (kernels/master_kernel.py:293-376, 392-396) behind wrap_grad_rw /
+ * wrap_grad_chi_sq (calc/__init__.py:56-105). */
+int pyiid_potential_grad(pyiid_ctx *ctx, const double *grad_pdf,
+                         const double *gcalc, const double *gobs, int n_atoms,
+                         int n_r, int potential, double *grad);
+
+/* ------------------------------------------------------------------------ *
+ * Fused potential and adjoint gradient for a batch of configurations.
+ *
+ * For each configuration b (atoms offsets[b] .. offsets[b+1]-1 of the packed
+ * arrays) computes on the PDF grid: F(Q) -> G(r) -> potential, and the exact
+ * gradient d(potential)/d(positions) through the adjoint of the chain
+ * (no [N,3,K] or [N,3,R] intermediate).  The gradient is the TRUE gradient
+ * (the reference's Calc1D forces equal -1/2 * conv * this; see
+ * calc/calc_1d.py:89-95 and cpu_experimental.py:8-15).
+ *   positions : device float  [total_atoms][3]
+ *   species   : host int32    [total_atoms]
+ *   offsets   : host int32    [n_configs + 1]
+ *   scatter   : host float    [n_species][n_bins]
+ *   gobs      : device double [n_r]
+ *   energy    : device double [n_configs][2]  (potential, scale)
+ *   grad      : device float  [total_atoms][3]  (may be NULL: energy only)
+ *   gcalc     : device double [n_configs][n_r]  (may be NULL)
+ *   fq        : device float  [n_configs][n_bins] (may be NULL)
+ * Replaces, for one configuration, the call chain of Calc1D.calculate
+ * (calc/calc_1d.py:44-95) -> get_pdf / get_grad_pdf
+ * (elasticscatter/__init__.py:343-391, 498-524) -> get_rw / get_grad_rw. */
+int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
+                               const int32_t *species, const int32_t *offsets,
+                               int n_configs, const float *scatter,
+                               int n_species, int n_bins, double qstep,
+                               double rstep, const double *rgrid, int n_r,
+                               double qmin, const double *gobs, int potential,
+                               double *energy, float *grad, double *gcalc,
+                               float *fq);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYIID_GB300_H */

@@ -1,0 +1,766 @@
+// capi.cu -- context, host-side layouts and the C ABI of include/pyiid_gb300.h.
+//
+// Host responsibilities (all O(N) or O(K*R), cached by content hash):
+//   * Layout: per configuration, a stable species sort (perm), tiles of at
+//     most 32 atoms that never straddle a (configuration, species) boundary,
+//     the F(Q) work items (tile I, run of tiles J <= I of one species) grouped
+//     by (configuration, species pair), and the pair counts per species pair.
+//   * na(Q): n * mean_{a>b} f_a f_b per configuration in FP64.
+//   * T: the linear map equal to the reference's F -> G FFT transform.
+// Device work is enqueued on the context stream; device buffers only grow.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/pyiid_gb300.h"
+#include "debye_kernels.cuh"
+#include "transform_kernels.cuh"
+
+using namespace pyiid;
+
+namespace {
+
+constexpr int kVersion = 10000;  // 1.0.0
+constexpr int kJMax = 32;        // max J tiles per F(Q) work item
+constexpr int kAdjRS = 64;       // adjoint re-seed period (bins)
+
+uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) {
+  const unsigned char *p = static_cast<const unsigned char *>(data);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+template <class T>
+uint64_t mix(uint64_t h, const T &v) {
+  return fnv1a(&v, sizeof(T), h);
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Layout {
+  uint64_t key = 0;
+  int total = 0, n_configs = 0, n_species = 0, n_spairs = 0;
+  std::vector<int> offsets, perm;
+  std::vector<int4> tiles;
+  std::vector<int2> cfg_tiles;
+  std::vector<int4> items;
+  std::vector<int> key_item_begin;
+  std::vector<int2> spair_species;
+  std::vector<double> pair_counts;  // [n_configs][n_spairs]
+  std::vector<int> natoms;          // per configuration
+  // device copies
+  int *d_perm = nullptr;
+  int4 *d_tiles = nullptr;
+  int2 *d_cfg_tiles = nullptr;
+  int4 *d_items = nullptr;
+  int *d_key_item_begin = nullptr;
+  int2 *d_spair = nullptr;
+};
+
+struct TMatrix {
+  uint64_t key = 0;
+  int n_bins = 0, n_r = 0, kmin = 0;
+  float *d_T = nullptr;
+};
+
+struct NaTable {
+  uint64_t key = 0;
+  double *d_na = nullptr;
+};
+
+std::mutex g_err_mu;
+std::string g_err;  // errors without a context
+
+}  // namespace
+
+struct pyiid_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t launches = 0;
+  std::unordered_map<std::string, DevBuf> bufs;
+  std::vector<std::unique_ptr<Layout>> layouts;  // small LRU (front = newest)
+  std::vector<std::unique_ptr<TMatrix>> tmats;
+  std::vector<std::unique_ptr<NaTable>> nas;
+  uint64_t ftab_key = 0;
+  int ftab_species = 0, ftab_bins = 0;
+  bool attrs_set = false;
+};
+
+namespace {
+
+int fail(pyiid_ctx *ctx, int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) {
+    ctx->err = buf;
+  } else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = buf;
+  }
+  return code;
+}
+
+#define CUDA_TRY(ctx, expr)                                                   \
+  do {                                                                        \
+    cudaError_t e_ = (expr);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? PYIID_ERR_OOM        \
+                                                       : PYIID_ERR_CUDA,      \
+                  "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_),     \
+                  __FILE__, __LINE__);                                        \
+    }                                                                         \
+  } while (0)
+
+#define LAUNCH_CHECK(ctx)                                                     \
+  do {                                                                        \
+    ++(ctx)->launches;                                                        \
+    cudaError_t e_ = cudaGetLastError();                                      \
+    if (e_ != cudaSuccess)                                                    \
+      return fail(ctx, PYIID_ERR_CUDA, "kernel launch failed: %s (%s:%d)",    \
+                  cudaGetErrorString(e_), __FILE__, __LINE__);                \
+  } while (0)
+
+#define TRY(expr)              \
+  do {                         \
+    int rc_ = (expr);          \
+    if (rc_ != PYIID_OK) return rc_; \
+  } while (0)
+
+// Grow-only device buffer by name.
+int ensure(pyiid_ctx *ctx, const char *name, size_t bytes, void **out) {
+  DevBuf &b = ctx->bufs[name];
+  if (b.bytes < bytes) {
+    if (b.p) CUDA_TRY(ctx, cudaFree(b.p));
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t alloc = std::max<size_t>(bytes, 256);
+    CUDA_TRY(ctx, cudaMalloc(&b.p, alloc));
+    b.bytes = alloc;
+  }
+  *out = b.p;
+  return PYIID_OK;
+}
+
+template <class T>
+int upload(pyiid_ctx *ctx, T **dst, const std::vector<T> &src) {
+  if (*dst) CUDA_TRY(ctx, cudaFree(*dst));
+  *dst = nullptr;
+  size_t n = std::max<size_t>(src.size(), 1);
+  CUDA_TRY(ctx, cudaMalloc((void **)dst, n * sizeof(T)));
+  if (!src.empty())
+    CUDA_TRY(ctx, cudaMemcpy(*dst, src.data(), src.size() * sizeof(T),
+                             cudaMemcpyHostToDevice));
+  return PYIID_OK;
+}
+
+void free_layout(Layout *L) {
+  cudaFree(L->d_perm);
+  cudaFree(L->d_tiles);
+  cudaFree(L->d_cfg_tiles);
+  cudaFree(L->d_items);
+  cudaFree(L->d_key_item_begin);
+  cudaFree(L->d_spair);
+}
+
+// Builds (or finds) the layout of a packed batch.
+int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
+               int n_configs, int n_species, Layout **out) {
+  const int total = offsets[n_configs];
+  uint64_t key = fnv1a(offsets, sizeof(int32_t) * (n_configs + 1));
+  key = fnv1a(species, sizeof(int32_t) * (size_t)total, key);
+  key = mix(key, n_species);
+  for (size_t i = 0; i < ctx->layouts.size(); ++i) {
+    if (ctx->layouts[i]->key == key) {
+      if (i != 0) std::swap(ctx->layouts[0], ctx->layouts[i]);
+      *out = ctx->layouts[0].get();
+      return PYIID_OK;
+    }
+  }
+  for (int i = 0; i < total; ++i)
+    if (species[i] < 0 || species[i] >= n_species)
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "species[%d] = %d outside [0, %d)", i, species[i], n_species);
+  auto L = std::make_unique<Layout>();
+  L->key = key;
+  L->total = total;
+  L->n_configs = n_configs;
+  L->n_species = n_species;
+  L->n_spairs = n_species * (n_species + 1) / 2;
+  L->offsets.assign(offsets, offsets + n_configs + 1);
+  L->perm.resize(total);
+  L->cfg_tiles.resize(n_configs);
+  L->natoms.resize(n_configs);
+  L->pair_counts.assign((size_t)n_configs * L->n_spairs, 0.0);
+  for (int sa = 0; sa < n_species; ++sa)
+    for (int sb = 0; sb <= sa; ++sb) L->spair_species.push_back(make_int2(sa, sb));
+  std::vector<int> count(n_species);
+  for (int c = 0; c < n_configs; ++c) {
+    const int o0 = offsets[c], o1 = offsets[c + 1];
+    L->natoms[c] = o1 - o0;
+    std::fill(count.begin(), count.end(), 0);
+    for (int i = o0; i < o1; ++i) count[species[i]]++;
+    std::vector<int> start(n_species, o0);
+    for (int s = 1; s < n_species; ++s) start[s] = start[s - 1] + count[s - 1];
+    std::vector<int> fillp = start;
+    for (int i = o0; i < o1; ++i) L->perm[fillp[species[i]]++] = i;
+    const int t0 = (int)L->tiles.size();
+    for (int s = 0; s < n_species; ++s)
+      for (int a = 0; a < count[s]; a += kTile)
+        L->tiles.push_back(
+            make_int4(start[s] + a, std::min(kTile, count[s] - a), c, s));
+    const int t1 = (int)L->tiles.size();
+    L->cfg_tiles[c] = make_int2(t0, t1);
+    for (int sa = 0; sa < n_species; ++sa)
+      for (int sb = 0; sb <= sa; ++sb) {
+        const double na = count[sa], nb = count[sb];
+        L->pair_counts[(size_t)c * L->n_spairs + sa * (sa + 1) / 2 + sb] =
+            (sa == sb) ? na * (na - 1) / 2 : na * nb;
+      }
+    // F(Q) items: tile I with runs of tiles J <= I of one species
+    for (int I = t0; I < t1; ++I) {
+      int J = t0;
+      while (J <= I) {
+        const int sJ = L->tiles[J].w;
+        int Je = J;
+        while (Je <= I && L->tiles[Je].w == sJ && Je - J < kJMax) ++Je;
+        const int sI = L->tiles[I].w;
+        const int sp = sI * (sI + 1) / 2 + sJ;
+        L->items.push_back(make_int4(I, J, Je, c * L->n_spairs + sp));
+        J = Je;
+      }
+    }
+  }
+  std::stable_sort(L->items.begin(), L->items.end(),
+                   [](const int4 &a, const int4 &b) { return a.w < b.w; });
+  const int nkeys = n_configs * L->n_spairs;
+  L->key_item_begin.assign(nkeys + 1, 0);
+  for (const int4 &it : L->items) L->key_item_begin[it.w + 1]++;
+  for (int k = 0; k < nkeys; ++k) L->key_item_begin[k + 1] += L->key_item_begin[k];
+  TRY(upload(ctx, &L->d_perm, L->perm));
+  TRY(upload(ctx, &L->d_tiles, L->tiles));
+  TRY(upload(ctx, &L->d_cfg_tiles, L->cfg_tiles));
+  TRY(upload(ctx, &L->d_items, L->items));
+  TRY(upload(ctx, &L->d_key_item_begin, L->key_item_begin));
+  TRY(upload(ctx, &L->d_spair, L->spair_species));
+  ctx->layouts.insert(ctx->layouts.begin(), std::move(L));
+  while (ctx->layouts.size() > 4) {
+    free_layout(ctx->layouts.back().get());
+    ctx->layouts.pop_back();
+  }
+  *out = ctx->layouts[0].get();
+  return PYIID_OK;
+}
+
+// Uploads the per-species form factor table if it changed.
+int get_ftab(pyiid_ctx *ctx, const float *scatter, int n_species, int n_bins,
+             float **out) {
+  const size_t n = (size_t)n_species * n_bins;
+  uint64_t key = fnv1a(scatter, n * sizeof(float));
+  key = mix(key, n_species);
+  key = mix(key, n_bins);
+  void *p;
+  TRY(ensure(ctx, "ftab", n * sizeof(float), &p));
+  if (key != ctx->ftab_key) {
+    CUDA_TRY(ctx, cudaMemcpy(p, scatter, n * sizeof(float),
+                             cudaMemcpyHostToDevice));
+    ctx->ftab_key = key;
+  }
+  *out = static_cast<float *>(p);
+  return PYIID_OK;
+}
+
+// na[c][k] = N_c * (sum_sp pairs_sp f_sa f_sb) / P_c  (NaN when P_c == 0,
+// as numpy's mean of an empty array).
+int get_na(pyiid_ctx *ctx, const Layout *L, const float *scatter, int n_bins,
+           double **out) {
+  uint64_t key = mix(L->key, ctx->ftab_key);
+  key = mix(key, n_bins);
+  for (size_t i = 0; i < ctx->nas.size(); ++i)
+    if (ctx->nas[i]->key == key) {
+      *out = ctx->nas[i]->d_na;
+      return PYIID_OK;
+    }
+  std::vector<double> na((size_t)L->n_configs * n_bins);
+  for (int c = 0; c < L->n_configs; ++c) {
+    const double n = L->natoms[c];
+    const double P = n * (n - 1) / 2;
+    for (int k = 0; k < n_bins; ++k) {
+      double s = 0.0;
+      for (int sp = 0; sp < L->n_spairs; ++sp) {
+        const int2 ss = L->spair_species[sp];
+        s += L->pair_counts[(size_t)c * L->n_spairs + sp] *
+             (double)scatter[(size_t)ss.x * n_bins + k] *
+             (double)scatter[(size_t)ss.y * n_bins + k];
+      }
+      na[(size_t)c * n_bins + k] = (P > 0) ? n * s / P : NAN;
+    }
+  }
+  auto T = std::make_unique<NaTable>();
+  T->key = key;
+  TRY(upload(ctx, &T->d_na, na));
+  ctx->nas.insert(ctx->nas.begin(), std::move(T));
+  while (ctx->nas.size() > 4) {
+    cudaFree(ctx->nas.back()->d_na);
+    ctx->nas.pop_back();
+  }
+  *out = ctx->nas[0]->d_na;
+  return PYIID_OK;
+}
+
+// The reference transform (kernels/master_kernel.py:39-203) as a matrix.
+// With F' = F zeroed below kz = ceil(qmin/qstep), padded to
+// len = max(n_bins, ceil(pi/rstep/qstep)), npad2 = 2 * 2^ceil(log2(
+// round(qmin/qstep) + len)), the odd-extended inverse FFT gives
+//   gpad[i] = (qstep/pi) sum_m F'_m sin(2 pi m i / npad2),
+// and the interpolation onto r (drpad = pi/(npad2 qstep), x = r/drpad/2,
+// lo = int(x), w = x - lo) gives G(r) = 2((1-w) gpad[lo] + w gpad[lo+1]), so
+//   T[m][i] = (2 qstep/pi) ((1-w) sin(2 pi m lo/npad2) + w sin(2 pi m (lo+1)/npad2)).
+// The sine arguments use exact integer reduction (m * lo mod npad2).
+int get_tmatrix(pyiid_ctx *ctx, int n_bins, double qstep, double rstep,
+                const double *rgrid, int n_r, double qmin, TMatrix **out) {
+  uint64_t key = fnv1a(rgrid, sizeof(double) * (size_t)n_r);
+  key = mix(key, n_bins);
+  key = mix(key, qstep);
+  key = mix(key, rstep);
+  key = mix(key, qmin);
+  for (size_t i = 0; i < ctx->tmats.size(); ++i)
+    if (ctx->tmats[i]->key == key) {
+      *out = ctx->tmats[i].get();
+      return PYIID_OK;
+    }
+  if (!(qstep > 0) || !(rstep > 0))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "qstep and rstep must be > 0");
+  const int kz = (int)std::ceil(qmin / qstep);
+  const long nfromdr = (long)std::ceil(M_PI / rstep / qstep);
+  const long len = std::max<long>(n_bins, nfromdr);
+  const long padrmin = (long)std::nearbyint(qmin / qstep);  // ties to even
+  const long npad1 = padrmin + len;
+  const long npad2 =
+      (1L << (long)std::ceil(std::log((double)npad1) / std::log(2.0))) * 2;
+  const double drpad = M_PI / ((double)npad2 * qstep);
+  std::vector<float> T((size_t)n_bins * n_r, 0.f);
+  for (int i = 0; i < n_r; ++i) {
+    const double x = rgrid[i] / drpad / 2;
+    const long lo = (long)x;  // truncation, as numpy astype(int)
+    const double w = x - (double)lo;
+    if (lo < 0 || lo + 1 >= npad2)
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "r = %g is outside the transform range", rgrid[i]);
+    for (int m = std::max(kz, 0); m < n_bins; ++m) {
+      const long a = (long)(((__int128)m * lo) % npad2);
+      const long b = (long)(((__int128)m * (lo + 1)) % npad2);
+      const double sa = std::sin(2.0 * M_PI * (double)a / (double)npad2);
+      const double sb = std::sin(2.0 * M_PI * (double)b / (double)npad2);
+      T[(size_t)m * n_r + i] =
+          (float)(2.0 * qstep / M_PI * ((1.0 - w) * sa + w * sb));
+    }
+  }
+  auto M = std::make_unique<TMatrix>();
+  M->key = key;
+  M->n_bins = n_bins;
+  M->n_r = n_r;
+  M->kmin = std::max(kz, 0);
+  TRY(upload(ctx, &M->d_T, T));
+  ctx->tmats.insert(ctx->tmats.begin(), std::move(M));
+  while (ctx->tmats.size() > 4) {
+    cudaFree(ctx->tmats.back()->d_T);
+    ctx->tmats.pop_back();
+  }
+  *out = ctx->tmats[0].get();
+  return PYIID_OK;
+}
+
+void split_double(double x, float &hi, float &lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
+int set_attrs(pyiid_ctx *ctx) {
+  if (ctx->attrs_set) return PYIID_OK;
+  CUDA_TRY(ctx, cudaFuncSetAttribute(gradfq_kernel<32>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     3 * kTile * kTile * 16));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(fq_pair_kernel<32>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     2 * kTile * kTile * 16 + 2 * 32 * kBlock * 4));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(adjoint_kernel<kAdjRS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     160 * 1024));
+  ctx->attrs_set = true;
+  return PYIID_OK;
+}
+
+int check_common(pyiid_ctx *ctx, int n_configs, const int32_t *offsets,
+                 int n_species, int n_bins, double qbin, int k_begin) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_configs < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_configs < 1");
+  if (offsets[0] != 0)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "offsets[0] must be 0");
+  for (int c = 0; c < n_configs; ++c)
+    if (offsets[c + 1] < offsets[c])
+      return fail(ctx, PYIID_ERR_INVALID_ARG, "offsets must be non-decreasing");
+  if (n_species < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_species < 1");
+  if (n_bins < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_bins < 1");
+  if (n_bins > (1 << 24))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "n_bins > 2^24 is not supported");
+  if (!(qbin > 0) || !std::isfinite(qbin))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "qbin must be a positive number");
+  if (k_begin < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "k_begin < 0");
+  return PYIID_OK;
+}
+
+// Pair sums + finishing: fq[c][k] for k in [k_begin, n_bins) (zero below).
+int run_fq(pyiid_ctx *ctx, const Layout *L, const float *positions,
+           const float *d_ftab, const double *d_na, int n_bins, double qbin,
+           int k_begin, float *fq, double *fq_raw) {
+  float dq_hi, dq_lo;
+  split_double(qbin, dq_hi, dq_lo);
+  const int kb0 = std::min(k_begin, n_bins) & ~1;
+  const int n_items = (int)L->items.size();
+  double *partial = nullptr;
+  if (n_items > 0 && kb0 < n_bins) {
+    constexpr int Lb = 32;
+    const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    const int n_cb = (chunks_total + 127) / 128;
+    const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
+    const int n_groups = kBlock / n_chunks;
+    void *p;
+    TRY(ensure(ctx, "fq_partial", (size_t)n_items * n_bins * sizeof(double), &p));
+    partial = static_cast<double *>(p);
+    // records (reused by the FP64 group reduction) + per-thread Kahan state
+    const size_t smem = 2 * kTile * kTile * sizeof(float4) +
+                        2 * (size_t)Lb * kBlock * sizeof(float);
+    dim3 grid(n_items, n_cb);
+    fq_pair_kernel<Lb><<<grid, kBlock, smem, ctx->stream>>>(
+        positions, L->d_perm, L->d_tiles, L->d_items, dq_hi, dq_lo, kb0,
+        n_chunks, n_groups, n_bins, partial);
+    LAUNCH_CHECK(ctx);
+  }
+  dim3 g2((n_bins + 127) / 128, L->n_configs);
+  const int kb_out = (n_items > 0) ? std::min(k_begin, n_bins) : n_bins;
+  fq_finish_kernel<<<g2, 128, 0, ctx->stream>>>(
+      partial, L->d_key_item_begin, d_ftab, L->d_spair, d_na, L->n_spairs,
+      n_bins, kb_out, fq, fq_raw);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int batch_fq(pyiid_ctx *ctx, const float *positions, const int32_t *species,
+             const int32_t *offsets, int n_configs, const float *scatter,
+             int n_species, int n_bins, double qbin, int k_begin, float *fq) {
+  TRY(check_common(ctx, n_configs, offsets, n_species, n_bins, qbin, k_begin));
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  Layout *L;
+  TRY(get_layout(ctx, species, offsets, n_configs, n_species, &L));
+  float *d_ftab;
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, &d_ftab));
+  double *d_na;
+  TRY(get_na(ctx, L, scatter, n_bins, &d_na));
+  return run_fq(ctx, L, positions, d_ftab, d_na, n_bins, qbin, k_begin, fq,
+                nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pyiid_version(void) { return kVersion; }
+
+int pyiid_create(pyiid_ctx **out, int device) {
+  if (!out) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null output pointer");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(nullptr, PYIID_ERR_CUDA, "no CUDA device: %s",
+                e == cudaSuccess ? "device count is 0" : cudaGetErrorString(e));
+  if (device < 0 || device >= n)
+    return fail(nullptr, PYIID_ERR_INVALID_ARG, "device %d outside [0, %d)",
+                device, n);
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess)
+    return fail(nullptr, PYIID_ERR_CUDA, "cudaGetDeviceProperties: %s",
+                cudaGetErrorString(e));
+  if (prop.major * 10 + prop.minor != 103)
+    return fail(nullptr, PYIID_ERR_CUDA,
+                "device %d is sm_%d%d; this library is built for sm_103a only",
+                device, prop.major, prop.minor);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess)
+    return fail(nullptr, PYIID_ERR_CUDA, "cudaSetDevice: %s",
+                cudaGetErrorString(e));
+  pyiid_ctx *ctx = new (std::nothrow) pyiid_ctx();
+  if (!ctx) return fail(nullptr, PYIID_ERR_OOM, "out of host memory");
+  ctx->device = device;
+  *out = ctx;
+  return PYIID_OK;
+}
+
+int pyiid_destroy(pyiid_ctx *ctx) {
+  if (!ctx) return PYIID_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->bufs) cudaFree(kv.second.p);
+  for (auto &L : ctx->layouts) free_layout(L.get());
+  for (auto &T : ctx->tmats) cudaFree(T->d_T);
+  for (auto &N : ctx->nas) cudaFree(N->d_na);
+  delete ctx;
+  return PYIID_OK;
+}
+
+int pyiid_set_stream(pyiid_ctx *ctx, void *stream) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return PYIID_OK;
+}
+
+int pyiid_synchronize(pyiid_ctx *ctx) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return PYIID_OK;
+}
+
+const char *pyiid_last_error(const pyiid_ctx *ctx) {
+  if (ctx) return ctx->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_err.c_str();
+}
+
+int64_t pyiid_launch_count(const pyiid_ctx *ctx) {
+  return ctx ? ctx->launches : -1;
+}
+
+int pyiid_fq(pyiid_ctx *ctx, const float *positions, const int32_t *species,
+             int n_atoms, const float *scatter, int n_species, int n_bins,
+             double qbin, int k_begin, float *fq) {
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  const int32_t offsets[2] = {0, n_atoms};
+  return batch_fq(ctx, positions, species, offsets, 1, scatter, n_species,
+                  n_bins, qbin, k_begin, fq);
+}
+
+int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
+                  const int32_t *species, int n_atoms, const float *scatter,
+                  int n_species, int n_bins, double qbin, int k_begin,
+                  float *grad) {
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  const int32_t offsets[2] = {0, n_atoms};
+  TRY(check_common(ctx, 1, offsets, n_species, n_bins, qbin, k_begin));
+  if (n_atoms == 0) return PYIID_OK;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  Layout *L;
+  TRY(get_layout(ctx, species, offsets, 1, n_species, &L));
+  float *d_ftab;
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, &d_ftab));
+  double *d_na;
+  TRY(get_na(ctx, L, scatter, n_bins, &d_na));
+  const int kbo = std::min(k_begin, n_bins);
+  const int kb0 = kbo & ~1;
+  void *p;
+  TRY(ensure(ctx, "coef",
+             (size_t)n_species * n_species * n_bins * sizeof(float), &p));
+  float *coef = static_cast<float *>(p);
+  gradfq_coef_kernel<<<64, 256, 0, ctx->stream>>>(d_na, d_ftab, n_species,
+                                                  n_bins, 1, coef);
+  LAUNCH_CHECK(ctx);
+  if (kb0 < n_bins) {
+    constexpr int Lb = 32;
+    const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    const int cpc = 8;
+    float dq_hi, dq_lo;
+    split_double(qbin, dq_hi, dq_lo);
+    dim3 grid((unsigned)L->tiles.size(), (chunks_total + cpc - 1) / cpc);
+    gradfq_kernel<Lb><<<grid, kTile * cpc, 3 * kTile * kTile * 16,
+                        ctx->stream>>>(
+        positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
+        chunks_total, cpc, n_bins, coef, n_species, grad);
+    LAUNCH_CHECK(ctx);
+  }
+  if (kbo > 0)
+    CUDA_TRY(ctx, cudaMemset2DAsync(grad, (size_t)n_bins * sizeof(float), 0,
+                                    (size_t)kbo * sizeof(float),
+                                    (size_t)3 * n_atoms, ctx->stream));
+  return PYIID_OK;
+}
+
+int pyiid_pdf(pyiid_ctx *ctx, const float *fq, int n_configs, int n_bins,
+              double qstep, double rstep, const double *rgrid, int n_r,
+              double qmin, double *gr) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_configs < 1 || n_bins < 1 || n_r < 0)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  if (n_r == 0) return PYIID_OK;
+  if (n_bins > 12288)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "n_bins > 12288 is not supported");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TMatrix *T;
+  TRY(get_tmatrix(ctx, n_bins, qstep, rstep, rgrid, n_r, qmin, &T));
+  dim3 grid((n_r + 255) / 256, n_configs);
+  pdf_kernel<<<grid, 256, n_bins * sizeof(float), ctx->stream>>>(
+      fq, T->d_T, n_bins, n_r, T->kmin, gr);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
+                   int n_bins, double qstep, double rstep, const double *rgrid,
+                   int n_r, double qmin, double *grad_pdf) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_atoms < 0 || n_bins < 1 || n_r < 0)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  if (n_atoms == 0 || n_r == 0) return PYIID_OK;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TMatrix *T;
+  TRY(get_tmatrix(ctx, n_bins, qstep, rstep, rgrid, n_r, qmin, &T));
+  const int rows = 3 * n_atoms;
+  dim3 grid((n_r + 127) / 128, (rows + 127) / 128);
+  gemm_rows_T_kernel<<<grid, 256, 0, ctx->stream>>>(grad_fq, T->d_T, rows,
+                                                    n_bins, n_r, T->kmin,
+                                                    grad_pdf);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int pyiid_potential(pyiid_ctx *ctx, const double *gobs, const double *gcalc,
+                    int n_configs, int n_r, int potential, double *out) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_configs < 1 || n_r < 1)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  if (potential != PYIID_POTENTIAL_RW && potential != PYIID_POTENTIAL_CHI_SQ)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "unknown potential %d", potential);
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  potential_kernel<<<n_configs, 256, 0, ctx->stream>>>(gobs, gcalc, n_r,
+                                                       potential, out, nullptr);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int pyiid_potential_grad(pyiid_ctx *ctx, const double *grad_pdf,
+                         const double *gcalc, const double *gobs, int n_atoms,
+                         int n_r, int potential, double *grad) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_atoms < 0 || n_r < 1)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  if (potential != PYIID_POTENTIAL_RW && potential != PYIID_POTENTIAL_CHI_SQ)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "unknown potential %d", potential);
+  if (n_atoms == 0) return PYIID_OK;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  void *p;
+  TRY(ensure(ctx, "energy1", 2 * sizeof(double), &p));
+  double *e = static_cast<double *>(p);
+  TRY(ensure(ctx, "cvec", (size_t)n_r * sizeof(float), &p));
+  float *cvec = static_cast<float *>(p);
+  potential_kernel<<<1, 256, 0, ctx->stream>>>(gobs, gcalc, n_r, potential, e,
+                                               cvec);
+  LAUNCH_CHECK(ctx);
+  const int rows = 3 * n_atoms;
+  potential_grad_rows_kernel<<<(rows * 32 + 255) / 256, 256, 0, ctx->stream>>>(
+      grad_pdf, cvec, rows, n_r, grad);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
+                               const int32_t *species, const int32_t *offsets,
+                               int n_configs, const float *scatter,
+                               int n_species, int n_bins, double qstep,
+                               double rstep, const double *rgrid, int n_r,
+                               double qmin, const double *gobs, int potential,
+                               double *energy, float *grad, double *gcalc,
+                               float *fq) {
+  TRY(check_common(ctx, n_configs, offsets, n_species, n_bins, qstep, 0));
+  if (n_r < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_r < 1");
+  if (n_bins > 12288)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "n_bins > 12288 is not supported");
+  if (potential != PYIID_POTENTIAL_RW && potential != PYIID_POTENTIAL_CHI_SQ)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "unknown potential %d", potential);
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  Layout *L;
+  TRY(get_layout(ctx, species, offsets, n_configs, n_species, &L));
+  float *d_ftab;
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, &d_ftab));
+  double *d_na;
+  TRY(get_na(ctx, L, scatter, n_bins, &d_na));
+  TMatrix *T;
+  TRY(get_tmatrix(ctx, n_bins, qstep, rstep, rgrid, n_r, qmin, &T));
+  const int kmin = T->kmin;
+  void *p;
+  float *d_fq = fq;
+  if (!d_fq) {
+    TRY(ensure(ctx, "b_fq", (size_t)n_configs * n_bins * sizeof(float), &p));
+    d_fq = static_cast<float *>(p);
+  }
+  double *d_gc = gcalc;
+  if (!d_gc) {
+    TRY(ensure(ctx, "b_gcalc", (size_t)n_configs * n_r * sizeof(double), &p));
+    d_gc = static_cast<double *>(p);
+  }
+  TRY(run_fq(ctx, L, positions, d_ftab, d_na, n_bins, qstep, kmin, d_fq,
+             nullptr));
+  dim3 gp((n_r + 255) / 256, n_configs);
+  pdf_kernel<<<gp, 256, n_bins * sizeof(float), ctx->stream>>>(
+      d_fq, T->d_T, n_bins, n_r, kmin, d_gc);
+  LAUNCH_CHECK(ctx);
+  float *cvec = nullptr;
+  if (grad) {
+    TRY(ensure(ctx, "b_cvec", (size_t)n_configs * n_r * sizeof(float), &p));
+    cvec = static_cast<float *>(p);
+  }
+  potential_kernel<<<n_configs, 256, 0, ctx->stream>>>(gobs, d_gc, n_r,
+                                                       potential, energy, cvec);
+  LAUNCH_CHECK(ctx);
+  if (!grad || L->total == 0) return PYIID_OK;
+  TRY(ensure(ctx, "b_w", (size_t)n_configs * n_bins * sizeof(double), &p));
+  double *w = static_cast<double *>(p);
+  const int nwarps = n_configs * n_bins;
+  wvec_kernel<<<(nwarps * 32 + 255) / 256, 256, 0, ctx->stream>>>(
+      T->d_T, cvec, n_bins, n_r, kmin, n_configs, w);
+  LAUNCH_CHECK(ctx);
+  const int kb0 = kmin & ~1;
+  const int kp = std::max(kAdjRS, ((n_bins - kb0 + kAdjRS - 1) / kAdjRS) * kAdjRS);
+  const size_t ntab = (size_t)n_configs * n_species * n_species * 2 * kp;
+  TRY(ensure(ctx, "b_tabs", ntab * sizeof(float2), &p));
+  float2 *tabs = static_cast<float2 *>(p);
+  adjoint_table_kernel<<<256, 256, 0, ctx->stream>>>(
+      w, d_na, d_ftab, n_species, n_bins, kmin, kb0, kp, n_configs, tabs);
+  LAUNCH_CHECK(ctx);
+  float dq_hi, dq_lo;
+  split_double(qstep, dq_hi, dq_lo);
+  const size_t smem = (size_t)n_species * 2 * kp * sizeof(float2);
+  if (smem > 160 * 1024)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "adjoint tables (%zu bytes) exceed shared memory", smem);
+  if (!L->tiles.empty()) {
+    adjoint_kernel<kAdjRS><<<(unsigned)L->tiles.size(), kBlock, smem,
+                             ctx->stream>>>(positions, L->d_perm, L->d_tiles,
+                                            L->d_cfg_tiles, dq_hi, dq_lo, kb0,
+                                            kp, tabs, n_species, grad);
+    LAUNCH_CHECK(ctx);
+  }
+  return PYIID_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,454 @@
+// debye_kernels.cuh -- pair-tiled Debye kernels for sm_103a.
+//
+// Atoms of every configuration are sorted by species and cut into tiles of at
+// most kTile atoms that never straddle a (configuration, species) boundary, so
+// every tile pair has one species pair and the form factors factor out of the
+// pair loops:
+//   S_k = sum_{sa>=sb} f_sa(Q_k) f_sb(Q_k) D^{sa sb}_k,
+//   D^{sa sb}_k = sum over pairs of that species pair of sin(Q_k r)/r.
+// The kernels therefore never read form factors in their inner loops; the
+// small finishing kernels apply them.
+#pragma once
+
+#include "pair_math.cuh"
+
+namespace pyiid {
+
+constexpr int kTile = 32;    // atoms per tile
+constexpr int kBlock = 256;  // threads per CTA of the pair kernels
+
+// Tile descriptor: start (in sorted order), atom count, configuration, species.
+// (stored as int4)
+
+// Triangular index q in [0, n(n-1)/2) -> (a, b), a > b.
+__device__ __forceinline__ void tri_index(int q, int &a, int &b) {
+  int ai = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)q)) * 0.5f);
+  while (ai * (ai - 1) / 2 > q) --ai;
+  while ((ai + 1) * ai / 2 <= q) ++ai;
+  a = ai;
+  b = q - ai * (ai - 1) / 2;
+}
+
+__device__ __forceinline__ float4 load_atom(const float *__restrict__ pos,
+                                            const int *__restrict__ perm,
+                                            int sorted_index) {
+  int o = perm[sorted_index];
+  return make_float4(pos[3 * o], pos[3 * o + 1], pos[3 * o + 2], 0.f);
+}
+
+// ===================================================================== F(Q)
+// One CTA per work item (tile I, tiles [J0, J1) of one species pair).  Thread
+// (chunk c, group g) accumulates bins [kbase, kbase+L) over the pairs q = g,
+// g + n_groups, ... of every tile pair.  Per pair the record holds
+//   a = (th_hi, th_lo, lambda, sigma)
+//   b = (sin_th / r, -lambda / (2 r), 1 / r, 0)
+// so that the recurrence runs on t_k = sin(k theta_e) / r directly.
+// Per bin and pair: FFMA + FADD (recurrence) + FADD/FFMA (accumulate).
+// Per tile pair the FP32 register sums are folded into a Kahan-compensated
+// FP32 accumulator kept in shared memory (two floats per bin and thread); the
+// CTA reduces its groups in FP64 and writes one partial row.
+// Dynamic shared memory: 2*32*32 float4 records + 2*L*blockDim floats; the
+// final FP64 reduction reuses the record space (n_chunks*L doubles <= 32 KB).
+template <int L>
+__global__ void __launch_bounds__(kBlock, 2)
+    fq_pair_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                   const int4 *__restrict__ tiles,
+                   const int4 *__restrict__ items, float dq_hi, float dq_lo,
+                   int kb0, int n_chunks, int n_groups, int n_bins,
+                   double *__restrict__ partial) {
+  extern __shared__ float4 smem[];
+  float4 *recA = smem;
+  float4 *recB = smem + kTile * kTile;
+  // per-thread Kahan sum and compensation, [j][thread] (conflict-free)
+  float *kS = reinterpret_cast<float *>(smem + 2 * kTile * kTile);
+  float *kC = kS + L * blockDim.x;
+  __shared__ float4 sI[kTile], sJ[kTile];
+
+  const int4 it = items[blockIdx.x];
+  const int4 ti = tiles[it.x];
+  const int tid = threadIdx.x;
+  const int c = tid % n_chunks;
+  const int g = tid / n_chunks;
+  const bool active = g < n_groups;
+  const int kbase = kb0 + (blockIdx.y * n_chunks + c) * L;
+  const float kf = (float)kbase;
+
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+
+#pragma unroll
+  for (int j = 0; j < L; ++j) {
+    kS[j * blockDim.x + tid] = 0.f;
+    kC[j * blockDim.x + tid] = 0.f;
+  }
+
+  for (int tj = it.y; tj < it.z; ++tj) {
+    const int4 tJ = tiles[tj];
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool diag = (tj == it.x);
+    const int np = diag ? ti.y * (ti.y - 1) / 2 : ti.y * tJ.y;
+    for (int q = tid; q < np; q += blockDim.x) {
+      int a, b;
+      if (diag) {
+        tri_index(q, a, b);
+      } else {
+        a = q / tJ.y;
+        b = q - a * tJ.y;
+      }
+      const float4 pa = sI[a];
+      const float4 pb = diag ? sI[b] : sJ[b];
+      float dx, dy, dz;
+      PairPhase p = pair_phase(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                               dq_lo, dx, dy, dz);
+      recA[q] = make_float4(p.th_hi, p.th_lo, p.lam, p.sigma);
+      recB[q] = make_float4(p.sin_th * p.inv_r, -0.5f * p.lam * p.inv_r,
+                            p.inv_r, 0.f);
+    }
+    __syncthreads();
+    if (active) {
+      float acc[L];
+#pragma unroll
+      for (int j = 0; j < L; ++j) acc[j] = 0.f;
+      for (int q = g; q < np; q += n_groups) {
+        const float4 ra = recA[q];
+        const float4 rb = recB[q];
+        float s0, c0;
+        seed_sincos(kf, ra.x, ra.y, s0, c0);
+        float t = rb.z * s0;
+        float v = fmaf(rb.x, c0, rb.y * s0);
+        acc[0] += t;
+#pragma unroll
+        for (int j = 1; j < L; ++j) {
+          v = fmaf(ra.z, t, v);
+          t = t + v;
+          if (j & 1)
+            acc[j] = fmaf(t, ra.w, acc[j]);
+          else
+            acc[j] += t;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const float Sj = kS[j * blockDim.x + tid];
+        const float y = __fsub_rn(acc[j], kC[j * blockDim.x + tid]);
+        const float s = __fadd_rn(Sj, y);
+        kC[j * blockDim.x + tid] = __fsub_rn(__fsub_rn(s, Sj), y);
+        kS[j * blockDim.x + tid] = s;
+      }
+    }
+  }
+
+  // reduce the groups of each chunk in FP64 (the record buffer is dead now)
+  __syncthreads();
+  double *red = reinterpret_cast<double *>(smem);
+  for (int gg = 0; gg < n_groups; ++gg) {
+    if (active && g == gg) {
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const double v = (double)kS[j * blockDim.x + tid] -
+                         (double)kC[j * blockDim.x + tid];
+        red[c * L + j] = (gg == 0) ? v : red[c * L + j] + v;
+      }
+    }
+    __syncthreads();
+  }
+  const int nk = n_chunks * L;
+  const int kfirst = kb0 + blockIdx.y * nk;
+  double *out = partial + (size_t)blockIdx.x * n_bins;
+  for (int i = tid; i < nk; i += blockDim.x) {
+    const int k = kfirst + i;
+    if (k < n_bins) out[k] = red[i];
+  }
+}
+
+// Finishing kernel for F(Q): for configuration b and bin k
+//   S_k  = sum_sp f_sa f_sb sum_{items of key (b, sp)} partial[item][k]
+//   F_k  = 2 * nan_to_num(float(S_k / na_k))
+// na is precomputed per (config, bin) on the host in FP64 (it depends only on
+// species counts and form factors).  Configurations with < 2 atoms give 0.
+__global__ void fq_finish_kernel(const double *__restrict__ partial,
+                                 const int *__restrict__ key_item_begin,
+                                 const float *__restrict__ ftab,
+                                 const int2 *__restrict__ spair_species,
+                                 const double *__restrict__ na, int n_spairs,
+                                 int n_bins, int kb_out, float *__restrict__ fq,
+                                 double *__restrict__ fq_raw) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (k >= n_bins) return;
+  float outv = 0.f;
+  double sraw = 0.0;
+  if (k >= kb_out) {
+    double s = 0.0;
+    for (int sp = 0; sp < n_spairs; ++sp) {
+      const int key = b * n_spairs + sp;
+      const int i0 = key_item_begin[key], i1 = key_item_begin[key + 1];
+      if (i0 == i1) continue;
+      double d = 0.0;
+      for (int i = i0; i < i1; ++i) d += partial[(size_t)i * n_bins + k];
+      const int2 ss = spair_species[sp];
+      s += (double)ftab[ss.x * n_bins + k] * (double)ftab[ss.y * n_bins + k] *
+           d;
+    }
+    sraw = s;
+    const double nak = na[(size_t)b * n_bins + k];
+    // the reference divides float32 by float32 and nan_to_num's the result
+    float v = (float)s / (float)nak;
+    if (isnan(v)) v = 0.f;
+    if (isinf(v)) v = v > 0.f ? 3.402823466e38f : -3.402823466e38f;
+    outv = 2.0f * v;
+    if (isinf(outv)) outv = outv > 0.f ? 3.402823466e38f : -3.402823466e38f;
+  }
+  if (fq) fq[(size_t)b * n_bins + k] = outv;
+  if (fq_raw) fq_raw[(size_t)b * n_bins + k] = sraw;
+}
+
+// ==================================================================== dF/dx
+// Owner-computes: CTA (tile I, chunk block) with threads (atom a, chunk cl);
+// every thread sweeps all tiles J of its configuration and accumulates the
+// 3 x L gradient bins of its atom, so no atomics or partials are needed.
+// Records per (a in I, b in J):
+//   a = (th_hi, th_lo, lambda, sigma)
+//   b = (beta sin_th, -beta lambda / 2, beta, gamma')   beta = -1/r^3,
+//                                                        gamma' = -r dq/(2 sin_th)
+//   c = (dx, dy, dz, 0)
+// With t, v scaled by beta, per bin
+//   g_k = sigma^k (k gamma' (v_k + v_{k+1}) + t_k) = (Q_k cos(Q_k r) - sin(Q_k r)/r)/r^2.
+// Per bin and ordered pair: 2 (recurrence) + 1 (u) + 1 (k gamma') + 1 (g) +
+// 3 (accumulate) = 8 FP32 instructions.
+// At every species change of J (and at the end) the thread folds
+// coef[b][sa][sb][k] * acc into its own output rows.
+template <int L>
+__global__ void __launch_bounds__(kBlock, 2)
+    gradfq_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                  const int4 *__restrict__ tiles,
+                  const int2 *__restrict__ cfg_tiles, float dq_hi,
+                  float dq_lo, int kb0, int chunks_total, int chunks_per_cta,
+                  int n_bins, const float *__restrict__ coef, int n_species,
+                  float *__restrict__ out) {
+  extern __shared__ float4 smem[];
+  float4 *recA = smem;
+  float4 *recB = smem + kTile * kTile;
+  float4 *recC = smem + 2 * kTile * kTile;
+  __shared__ float4 sI[kTile], sJ[kTile];
+
+  const int4 ti = tiles[blockIdx.x];
+  const int2 ct = cfg_tiles[ti.z];
+  const int tid = threadIdx.x;
+  const int al = tid / chunks_per_cta;
+  const int chunk = blockIdx.y * chunks_per_cta + tid % chunks_per_cta;
+  const bool active = (al < ti.y) && (chunk < chunks_total);
+  const int kbase = kb0 + chunk * L;
+  const float kf = (float)kbase;
+
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+
+  float ax[L], ay[L], az[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) {
+    ax[j] = 0.f;
+    ay[j] = 0.f;
+    az[j] = 0.f;
+  }
+  int cur_sb = -1;
+  bool first_flush = true;
+  const int out_row = active ? perm[ti.x + al] : 0;
+
+  auto flush = [&](int sb, bool last) {
+    if (!active) return;
+    const float *cf =
+        coef + (((size_t)ti.z * n_species + ti.w) * n_species + sb) * n_bins;
+    float *o = out + (size_t)out_row * 3 * n_bins;
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      const int k = kbase + j;
+      if (k < n_bins) {
+        const float w = cf[k];
+        float vx = w * ax[j], vy = w * ay[j], vz = w * az[j];
+        if (!first_flush) {
+          vx += o[k];
+          vy += o[n_bins + k];
+          vz += o[2 * n_bins + k];
+        }
+        if (last) {
+          vx = isnan(vx) ? 0.f : (isinf(vx) ? copysignf(3.402823466e38f, vx) : vx);
+          vy = isnan(vy) ? 0.f : (isinf(vy) ? copysignf(3.402823466e38f, vy) : vy);
+          vz = isnan(vz) ? 0.f : (isinf(vz) ? copysignf(3.402823466e38f, vz) : vz);
+        }
+        o[k] = vx;
+        o[n_bins + k] = vy;
+        o[2 * n_bins + k] = vz;
+      }
+      ax[j] = 0.f;
+      ay[j] = 0.f;
+      az[j] = 0.f;
+    }
+    first_flush = false;
+  };
+
+  for (int tj = ct.x; tj < ct.y; ++tj) {
+    const int4 tJ = tiles[tj];
+    if (cur_sb >= 0 && tJ.w != cur_sb) flush(cur_sb, false);
+    cur_sb = tJ.w;
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool same = (tj == (int)blockIdx.x);
+    for (int q = tid; q < kTile * kTile; q += blockDim.x) {
+      const int a = q / kTile, b = q % kTile;
+      float4 ra = make_float4(0.f, 0.f, 0.f, 1.f);
+      float4 rb = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (a < ti.y && b < tJ.y && !(same && a == b)) {
+        const float4 pa = sI[a];
+        const float4 pb = sJ[b];
+        float dx, dy, dz;
+        PairPhase p = pair_phase(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                 dq_lo, dx, dy, dz);
+        const float beta = -(p.inv_r * p.inv_r * p.inv_r);
+        const float gam = -p.r * dq_hi / (2.0f * p.sin_th);
+        ra = make_float4(p.th_hi, p.th_lo, p.lam, p.sigma);
+        rb = make_float4(beta * p.sin_th, -0.5f * p.lam * beta, beta, gam);
+        rc = make_float4(dx, dy, dz, 0.f);
+      }
+      recA[q] = ra;
+      recB[q] = rb;
+      recC[q] = rc;
+    }
+    __syncthreads();
+    if (active) {
+      for (int b = 0; b < tJ.y; ++b) {
+        const int q = al * kTile + b;
+        const float4 ra = recA[q];
+        const float4 rb = recB[q];
+        const float4 rc = recC[q];
+        float s0, c0;
+        seed_sincos(kf, ra.x, ra.y, s0, c0);
+        float t = rb.z * s0;
+        float v = fmaf(rb.x, c0, rb.y * s0);
+        float kg = kf * rb.w;
+        const float sx = ra.w * rc.x, sy = ra.w * rc.y, sz = ra.w * rc.z;
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+          const float vn = fmaf(ra.z, t, v);
+          const float u = v + vn;
+          const float gk = fmaf(kg, u, t);
+          if (j & 1) {
+            ax[j] = fmaf(gk, sx, ax[j]);
+            ay[j] = fmaf(gk, sy, ay[j]);
+            az[j] = fmaf(gk, sz, az[j]);
+          } else {
+            ax[j] = fmaf(gk, rc.x, ax[j]);
+            ay[j] = fmaf(gk, rc.y, ay[j]);
+            az[j] = fmaf(gk, rc.z, az[j]);
+          }
+          t = t + vn;
+          v = vn;
+          kg += rb.w;
+        }
+      }
+    }
+  }
+  if (cur_sb >= 0) flush(cur_sb, true);
+}
+
+// =================================================================== adjoint
+// d(potential)/dx_a = sum_b (x_a - x_b) s_ab,  s_ab = sum_k W^{sa sb}_k g_k(r_ab)
+// with W_k = 2 w_k f_sa f_sb / na_k and w = T c the back-projected G(r)
+// adjoint.  Owner-computes: CTA = tile I, thread (atom a = lane, group =
+// warp); group gp handles b = gp, gp + 8, ... of every tile J, so the lanes of
+// a warp share b and the weight tables are broadcast reads.
+// Tables hold, for sigma = +1 and -1, A_k = k W_k sigma^k, B_k = W_k sigma^k as
+// float2, padded with zeros to kp bins (a multiple of the re-seed period RS):
+//   s_ab = gamma' sum_k A_k (v_k + v_{k+1}) + sum_k B_k t_k   (t, v scaled by beta)
+// Per bin and ordered pair: 2 (recurrence) + 1 (u) + 2 (accumulate) FP32
+// instructions and half an LDS.128.
+template <int RS>
+__global__ void __launch_bounds__(kBlock)
+    adjoint_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                   const int4 *__restrict__ tiles,
+                   const int2 *__restrict__ cfg_tiles, float dq_hi,
+                   float dq_lo, int kb0, int kp,
+                   const float2 *__restrict__ tabs, int n_species,
+                   float *__restrict__ grad) {
+  extern __shared__ float2 stab[];  // [n_species][2][kp]
+  __shared__ float4 sI[kTile], sJ[kTile];
+  __shared__ float sred[kBlock / kTile][kTile][3];
+
+  const int4 ti = tiles[blockIdx.x];
+  const int2 ct = cfg_tiles[ti.z];
+  const int tid = threadIdx.x;
+  const int lane = tid % kTile;
+  const int grp = tid / kTile;
+  const int ngrp = blockDim.x / kTile;
+
+  // this tile's tables: [sb][sigma][kp] for (config, sa)
+  const float2 *src =
+      tabs + ((size_t)ti.z * n_species + ti.w) * n_species * 2 * kp;
+  for (int i = tid; i < n_species * 2 * kp; i += blockDim.x) stab[i] = src[i];
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+
+  float gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int tj = ct.x; tj < ct.y; ++tj) {
+    const int4 tJ = tiles[tj];
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool same = (tj == (int)blockIdx.x);
+    const float2 *tb = stab + (size_t)tJ.w * 2 * kp;
+    if (lane < ti.y) {
+      const float4 pa = sI[lane];
+      for (int b = grp; b < tJ.y; b += ngrp) {
+        if (same && b == lane) continue;
+        const float4 pb = sJ[b];
+        float dx, dy, dz;
+        PairPhase p = pair_phase(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                 dq_lo, dx, dy, dz);
+        const float beta = -(p.inv_r * p.inv_r * p.inv_r);
+        const float c1 = beta * p.sin_th;
+        const float c2 = -0.5f * p.lam * beta;
+        const float gam = -p.r * dq_hi / (2.0f * p.sin_th);
+        const float4 *tab4 = reinterpret_cast<const float4 *>(
+            tb + (p.sigma > 0.f ? 0 : kp));
+        float acc1 = 0.f, acc2 = 0.f;
+        for (int blk = 0; blk < kp; blk += RS) {
+          float s0, c0;
+          seed_sincos((float)(kb0 + blk), p.th_hi, p.th_lo, s0, c0);
+          float t = beta * s0;
+          float v = fmaf(c1, c0, c2 * s0);
+#pragma unroll
+          for (int j = 0; j < RS; j += 2) {
+            const float4 w = tab4[(blk + j) >> 1];
+            float vn = fmaf(p.lam, t, v);
+            acc1 = fmaf(w.x, v + vn, acc1);
+            acc2 = fmaf(w.y, t, acc2);
+            t = t + vn;
+            v = vn;
+            vn = fmaf(p.lam, t, v);
+            acc1 = fmaf(w.z, v + vn, acc1);
+            acc2 = fmaf(w.w, t, acc2);
+            t = t + vn;
+            v = vn;
+          }
+        }
+        const float s = fmaf(gam, acc1, acc2);
+        gx = fmaf(s, dx, gx);
+        gy = fmaf(s, dy, gy);
+        gz = fmaf(s, dz, gz);
+      }
+    }
+  }
+  sred[grp][lane][0] = gx;
+  sred[grp][lane][1] = gy;
+  sred[grp][lane][2] = gz;
+  __syncthreads();
+  if (tid < ti.y * 3) {
+    const int a = tid / 3, cpt = tid % 3;
+    float s = 0.f;
+    for (int gg = 0; gg < ngrp; ++gg) s += sred[gg][a][cpt];
+    grad[(size_t)perm[ti.x + a] * 3 + cpt] = s;
+  }
+}
+
+}  // namespace pyiid

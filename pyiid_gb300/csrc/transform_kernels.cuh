@@ -1,0 +1,269 @@
+// transform_kernels.cuh -- F(Q) -> G(r), potentials and the adjoint weights.
+//
+// The reference's F -> G transform (zero pad, odd extension, inverse FFT,
+// linear interpolation onto the r grid) is a fixed linear map
+//   G(r_i) = sum_k F_k T[k][i]
+// (see the host builder of T for the derivation).  T is stored [n_bins][n_r]
+// in FP32, so G for a batch of configurations is a skinny GEMM streaming T
+// from HBM/L2 once per CTA column block.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace pyiid {
+
+// gr[b][i] = sum_k fq[b][k] * T[k][i]  (FP32 products, FP32 blocks of 32 bins
+// summed in FP64).  grid (ceil(n_r/256), n_configs)
+__global__ void pdf_kernel(const float *__restrict__ fq,
+                           const float *__restrict__ T, int n_bins, int n_r,
+                           int kmin, double *__restrict__ gr) {
+  extern __shared__ float sf[];
+  const int b = blockIdx.y;
+  for (int k = threadIdx.x; k < n_bins; k += blockDim.x)
+    sf[k] = (k >= kmin) ? fq[(size_t)b * n_bins + k] : 0.f;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_r) return;
+  double acc = 0.0;
+  for (int k0 = kmin; k0 < n_bins; k0 += 32) {
+    float part = 0.f;
+    const int k1 = min(k0 + 32, n_bins);
+    for (int k = k0; k < k1; ++k) part = fmaf(sf[k], T[(size_t)k * n_r + i], part);
+    acc += (double)part;
+  }
+  gr[(size_t)b * n_r + i] = acc;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *scratch) {
+  // scratch: [32][NV]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) scratch[wid * NV + i] = v[i];
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += scratch[w * NV + i];
+    v[i] = s;
+  }
+  __syncthreads();
+}
+
+// Potential per configuration (one CTA each):
+//   a = (gc.go)/(gc.gc); Rw: a <= 0 -> (1, 1), else sqrt(|go - a gc|^2/|go|^2)
+//   chi^2: s = a if a > 0 else 1, value = |go - s gc|^2
+// Optionally the adjoint vector c = d(value)/d(gcalc) exactly as the
+// reference's get_grad_rw / get_grad_chi_sq contract it (the derivative of
+// the scale uses the raw a even when the value used scale 1):
+//   c_i = pre [s E_i + (gc.E) (go_i - 2 a gc_i)/(gc.gc)],  E = go - s gc,
+//   pre = -Rw/|E|^2 (Rw) or -2 (chi^2).
+__global__ void potential_kernel(const double *__restrict__ gobs,
+                                 const double *__restrict__ gcalc, int n_r,
+                                 int potential, double *__restrict__ out,
+                                 float *__restrict__ cvec) {
+  __shared__ double scratch[32 * 3];
+  const int b = blockIdx.x;
+  const double *gc = gcalc + (size_t)b * n_r;
+  double v3[3] = {0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < n_r; i += blockDim.x) {
+    const double c = gc[i], o = gobs[i];
+    v3[0] += c * o;
+    v3[1] += c * c;
+    v3[2] += o * o;
+  }
+  block_sum<3>(v3, scratch);
+  const double gco = v3[0], gcc = v3[1], goo = v3[2];
+  const double a = gco / gcc;
+  // the reference replaces a non-positive scale by 1; a NaN scale stays NaN
+  const double s = (a <= 0.0) ? 1.0 : a;
+  double v2[2] = {0.0, 0.0};
+  for (int i = threadIdx.x; i < n_r; i += blockDim.x) {
+    const double e = gobs[i] - s * gc[i];
+    v2[0] += e * e;
+    v2[1] += gc[i] * e;
+  }
+  block_sum<2>(v2, scratch);
+  const double ee = v2[0], gce = v2[1];
+  double value, pre;
+  if (potential == 0) {
+    if (a <= 0.0) {
+      value = 1.0;
+    } else {
+      value = sqrt(ee / goo);
+    }
+    pre = -value / ee;
+  } else {
+    value = ee;
+    pre = -2.0;
+  }
+  if (threadIdx.x == 0) {
+    out[2 * b] = value;
+    out[2 * b + 1] = s;
+  }
+  if (cvec) {
+    for (int i = threadIdx.x; i < n_r; i += blockDim.x) {
+      const double e = gobs[i] - s * gc[i];
+      const double ci = pre * (s * e + gce * (gobs[i] - 2.0 * a * gc[i]) / gcc);
+      cvec[(size_t)b * n_r + i] = (float)ci;
+    }
+  }
+}
+
+// w[b][k] = sum_i T[k][i] c[b][i]: one warp per (b, k); FP32 products, lane
+// partials reduced in FP64.
+__global__ void wvec_kernel(const float *__restrict__ T,
+                            const float *__restrict__ cvec, int n_bins,
+                            int n_r, int kmin, int n_configs,
+                            double *__restrict__ w) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= n_configs * n_bins) return;
+  const int b = gw / n_bins, k = gw % n_bins;
+  double acc = 0.0;
+  if (k >= kmin) {
+    const float *row = T + (size_t)k * n_r;
+    const float *c = cvec + (size_t)b * n_r;
+    float part = 0.f;
+    for (int i = lane; i < n_r; i += 32) part = fmaf(row[i], c[i], part);
+    acc = warp_sum((double)part);
+  }
+  if (lane == 0) w[(size_t)b * n_bins + k] = acc;
+}
+
+// Adjoint tables: tabs[b][sa][sb][sigma][kk] = (A, B),
+//   k = kb0 + kk, W = 2 w_k f_sa f_sb / na_k (0 outside [kmin, n_bins) or
+//   where na_k = 0), A = k W sigma^k, B = W sigma^k.
+__global__ void adjoint_table_kernel(const double *__restrict__ w,
+                                     const double *__restrict__ na,
+                                     const float *__restrict__ ftab,
+                                     int n_species, int n_bins, int kmin,
+                                     int kb0, int kp, int n_configs,
+                                     float2 *__restrict__ tabs) {
+  const size_t total = (size_t)n_configs * n_species * n_species * kp;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int kk = idx % kp;
+    size_t rest = idx / kp;
+    const int sb = rest % n_species;
+    rest /= n_species;
+    const int sa = rest % n_species;
+    const int b = (int)(rest / n_species);
+    const int k = kb0 + kk;
+    double W = 0.0;
+    if (k >= kmin && k < n_bins) {
+      const double nak = na[(size_t)b * n_bins + k];
+      if (nak != 0.0)
+        W = 2.0 * w[(size_t)b * n_bins + k] * (double)ftab[sa * n_bins + k] *
+            (double)ftab[sb * n_bins + k] / nak;
+    }
+    const float Wp = (float)W;
+    const float Wm = (k & 1) ? -Wp : Wp;
+    const float kf = (float)k;
+    float2 *base = tabs + ((((size_t)b * n_species + sa) * n_species + sb) * 2) * kp;
+    base[kk] = make_float2(kf * Wp, Wp);
+    base[kp + kk] = make_float2(kf * Wm, Wm);
+  }
+}
+
+// dF coefficient table for the reference-convention gradient:
+//   coef[b][sa][sb][k] = -f_sa f_sb / na_k   (float division as the reference)
+__global__ void gradfq_coef_kernel(const double *__restrict__ na,
+                                   const float *__restrict__ ftab,
+                                   int n_species, int n_bins, int n_configs,
+                                   float *__restrict__ coef) {
+  const size_t total = (size_t)n_configs * n_species * n_species * n_bins;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int k = idx % n_bins;
+    size_t rest = idx / n_bins;
+    const int sb = rest % n_species;
+    rest /= n_species;
+    const int sa = rest % n_species;
+    const int b = (int)(rest / n_species);
+    const float nak = (float)na[(size_t)b * n_bins + k];
+    coef[idx] = -(ftab[sa * n_bins + k] * ftab[sb * n_bins + k]) / nak;
+  }
+}
+
+// Compat G(r) gradient: out[row][i] = sum_k A[row][k] T[k][i] (FP32 GEMM,
+// 128x128 CTA tile, 8x8 per thread, FP64 output).  Rows are the 3N rows of a
+// reference-convention grad_fq.
+__global__ void __launch_bounds__(256)
+    gemm_rows_T_kernel(const float *__restrict__ A, const float *__restrict__ T,
+                       int n_rows, int n_bins, int n_r, int kmin,
+                       double *__restrict__ out) {
+  __shared__ float sA[8][128 + 4];
+  __shared__ float sB[8][128 + 4];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int row0 = blockIdx.y * 128, col0 = blockIdx.x * 128;
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int k0 = kmin; k0 < n_bins; k0 += 8) {
+    // load A tile: 128 rows x 8 k  (256 threads x 4 elements)
+    for (int e = threadIdx.x; e < 128 * 8; e += 256) {
+      const int r = e / 8, kk = e % 8;
+      const int gr = row0 + r, gk = k0 + kk;
+      sA[kk][r] = (gr < n_rows && gk < n_bins) ? A[(size_t)gr * n_bins + gk] : 0.f;
+    }
+    for (int e = threadIdx.x; e < 128 * 8; e += 256) {
+      const int kk = e / 128, c = e % 128;
+      const int gk = k0 + kk, gc = col0 + c;
+      sB[kk][c] = (gk < n_bins && gc < n_r) ? T[(size_t)gk * n_r + gc] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      float a[8], bb[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = sA[kk][ty * 8 + i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) bb[j] = sB[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int gr = row0 + ty * 8 + i;
+    if (gr >= n_rows) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int gc = col0 + tx + 16 * j;
+      if (gc < n_r) out[(size_t)gr * n_r + gc] = (double)acc[i][j];
+    }
+  }
+}
+
+// Compat potential gradient from an explicit grad_pdf: one warp per row,
+// grad[row] = sum_i c_i gpdf[row][i], with c recomputed from (gcalc, gobs).
+__global__ void potential_grad_rows_kernel(const double *__restrict__ gpdf,
+                                           const float *__restrict__ cvec,
+                                           int n_rows, int n_r,
+                                           double *__restrict__ grad) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= n_rows) return;
+  const double *row = gpdf + (size_t)gw * n_r;
+  double acc = 0.0;
+  for (int i = lane; i < n_r; i += 32) acc += (double)cvec[i] * row[i];
+  acc = warp_sum(acc);
+  if (lane == 0) grad[gw] = acc;
+}
+
+}  // namespace pyiid

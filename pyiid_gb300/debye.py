@@ -1,0 +1,187 @@
+"""Device-side functional API over the C ABI (torch tensors in, tensors out).
+
+Inputs that describe the system (species ids, form-factor tables, r grid) are
+host numpy arrays; positions, F(Q), G(r) and gradients are CUDA tensors on the
+current device, so chains of calls stay on the GPU.  Every function launches
+on torch's current stream.
+"""
+import numpy as np
+import torch
+
+from ._native import context, POTENTIALS, NativeError
+
+__all__ = ['fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
+           'batch_potential_grad', 'as_positions']
+
+_f32p = None
+
+
+def _np(a, dtype):
+    return np.ascontiguousarray(np.asarray(a, dtype=dtype))
+
+
+def _ptr(a, ctype):
+    import ctypes
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def as_positions(x, device=None):
+    """float32 contiguous CUDA tensor [N, 3] from an array or tensor."""
+    if isinstance(x, torch.Tensor):
+        t = x.detach()
+        if not t.is_cuda:
+            t = t.to('cuda' if device is None else device)
+        return t.to(torch.float32).contiguous()
+    return torch.as_tensor(_np(x, np.float32), device=device or 'cuda')
+
+
+def _check_dev(t, name, dtype):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise NativeError(f'{name} must be a CUDA tensor')
+    if t.dtype != dtype or not t.is_contiguous():
+        raise NativeError(f'{name} must be a contiguous {dtype} tensor')
+
+
+def fq(positions, species, scatter, qbin, k_begin=0):
+    """Reduced structure factor [K] (bins from Q = 0; bins < k_begin are 0)."""
+    import ctypes
+    pos = as_positions(positions)
+    n = pos.shape[0]
+    sp = _np(species, np.int32)
+    tab = _np(scatter, np.float32)
+    if tab.ndim != 2 or sp.shape != (n,):
+        raise NativeError('species must be [N] and scatter [S, K]')
+    out = torch.empty(tab.shape[1], dtype=torch.float32, device=pos.device)
+    ctx = context(pos.device.index)
+    ctx.call('pyiid_fq', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
+             tab.shape[0], tab.shape[1], float(qbin), int(k_begin),
+             ctypes.c_void_p(out.data_ptr()))
+    return out
+
+
+def grad_fq(positions, species, scatter, qbin, k_begin=0):
+    """Reference-convention gradient [N, 3, K] (= -1/2 dF/dx)."""
+    import ctypes
+    pos = as_positions(positions)
+    n = pos.shape[0]
+    sp = _np(species, np.int32)
+    tab = _np(scatter, np.float32)
+    out = torch.zeros((n, 3, tab.shape[1]), dtype=torch.float32,
+                      device=pos.device)
+    if n == 0:
+        return out
+    ctx = context(pos.device.index)
+    ctx.call('pyiid_grad_fq', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
+             tab.shape[0], tab.shape[1], float(qbin), int(k_begin),
+             ctypes.c_void_p(out.data_ptr()))
+    return out
+
+
+def pdf(fq_t, qstep, rstep, rgrid, qmin):
+    """G(r) [B, R] (float64) for F(Q) rows [B, K] (or [K] -> [R])."""
+    import ctypes
+    squeeze = fq_t.dim() == 1
+    f = fq_t.reshape(1, -1) if squeeze else fq_t
+    f = f.to(torch.float32).contiguous()
+    rg = _np(rgrid, np.float64)
+    out = torch.empty((f.shape[0], len(rg)), dtype=torch.float64,
+                      device=f.device)
+    if len(rg):
+        ctx = context(f.device.index)
+        ctx.call('pyiid_pdf', ctypes.c_void_p(f.data_ptr()), f.shape[0],
+                 f.shape[1], float(qstep), float(rstep),
+                 _ptr(rg, ctypes.c_double), len(rg), float(qmin),
+                 ctypes.c_void_p(out.data_ptr()))
+    return out[0] if squeeze else out
+
+
+def grad_pdf(grad_fq_t, qstep, rstep, rgrid, qmin):
+    """Transform of every row of a [N, 3, K] gradient -> [N, 3, R] float64."""
+    import ctypes
+    g = grad_fq_t.to(torch.float32).contiguous()
+    n, _, k = g.shape
+    rg = _np(rgrid, np.float64)
+    out = torch.zeros((n, 3, len(rg)), dtype=torch.float64, device=g.device)
+    if n and len(rg):
+        ctx = context(g.device.index)
+        ctx.call('pyiid_grad_pdf', ctypes.c_void_p(g.data_ptr()), n, k,
+                 float(qstep), float(rstep), _ptr(rg, ctypes.c_double),
+                 len(rg), float(qmin), ctypes.c_void_p(out.data_ptr()))
+    return out
+
+
+def potential(gobs, gcalc, kind='rw'):
+    """(value, scale) rows [B, 2] for gcalc [B, R] (or [R] -> [2])."""
+    import ctypes
+    squeeze = gcalc.dim() == 1
+    gc = (gcalc.reshape(1, -1) if squeeze else gcalc).to(torch.float64)
+    gc = gc.contiguous()
+    go = gobs.to(device=gc.device, dtype=torch.float64).contiguous()
+    out = torch.empty((gc.shape[0], 2), dtype=torch.float64, device=gc.device)
+    ctx = context(gc.device.index)
+    ctx.call('pyiid_potential', ctypes.c_void_p(go.data_ptr()),
+             ctypes.c_void_p(gc.data_ptr()), gc.shape[0], gc.shape[1],
+             POTENTIALS[kind], ctypes.c_void_p(out.data_ptr()))
+    return out[0] if squeeze else out
+
+
+def potential_grad(grad_pdf_t, gcalc, gobs, kind='rw'):
+    """sum_r c_r dG_r for each [a, c] row of grad_pdf [N, 3, R] -> [N, 3]."""
+    import ctypes
+    gp = grad_pdf_t.to(torch.float64).contiguous()
+    gc = gcalc.to(device=gp.device, dtype=torch.float64).contiguous()
+    go = gobs.to(device=gp.device, dtype=torch.float64).contiguous()
+    n = gp.shape[0]
+    out = torch.zeros((n, 3), dtype=torch.float64, device=gp.device)
+    if n:
+        ctx = context(gp.device.index)
+        ctx.call('pyiid_potential_grad', ctypes.c_void_p(gp.data_ptr()),
+                 ctypes.c_void_p(gc.data_ptr()), ctypes.c_void_p(go.data_ptr()),
+                 n, gp.shape[2], POTENTIALS[kind],
+                 ctypes.c_void_p(out.data_ptr()))
+    return out
+
+
+def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
+                         rgrid, qmin, gobs, kind='rw', want_grad=True,
+                         out=None):
+    """Fused F -> G -> potential (+ adjoint gradient) for packed configs.
+
+    positions [sum N, 3] (CUDA), species [sum N] and offsets [B+1] (host).
+    Returns dict(energy [B, 2] f64, grad [sum N, 3] f32 or None,
+    gcalc [B, R] f64, fq [B, K] f32).  ``out`` may pass preallocated tensors
+    with those keys (used under CUDA-graph capture).
+    """
+    import ctypes
+    pos = as_positions(positions)
+    sp = _np(species, np.int32)
+    off = _np(offsets, np.int32)
+    tab = _np(scatter, np.float32)
+    rg = _np(rgrid, np.float64)
+    b = len(off) - 1
+    dev = pos.device
+    go = gobs.to(device=dev, dtype=torch.float64).contiguous()
+    if out is None:
+        out = {
+            'energy': torch.empty((b, 2), dtype=torch.float64, device=dev),
+            'grad': (torch.empty((pos.shape[0], 3), dtype=torch.float32,
+                                 device=dev) if want_grad else None),
+            'gcalc': torch.empty((b, len(rg)), dtype=torch.float64,
+                                 device=dev),
+            'fq': torch.empty((b, tab.shape[1]), dtype=torch.float32,
+                              device=dev),
+        }
+    ctx = context(dev.index)
+    g = out.get('grad')
+    ctx.call('pyiid_batch_potential_grad', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
+             _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
+             float(qstep), float(rstep), _ptr(rg, ctypes.c_double), len(rg),
+             float(qmin), ctypes.c_void_p(go.data_ptr()), POTENTIALS[kind],
+             ctypes.c_void_p(out['energy'].data_ptr()),
+             ctypes.c_void_p(g.data_ptr() if g is not None else 0),
+             ctypes.c_void_p(out['gcalc'].data_ptr()),
+             ctypes.c_void_p(out['fq'].data_ptr()))
+    return out

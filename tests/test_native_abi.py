@@ -1,0 +1,54 @@
+"""The C-ABI library builds, loads and exports every symbol of the header.
+
+CPU-only: no compute call is made; pyiid_create must fail cleanly (status +
+message, no crash) when no GB300 is present.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import REPO, gpu_available
+
+
+def header_symbols():
+    src = open(os.path.join(REPO, 'include', 'pyiid_gb300.h')).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    return sorted(set(re.findall(r'\b(pyiid_[a-z_0-9]+)\s*\(', src)))
+
+
+def test_library_exports_every_header_symbol():
+    from pyiid_gb300 import _native
+    lib = _native.load()
+    declared = header_symbols()
+    assert declared, 'no symbols parsed from the header'
+    for name in declared:
+        assert hasattr(lib, name), f'{name} missing from the library'
+    # the Python binding declares exactly the header's entry points
+    assert set(_native.symbols()) == set(declared)
+
+
+def test_version():
+    from pyiid_gb300 import _native
+    assert _native.load().pyiid_version() == 10000
+
+
+@pytest.mark.skipif(gpu_available(), reason='checks the no-GPU error path')
+def test_create_without_gpu_reports_error():
+    from pyiid_gb300 import _native
+    lib = _native.load()
+    h = ctypes.c_void_p()
+    rc = lib.pyiid_create(ctypes.byref(h), 0)
+    assert rc != 0
+    assert lib.pyiid_last_error(None)
+    with pytest.raises(_native.NativeError):
+        _native.Context(0)
+
+
+def test_null_context_is_rejected():
+    from pyiid_gb300 import _native
+    lib = _native.load()
+    assert lib.pyiid_set_stream(None, None) != 0
+    assert lib.pyiid_synchronize(None) != 0
+    assert lib.pyiid_launch_count(None) == -1
