@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Exact F(Q) + full gradient evaluations per second on one GB300.
+
+Workload (one "step" = one exact evaluation): a 20,000-atom spherical fcc Pt
+particle (a = 3.92 A, the 20,000 sites nearest the origin, seeded N(0, 0.02^2)
+displacements, float32), Q grid 0.5-30 1/A step 0.02 (1500 bins from Q = 0,
+1475 returned), stand-in Pt form factor; outputs F(Q) [1475] and the full
+gradient dF/dx [20000, 3, 1475] in the reference convention.  Inputs are
+synthetic (seeded); the gradient output (354 MB) exceeds the 129 MB L2 and L2
+is flushed between timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU path (the FP32 C port of its numba
+code, oracle/debye_ref.c) on the host cores for the same workload, on a
+bounded sample of pairs per step, and prints the same JSON line.
+Under torchrun every rank evaluates its own copy (weak scaling, no
+collective on the data path); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = 'exact F(Q)+grad evals/s'
+N_ATOMS, A_PT, SIGMA, SEED = 20000, 3.92, 0.02, 2
+QMIN, QMAX, QBIN = 0.5, 30.0, 0.02
+FLOPS_GRAD_TERM = 20   # flop-equivalents per unordered pair-bin of dF/dx
+FLOPS_F_TERM = 10      # ... of F(Q)
+
+
+def workload():
+    from pyiid_gb300 import structures
+    from pyiid_gb300.scatter_factors import species_tables
+    pos = structures.displaced(structures.fcc_nearest(A_PT, N_ATOMS), SIGMA,
+                               SEED)
+    n_bins = int(np.floor(QMAX / QBIN))
+    k_begin = int(np.floor(QMIN / QBIN))
+    sp, tab, _ = species_tables([78] * len(pos), QBIN, n_bins)
+    return pos, sp, tab, n_bins, k_begin
+
+
+def config_dict(n_bins, k_begin, extra=None):
+    d = {'workload': 'single fcc Pt nanoparticle, exact F(Q) + full dF/dx',
+         'n_atoms': N_ATOMS, 'lattice_a': A_PT, 'sigma': SIGMA,
+         'q_grid': [QMIN, QMAX, QBIN], 'bins_returned': n_bins - k_begin,
+         'pairs': N_ATOMS * (N_ATOMS - 1) // 2,
+         'l2': 'flushed between timed steps (256 MiB write)'}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(REPO, 'gpurun_out', f'clocks_{os.getpid()}.csv')
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.device),
+                 f'--query-gpu={self.FIELDS}', '--format=csv,noheader,nounits',
+                 '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable']}
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(',')]
+            if len(p) < 8:
+                continue
+            try:
+                rows.append((float(p[0]), float(p[1]), float(p[2]), p[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no samples']}
+        pw = np.array([r[2] for r in rows])
+        load = [r for r in rows if r[2] >= 0.5 * pw.max()] or rows
+        reasons = set()
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap')
+        for r in load:
+            for nm, v in zip(names, r[3]):
+                if v.lower().startswith('active'):
+                    reasons.add(nm)
+        return {'sm_mhz': float(np.median([r[0] for r in load])),
+                'sm_max_mhz': float(max(r[1] for r in rows)),
+                'power_w_max': float(pw.max()),
+                'samples': len(rows), 'reasons': sorted(reasons)}
+
+
+# ------------------------------------------------------------- GPU arm
+def fp32_peak_tflops(torch, dev):
+    """Measured FP32 (CUDA-core) peak: cuBLAS SGEMM 8192^3, TF32 off."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device=dev)
+    b = torch.randn(n, n, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = max(best, 2 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def run_gpu(args, rank, world, local):
+    import torch
+    from pyiid_gb300 import debye
+    from pyiid_gb300._native import context
+    dev = torch.device('cuda', local)
+    torch.cuda.set_device(dev)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+        pg = dist
+    pos, sp, tab, n_bins, k_begin = workload()
+    n = len(pos)
+    pairs = n * (n - 1) // 2
+    k_ret = n_bins - k_begin
+    pos_d = torch.as_tensor(pos, device=dev)
+    fq = torch.empty(n_bins, dtype=torch.float32, device=dev)
+    grad = torch.empty((n, 3, n_bins), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    ctx = context(local)
+
+    def step():
+        debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
+        debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)]
+          for _ in range(args.steps)]
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
+            ev[i][1].record(stream)
+            debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
+            ev[i][2].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = ctx.launches - launches0
+    t_f = [ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)]
+    t_g = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
+    ms_step = float(np.sum(t_f) + np.sum(t_g)) / args.steps
+    if pg:
+        t = torch.tensor([ms_step], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world / (ms_step * 1e-3)
+
+    # end to end: pinned host positions -> device, F + dF/dx, results -> pinned host
+    h_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    h_pos.copy_(torch.as_tensor(pos))
+    h_fq = torch.empty(n_bins, dtype=torch.float32, pin_memory=True)
+    h_grad = torch.empty((n, 3, n_bins), dtype=torch.float32, pin_memory=True)
+    e2e_steps = max(2, min(args.steps, 5))
+    times = []
+    for i in range(e2e_steps + 1):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        pos_d.copy_(h_pos, non_blocking=True)
+        debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
+        debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
+        h_fq.copy_(fq, non_blocking=True)
+        h_grad.copy_(grad, non_blocking=True)
+        e.record(stream)
+        e.synchronize()
+        if i:
+            times.append(s.elapsed_time(e))
+    e2e_ms = float(np.mean(times))
+    if pg:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    # correctness guard on what was timed: finite, nonzero
+    assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
+
+    peak = fp32_peak_tflops(torch, dev) if rank == 0 else None
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    if rank != 0:
+        return None
+    g_ms = float(np.mean(t_g))
+    f_ms = float(np.mean(t_f))
+    achieved = pairs * k_ret * FLOPS_GRAD_TERM / (g_ms * 1e-3) / 1e12
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'evals/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'fp32 (FP64 final reductions)', 'data': 'synthetic (seeded fcc Pt)',
+        'config': config_dict(n_bins, k_begin, {'parallelism': f'replica x{world}'}),
+        'kernel_ms': {'fq': f_ms, 'grad_fq': g_ms},
+        'pair_bin_terms_per_s': 2 * pairs * k_ret / (ms_step * 1e-3),
+        'wall_s_timed_region': wall,
+        'gpu_launches': int(launches),
+        'e2e': {'value': world / (e2e_ms * 1e-3), 'unit': 'evals/s',
+                'h2d_bytes_per_step': int(h_pos.numel() * 4),
+                'd2h_bytes_per_step': int(h_fq.numel() * 4 + h_grad.numel() * 4)},
+        'roofline': {
+            'bound': 'fp32', 'kernel': 'gradfq_kernel',
+            'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
+            'frac': achieved / peak if peak else None,
+            'peak_source': 'measured live: cuBLAS SGEMM 8192^3 (TF32 off)',
+            'algorithmic_flops_per_launch': pairs * k_ret * FLOPS_GRAD_TERM,
+            'traffic': traffic_from_profile(),
+        },
+        'clocks': clk.summary(),
+    }
+    return line
+
+
+def traffic_from_profile():
+    """DRAM bytes per gradfq launch from the committed ncu summary, if any."""
+    p = os.path.join(REPO, 'profiles', 'gradfq_kernel_pt20000.md')
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith('dram_bytes_per_launch_full_size:'):
+            try:
+                return float(line.split(':', 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------- CPU arm
+def cpu_sample(target_s=15.0, threads=0):
+    """Time the FP32 reference-path port on a bounded sample of the workload's
+    pairs (F and dF/dx tasks); return evals/s extrapolated to all pairs."""
+    from oracle import debye_c
+    pos, sp, tab, n_bins, k_begin = workload()
+    per_atom = tab[sp]
+    n = len(pos)
+    pairs = n * (n - 1) // 2
+    chunk = 2048
+    nthreads = threads or os.cpu_count()
+    # one calibration round, then a sample sized to ~target_s
+    t0 = time.perf_counter()
+    _, _, used = debye_c.port_tasks(pos, per_atom, QBIN, chunk, chunk * nthreads,
+                                    True, True, nthreads)
+    t1 = time.perf_counter() - t0
+    rounds = max(1, int(target_s / max(t1, 1e-3)))
+    sample_pairs = chunk * nthreads * rounds
+    t0 = time.perf_counter()
+    debye_c.port_tasks(pos, per_atom, QBIN, chunk, sample_pairs, True, True,
+                       nthreads)
+    dt = time.perf_counter() - t0
+    evals_per_s = sample_pairs / (dt * pairs)
+    return {'value': evals_per_s, 'unit': 'evals/s', 'cores': int(used),
+            'kind': 'port',
+            'sample': (f'{sample_pairs} of {pairs} pairs (all 1500 bins, F and '
+                       f'dF/dx tasks of {chunk} pairs) in {dt:.1f} s, '
+                       f'extrapolated linearly in pairs'),
+            'seconds': dt}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from oracle import build_oracle
+    build_oracle.build()
+    pos, sp, tab, n_bins, k_begin = workload()
+    vals = []
+    per_step = max(3.0, min(20.0, 60.0 / max(1, args.steps)))
+    for i in range(args.warmup):
+        cpu_sample(target_s=1.0)
+    for i in range(args.steps):
+        vals.append(cpu_sample(target_s=per_step))
+    v = float(np.mean([x['value'] for x in vals]))
+    base = dict(vals[-1])
+    base['value'] = v
+    return {
+        'metric': METRIC, 'value': v, 'unit': 'evals/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1e3 / v, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'fp32 (FP64 sums)',
+        'data': 'synthetic (seeded fcc Pt)', 'impl': 'reference',
+        'config': config_dict(n_bins, k_begin, {'parallelism': 'host cores'}),
+        'cpu_baseline': base,
+        'e2e': {'value': v, 'unit': 'evals/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == 'reference':
+        line = run_reference(args, rank, world)
+    else:
+        line = run_gpu(args, rank, world, local)
+        if line is not None and world == 1:
+            from oracle import build_oracle
+            build_oracle.build()
+            line['cpu_baseline'] = cpu_sample(target_s=args.cpu_seconds)
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == '__main__':
+    main()

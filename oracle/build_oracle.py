@@ -1,0 +1,34 @@
+"""Build recipe of the oracle's C restatements (test infrastructure).
+
+gcc -O3 -fopenmp -shared -fPIC oracle/debye_ref.c -> oracle/_lib/libdebye_ref.so
+
+The reference itself is pure Python (numba), so there is no reference C/C++
+source to compile into oracle/_ref; its Python code is exercised by
+tests/golden/make_golden.py instead.  No -march flags: the same source is
+built on x86_64 here and on aarch64 GPU hosts.
+"""
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBDIR = os.path.join(HERE, '_lib')
+LIB = os.path.join(LIBDIR, 'libdebye_ref.so')
+SRC = os.path.join(HERE, 'debye_ref.c')
+
+
+def build(force=False):
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+        return LIB
+    os.makedirs(LIBDIR, exist_ok=True)
+    cc = os.environ.get('CC') or shutil.which('gcc') or 'cc'
+    tmp = LIB + '.tmp'
+    subprocess.run([cc, '-O3', '-fopenmp', '-shared', '-fPIC', '-o', tmp, SRC,
+                    '-lm'], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == '__main__':
+    print(build(force=True))

@@ -42,7 +42,7 @@ def _check_dev(t, name, dtype):
         raise NativeError(f'{name} must be a contiguous {dtype} tensor')
 
 
-def fq(positions, species, scatter, qbin, k_begin=0):
+def fq(positions, species, scatter, qbin, k_begin=0, out=None):
     """Reduced structure factor [K] (bins from Q = 0; bins < k_begin are 0)."""
     import ctypes
     pos = as_positions(positions)
@@ -51,7 +51,10 @@ def fq(positions, species, scatter, qbin, k_begin=0):
     tab = _np(scatter, np.float32)
     if tab.ndim != 2 or sp.shape != (n,):
         raise NativeError('species must be [N] and scatter [S, K]')
-    out = torch.empty(tab.shape[1], dtype=torch.float32, device=pos.device)
+    if out is None:
+        out = torch.empty(tab.shape[1], dtype=torch.float32, device=pos.device)
+    else:
+        _check_dev(out, 'out', torch.float32)
     ctx = context(pos.device.index)
     ctx.call('pyiid_fq', ctypes.c_void_p(pos.data_ptr()),
              _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
@@ -60,15 +63,19 @@ def fq(positions, species, scatter, qbin, k_begin=0):
     return out
 
 
-def grad_fq(positions, species, scatter, qbin, k_begin=0):
-    """Reference-convention gradient [N, 3, K] (= -1/2 dF/dx)."""
+def grad_fq(positions, species, scatter, qbin, k_begin=0, out=None):
+    """Reference-convention gradient [N, 3, K] (= -1/2 dF/dx).  Every element
+    of ``out`` is written (bins < k_begin with 0)."""
     import ctypes
     pos = as_positions(positions)
     n = pos.shape[0]
     sp = _np(species, np.int32)
     tab = _np(scatter, np.float32)
-    out = torch.zeros((n, 3, tab.shape[1]), dtype=torch.float32,
-                      device=pos.device)
+    if out is None:
+        out = torch.empty((n, 3, tab.shape[1]), dtype=torch.float32,
+                          device=pos.device)
+    else:
+        _check_dev(out, 'out', torch.float32)
     if n == 0:
         return out
     ctx = context(pos.device.index)

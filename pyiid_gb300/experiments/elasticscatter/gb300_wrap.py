@@ -1,0 +1,70 @@
+"""The 'GB300' processor: the three plug-in callables of ElasticScatter.
+
+Same signatures, dtypes and conventions as the reference's processors
+(cpu_wrappers/flat_multi_cpu_wrap.py:22-102, gpu_wrappers/gpu_wrap.py:119-284,
+kernels/master_kernel.py:276-290):
+
+  wrap_fq(atoms, qbin=.1, sum_type='fq')       -> float32 [K]      (Q from 0)
+  wrap_fq_grad(atoms, qbin=.1, sum_type='fq')  -> float32 [N, 3, K] (-1/2 dF/dx)
+  grad_pdf(grad_fq, rstep, qstep, rgrid, qmin) -> float64 [N, 3, R]
+
+Each returns a fresh numpy array (the reference's tests check ``ans1 is not
+ans2``); all arithmetic runs in the sm_103a library.
+"""
+import numpy as np
+import torch
+
+from ... import debye
+
+__all__ = ['wrap_fq', 'wrap_fq_grad', 'grad_pdf', 'species_of']
+
+_NAMES = {'fq': 'F(Q) scatter'}
+
+
+def species_of(atoms, sum_type='fq'):
+    """(species [N] int32, table [S, K] float32) for the atoms' scatter array.
+
+    Uses the species column and tables that ElasticScatter._wrap_atoms
+    stores next to the reference's per-atom arrays when they are consistent;
+    otherwise derives them from the distinct rows of the per-atom array.
+    """
+    name = _NAMES.get(sum_type, 'PDF scatter')
+    per_atom = atoms.get_array(name)
+    n, k = per_atom.shape
+    sp = atoms.arrays.get('GB300 species')
+    tabs = atoms.info.get('GB300 tables')
+    if sp is not None and tabs is not None and name in tabs and len(sp) == n:
+        tab = tabs[name]
+        if tab.shape[1] == k and (n == 0 or (
+                np.array_equal(per_atom[0], tab[sp[0]]) and
+                np.array_equal(per_atom[-1], tab[sp[-1]]))):
+            return np.asarray(sp, np.int32), np.asarray(tab, np.float32)
+    if n == 0:
+        return np.zeros(0, np.int32), np.zeros((1, k), np.float32)
+    tab, inv = np.unique(np.asarray(per_atom, np.float32), axis=0,
+                         return_inverse=True)
+    return inv.reshape(-1).astype(np.int32), tab
+
+
+def _positions(atoms):
+    return torch.as_tensor(
+        np.ascontiguousarray(atoms.get_positions(), dtype=np.float32),
+        device='cuda')
+
+
+def wrap_fq(atoms, qbin=.1, sum_type='fq'):
+    sp, tab = species_of(atoms, sum_type)
+    f = debye.fq(_positions(atoms), sp, tab, qbin)
+    return f.cpu().numpy()
+
+
+def wrap_fq_grad(atoms, qbin=.1, sum_type='fq'):
+    sp, tab = species_of(atoms, sum_type)
+    g = debye.grad_fq(_positions(atoms), sp, tab, qbin)
+    return g.cpu().numpy()
+
+
+def grad_pdf(grad_fq, rstep, qstep, rgrid, qmin):
+    g = torch.as_tensor(np.ascontiguousarray(grad_fq, dtype=np.float32),
+                        device='cuda')
+    return debye.grad_pdf(g, qstep, rstep, rgrid, qmin).cpu().numpy()
