@@ -188,6 +188,24 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
                                double *energy, float *grad, double *gcalc,
                                float *fq);
 
+/* ------------------------------------------------------------------------ *
+ * Launch-shape variants (autotuning).
+ *
+ * The pair kernels come in several launch shapes (bins per thread, pairs
+ * interleaved per thread, threads per CTA).  A context uses one variant per
+ * kernel; pyiid_gb300's autotuner times them on the caller's sizes and sets
+ * the fastest.  No reference counterpart (the reference's numba launches are
+ * fixed, atomics/gpu_atomics.py:120-184).
+ *   kernel: PYIID_KERNEL_FQ (pyiid_fq and the F(Q) part of the batched call)
+ *           or PYIID_KERNEL_GRAD_FQ (pyiid_grad_fq).
+ *   params (pyiid_variant_info): {bins per thread, pairs per thread, threads
+ *   per CTA}. */
+enum { PYIID_KERNEL_FQ = 0, PYIID_KERNEL_GRAD_FQ = 1 };
+int pyiid_variant_count(int kernel);
+int pyiid_variant_info(int kernel, int variant, int *params, int n_params);
+int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant);
+int pyiid_get_variant(const pyiid_ctx *ctx, int kernel);
+
 #ifdef __cplusplus
 }
 #endif

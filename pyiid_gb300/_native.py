@@ -46,7 +46,13 @@ _SIGNATURES = {
     'pyiid_batch_potential_grad': (_c_int, [
         _vp, _vp, _i32p, _i32p, _c_int, _f32p, _c_int, _c_int, _c_dbl,
         _c_dbl, _f64p, _c_int, _c_dbl, _vp, _c_int, _vp, _vp, _vp, _vp]),
+    'pyiid_variant_count': (_c_int, [_c_int]),
+    'pyiid_variant_info': (_c_int, [_c_int, _c_int, _i32p, _c_int]),
+    'pyiid_set_variant': (_c_int, [_vp, _c_int, _c_int]),
+    'pyiid_get_variant': (_c_int, [_vp, _c_int]),
 }
+
+KERNELS = {'fq': 0, 'grad_fq': 1}
 
 
 class NativeError(RuntimeError):
@@ -132,6 +138,14 @@ class Context:
     def synchronize(self):
         self.check(self._lib.pyiid_synchronize(self.handle),
                    'pyiid_synchronize')
+
+    def set_variant(self, kernel, variant):
+        self.check(self._lib.pyiid_set_variant(self.handle, KERNELS[kernel],
+                                               int(variant)),
+                   'pyiid_set_variant')
+
+    def get_variant(self, kernel):
+        return int(self._lib.pyiid_get_variant(self.handle, KERNELS[kernel]))
 
     @property
     def launches(self):

@@ -34,6 +34,59 @@ constexpr int kVersion = 10000;  // 1.0.0
 constexpr int kJMax = 32;        // max J tiles per F(Q) work item
 constexpr int kAdjRS = 64;       // adjoint re-seed period (bins)
 
+// ---------------------------------------------------------------- variants
+// Launch shapes of the two pair kernels; pyiid_tune selects one per context.
+// F(Q): L bins per thread, NP pairs interleaved per thread.
+struct FqVariant {
+  int L, NP;
+};
+// dF/dx: L bins per thread, CPC chunks (threads) per atom in a CTA, NP pairs.
+struct GradVariant {
+  int L, CPC, NP;
+};
+
+using FqKernel = void (*)(const float *, const int *, const int4 *,
+                          const int4 *, float, float, int, int, int, int,
+                          double *);
+using GradKernel = void (*)(const float *, const int *, const int4 *,
+                            const int2 *, float, float, int, int, int,
+                            const float *, int, float *);
+
+struct FqEntry {
+  FqVariant v;
+  FqKernel k;
+};
+struct GradEntry {
+  GradVariant v;
+  GradKernel k;
+};
+
+const FqEntry kFqTable[] = {
+    {{32, 1}, fq_pair_kernel<32, 1>}, {{32, 2}, fq_pair_kernel<32, 2>},
+    {{16, 1}, fq_pair_kernel<16, 1>}, {{16, 2}, fq_pair_kernel<16, 2>},
+    {{24, 1}, fq_pair_kernel<24, 1>}, {{24, 2}, fq_pair_kernel<24, 2>},
+    {{48, 1}, fq_pair_kernel<48, 1>}, {{16, 4}, fq_pair_kernel<16, 4>},
+};
+// (the last template argument is the minimum resident CTAs per SM, i.e. the
+// register budget: 2 x 256 threads -> 128 registers, 3 x 256 -> 85)
+const GradEntry kGradTable[] = {
+    {{32, 8, 1}, gradfq_kernel<32, 8, 1, 2>},
+    {{32, 16, 1}, gradfq_kernel<32, 16, 1, 1>},
+    {{32, 4, 1}, gradfq_kernel<32, 4, 1, 4>},
+    {{16, 8, 1}, gradfq_kernel<16, 8, 1, 3>},
+    {{16, 8, 2}, gradfq_kernel<16, 8, 2, 2>},
+    {{16, 16, 2}, gradfq_kernel<16, 16, 2, 1>},
+    {{24, 8, 1}, gradfq_kernel<24, 8, 1, 2>},
+    {{16, 4, 1}, gradfq_kernel<16, 4, 1, 6>},
+};
+constexpr int kNumFq = sizeof(kFqTable) / sizeof(kFqTable[0]);
+constexpr int kNumGrad = sizeof(kGradTable) / sizeof(kGradTable[0]);
+
+size_t fq_smem(const FqVariant &v) {
+  return 2 * kTile * kTile * sizeof(float4) +
+         2 * (size_t)v.L * kBlock * sizeof(float);
+}
+
 uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) {
   const unsigned char *p = static_cast<const unsigned char *>(data);
   for (size_t i = 0; i < n; ++i) {
@@ -100,6 +153,8 @@ struct pyiid_ctx {
   uint64_t ftab_key = 0;
   int ftab_species = 0, ftab_bins = 0;
   bool attrs_set = false;
+  int fq_variant = 0;
+  int grad_variant = 0;
 };
 
 namespace {
@@ -396,12 +451,16 @@ void split_double(double x, float &hi, float &lo) {
 
 int set_attrs(pyiid_ctx *ctx) {
   if (ctx->attrs_set) return PYIID_OK;
-  CUDA_TRY(ctx, cudaFuncSetAttribute(gradfq_kernel<32>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     3 * kTile * kTile * 16));
-  CUDA_TRY(ctx, cudaFuncSetAttribute(fq_pair_kernel<32>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     2 * kTile * kTile * 16 + 2 * 32 * kBlock * 4));
+  for (int i = 0; i < kNumGrad; ++i)
+    CUDA_TRY(ctx, cudaFuncSetAttribute(
+                      kGradTable[i].k,
+                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                      3 * kTile * kTile * (int)sizeof(float4)));
+  for (int i = 0; i < kNumFq; ++i)
+    CUDA_TRY(ctx, cudaFuncSetAttribute(
+                      kFqTable[i].k,
+                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                      (int)fq_smem(kFqTable[i].v)));
   CUDA_TRY(ctx, cudaFuncSetAttribute(adjoint_kernel<kAdjRS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      160 * 1024));
@@ -438,19 +497,20 @@ int run_fq(pyiid_ctx *ctx, const Layout *L, const float *positions,
   const int n_items = (int)L->items.size();
   double *partial = nullptr;
   if (n_items > 0 && kb0 < n_bins) {
-    constexpr int Lb = 32;
+    const FqEntry &E = kFqTable[ctx->fq_variant];
+    const int Lb = E.v.L;
     const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
-    const int n_cb = (chunks_total + 127) / 128;
+    // at most 128 chunks per CTA (>= 2 pair groups) and n_chunks * L doubles
+    // must fit the 32 KB record space reused by the group reduction
+    const int max_chunks = std::min(128, 32768 / (8 * Lb));
+    const int n_cb = (chunks_total + max_chunks - 1) / max_chunks;
     const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
     const int n_groups = kBlock / n_chunks;
     void *p;
     TRY(ensure(ctx, "fq_partial", (size_t)n_items * n_bins * sizeof(double), &p));
     partial = static_cast<double *>(p);
-    // records (reused by the FP64 group reduction) + per-thread Kahan state
-    const size_t smem = 2 * kTile * kTile * sizeof(float4) +
-                        2 * (size_t)Lb * kBlock * sizeof(float);
     dim3 grid(n_items, n_cb);
-    fq_pair_kernel<Lb><<<grid, kBlock, smem, ctx->stream>>>(
+    E.k<<<grid, kBlock, fq_smem(E.v), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_items, dq_hi, dq_lo, kb0,
         n_chunks, n_groups, n_bins, partial);
     LAUNCH_CHECK(ctx);
@@ -586,16 +646,16 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
                                                   n_bins, 1, coef);
   LAUNCH_CHECK(ctx);
   if (kb0 < n_bins) {
-    constexpr int Lb = 32;
+    const GradEntry &E = kGradTable[ctx->grad_variant];
+    const int Lb = E.v.L, cpc = E.v.CPC;
     const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
-    const int cpc = 8;
     float dq_hi, dq_lo;
     split_double(qbin, dq_hi, dq_lo);
     dim3 grid((unsigned)L->tiles.size(), (chunks_total + cpc - 1) / cpc);
-    gradfq_kernel<Lb><<<grid, kTile * cpc, 3 * kTile * kTile * 16,
-                        ctx->stream>>>(
-        positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
-        chunks_total, cpc, n_bins, coef, n_species, grad);
+    E.k<<<grid, kTile * cpc, 3 * kTile * kTile * sizeof(float4),
+          ctx->stream>>>(positions, L->d_perm, L->d_tiles, L->d_cfg_tiles,
+                         dq_hi, dq_lo, kb0, chunks_total, n_bins, coef,
+                         n_species, grad);
     LAUNCH_CHECK(ctx);
   }
   if (kbo > 0)
@@ -761,6 +821,56 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
     LAUNCH_CHECK(ctx);
   }
   return PYIID_OK;
+}
+
+int pyiid_variant_count(int kernel) {
+  switch (kernel) {
+    case PYIID_KERNEL_FQ:
+      return kNumFq;
+    case PYIID_KERNEL_GRAD_FQ:
+      return kNumGrad;
+    default:
+      return -1;
+  }
+}
+
+int pyiid_variant_info(int kernel, int variant, int *params, int n_params) {
+  if (!params || n_params < 3)
+    return fail(nullptr, PYIID_ERR_INVALID_ARG, "params must hold 3 ints");
+  if (kernel == PYIID_KERNEL_FQ && variant >= 0 && variant < kNumFq) {
+    params[0] = kFqTable[variant].v.L;
+    params[1] = kFqTable[variant].v.NP;
+    params[2] = kBlock;
+    return PYIID_OK;
+  }
+  if (kernel == PYIID_KERNEL_GRAD_FQ && variant >= 0 && variant < kNumGrad) {
+    params[0] = kGradTable[variant].v.L;
+    params[1] = kGradTable[variant].v.NP;
+    params[2] = kTile * kGradTable[variant].v.CPC;
+    return PYIID_OK;
+  }
+  return fail(nullptr, PYIID_ERR_INVALID_ARG, "unknown kernel %d variant %d",
+              kernel, variant);
+}
+
+int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  const int n = pyiid_variant_count(kernel);
+  if (n < 0 || variant < 0 || variant >= n)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "unknown kernel %d variant %d",
+                kernel, variant);
+  if (kernel == PYIID_KERNEL_FQ)
+    ctx->fq_variant = variant;
+  else
+    ctx->grad_variant = variant;
+  return PYIID_OK;
+}
+
+int pyiid_get_variant(const pyiid_ctx *ctx, int kernel) {
+  if (!ctx) return -1;
+  if (kernel == PYIID_KERNEL_FQ) return ctx->fq_variant;
+  if (kernel == PYIID_KERNEL_GRAD_FQ) return ctx->grad_variant;
+  return -1;
 }
 
 }  // extern "C"

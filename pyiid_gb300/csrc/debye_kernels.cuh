@@ -39,7 +39,9 @@ __device__ __forceinline__ float4 load_atom(const float *__restrict__ pos,
 // ===================================================================== F(Q)
 // One CTA per work item (tile I, tiles [J0, J1) of one species pair).  Thread
 // (chunk c, group g) accumulates bins [kbase, kbase+L) over the pairs q = g,
-// g + n_groups, ... of every tile pair.  Per pair the record holds
+// g + n_groups, ... of every tile pair, NP pairs at a time (independent
+// recurrences interleaved for instruction-level parallelism).  Per pair the
+// record holds
 //   a = (th_hi, th_lo, lambda, sigma)
 //   b = (sin_th / r, -lambda / (2 r), 1 / r, 0)
 // so that the recurrence runs on t_k = sin(k theta_e) / r directly.
@@ -50,6 +52,24 @@ __device__ __forceinline__ float4 load_atom(const float *__restrict__ pos,
 // Dynamic shared memory: 2*32*32 float4 records + 2*L*blockDim floats; the
 // final FP64 reduction reuses the record space (n_chunks*L doubles <= 32 KB).
 template <int L>
+struct FqSeed {
+  float t, v, lam, sig;
+};
+
+template <int L>
+__device__ __forceinline__ FqSeed<L> fq_seed(const float4 &ra, const float4 &rb,
+                                             float kf, float mask) {
+  float s0, c0;
+  seed_sincos(kf, ra.x, ra.y, s0, c0);
+  FqSeed<L> z;
+  z.t = mask * (rb.z * s0);
+  z.v = mask * fmaf(rb.x, c0, rb.y * s0);
+  z.lam = ra.z;
+  z.sig = ra.w;
+  return z;
+}
+
+template <int L, int NP>
 __global__ void __launch_bounds__(kBlock, 2)
     fq_pair_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                    const int4 *__restrict__ tiles,
@@ -106,26 +126,31 @@ __global__ void __launch_bounds__(kBlock, 2)
                             p.inv_r, 0.f);
     }
     __syncthreads();
-    if (active) {
+    if (active && np > 0) {
       float acc[L];
 #pragma unroll
       for (int j = 0; j < L; ++j) acc[j] = 0.f;
-      for (int q = g; q < np; q += n_groups) {
-        const float4 ra = recA[q];
-        const float4 rb = recB[q];
-        float s0, c0;
-        seed_sincos(kf, ra.x, ra.y, s0, c0);
-        float t = rb.z * s0;
-        float v = fmaf(rb.x, c0, rb.y * s0);
-        acc[0] += t;
+      for (int q = g; q < np; q += NP * n_groups) {
+        FqSeed<L> z[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const int qq = q + p * n_groups;
+          const int qc = qq < np ? qq : np - 1;
+          z[p] = fq_seed<L>(recA[qc], recB[qc], kf, qq < np ? 1.f : 0.f);
+        }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) acc[0] += z[p].t;
 #pragma unroll
         for (int j = 1; j < L; ++j) {
-          v = fmaf(ra.z, t, v);
-          t = t + v;
-          if (j & 1)
-            acc[j] = fmaf(t, ra.w, acc[j]);
-          else
-            acc[j] += t;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            z[p].v = fmaf(z[p].lam, z[p].t, z[p].v);
+            z[p].t = z[p].t + z[p].v;
+            if (j & 1)
+              acc[j] = fmaf(z[p].t, z[p].sig, acc[j]);
+            else
+              acc[j] += z[p].t;
+          }
         }
       }
 #pragma unroll
@@ -208,7 +233,8 @@ __global__ void fq_finish_kernel(const double *__restrict__ partial,
 // Owner-computes: CTA (tile I, chunk block) with threads (atom a, chunk cl);
 // every thread sweeps all tiles J of its configuration and accumulates the
 // 3 x L gradient bins of its atom, so no atomics or partials are needed.
-// Records per (a in I, b in J):
+// Records per (a in I, b in J), stored [b][a] so the few atoms of a warp read
+// adjacent records (no bank conflicts):
 //   a = (th_hi, th_lo, lambda, sigma)
 //   b = (beta sin_th, -beta lambda / 2, beta, gamma')   beta = -1/r^3,
 //                                                        gamma' = -r dq/(2 sin_th)
@@ -216,16 +242,40 @@ __global__ void fq_finish_kernel(const double *__restrict__ partial,
 // With t, v scaled by beta, per bin
 //   g_k = sigma^k (k gamma' (v_k + v_{k+1}) + t_k) = (Q_k cos(Q_k r) - sin(Q_k r)/r)/r^2.
 // Per bin and ordered pair: 2 (recurrence) + 1 (u) + 1 (k gamma') + 1 (g) +
-// 3 (accumulate) = 8 FP32 instructions.
+// 3 (accumulate) = 8 FP32 instructions.  NP pairs are interleaved per thread.
 // At every species change of J (and at the end) the thread folds
 // coef[b][sa][sb][k] * acc into its own output rows.
-template <int L>
-__global__ void __launch_bounds__(kBlock, 2)
+struct GradState {
+  float t, v, kg, gam, lam, dx, dy, dz, sx, sy, sz;
+};
+
+__device__ __forceinline__ GradState grad_seed(const float4 &ra,
+                                               const float4 &rb,
+                                               const float4 &rc, float kf) {
+  float s0, c0;
+  seed_sincos(kf, ra.x, ra.y, s0, c0);
+  GradState z;
+  z.t = rb.z * s0;
+  z.v = fmaf(rb.x, c0, rb.y * s0);
+  z.kg = kf * rb.w;
+  z.gam = rb.w;
+  z.lam = ra.z;
+  z.dx = rc.x;
+  z.dy = rc.y;
+  z.dz = rc.z;
+  z.sx = ra.w * rc.x;
+  z.sy = ra.w * rc.y;
+  z.sz = ra.w * rc.z;
+  return z;
+}
+
+template <int L, int CPC, int NP, int MINB>
+__global__ void __launch_bounds__(kTile * CPC, MINB)
     gradfq_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                   const int4 *__restrict__ tiles,
                   const int2 *__restrict__ cfg_tiles, float dq_hi,
-                  float dq_lo, int kb0, int chunks_total, int chunks_per_cta,
-                  int n_bins, const float *__restrict__ coef, int n_species,
+                  float dq_lo, int kb0, int chunks_total, int n_bins,
+                  const float *__restrict__ coef, int n_species,
                   float *__restrict__ out) {
   extern __shared__ float4 smem[];
   float4 *recA = smem;
@@ -236,8 +286,8 @@ __global__ void __launch_bounds__(kBlock, 2)
   const int4 ti = tiles[blockIdx.x];
   const int2 ct = cfg_tiles[ti.z];
   const int tid = threadIdx.x;
-  const int al = tid / chunks_per_cta;
-  const int chunk = blockIdx.y * chunks_per_cta + tid % chunks_per_cta;
+  const int al = tid / CPC;
+  const int chunk = blockIdx.y * CPC + tid % CPC;
   const bool active = (al < ti.y) && (chunk < chunks_total);
   const int kbase = kb0 + chunk * L;
   const float kf = (float)kbase;
@@ -296,7 +346,7 @@ __global__ void __launch_bounds__(kBlock, 2)
     __syncthreads();
     const bool same = (tj == (int)blockIdx.x);
     for (int q = tid; q < kTile * kTile; q += blockDim.x) {
-      const int a = q / kTile, b = q % kTile;
+      const int b = q / kTile, a = q % kTile;
       float4 ra = make_float4(0.f, 0.f, 0.f, 1.f);
       float4 rb = make_float4(0.f, 0.f, 0.f, 0.f);
       float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -318,34 +368,34 @@ __global__ void __launch_bounds__(kBlock, 2)
     }
     __syncthreads();
     if (active) {
-      for (int b = 0; b < tJ.y; ++b) {
-        const int q = al * kTile + b;
-        const float4 ra = recA[q];
-        const float4 rb = recB[q];
-        const float4 rc = recC[q];
-        float s0, c0;
-        seed_sincos(kf, ra.x, ra.y, s0, c0);
-        float t = rb.z * s0;
-        float v = fmaf(rb.x, c0, rb.y * s0);
-        float kg = kf * rb.w;
-        const float sx = ra.w * rc.x, sy = ra.w * rc.y, sz = ra.w * rc.z;
+      // records beyond tJ.y are zero, so the NP-wide loop may run past it
+      for (int b = 0; b < tJ.y; b += NP) {
+        GradState z[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const int q = (b + p) * kTile + al;
+          z[p] = grad_seed(recA[q], recB[q], recC[q], kf);
+        }
 #pragma unroll
         for (int j = 0; j < L; ++j) {
-          const float vn = fmaf(ra.z, t, v);
-          const float u = v + vn;
-          const float gk = fmaf(kg, u, t);
-          if (j & 1) {
-            ax[j] = fmaf(gk, sx, ax[j]);
-            ay[j] = fmaf(gk, sy, ay[j]);
-            az[j] = fmaf(gk, sz, az[j]);
-          } else {
-            ax[j] = fmaf(gk, rc.x, ax[j]);
-            ay[j] = fmaf(gk, rc.y, ay[j]);
-            az[j] = fmaf(gk, rc.z, az[j]);
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float vn = fmaf(z[p].lam, z[p].t, z[p].v);
+            const float u = z[p].v + vn;
+            const float gk = fmaf(z[p].kg, u, z[p].t);
+            if (j & 1) {
+              ax[j] = fmaf(gk, z[p].sx, ax[j]);
+              ay[j] = fmaf(gk, z[p].sy, ay[j]);
+              az[j] = fmaf(gk, z[p].sz, az[j]);
+            } else {
+              ax[j] = fmaf(gk, z[p].dx, ax[j]);
+              ay[j] = fmaf(gk, z[p].dy, ay[j]);
+              az[j] = fmaf(gk, z[p].dz, az[j]);
+            }
+            z[p].t = z[p].t + vn;
+            z[p].v = vn;
+            z[p].kg += z[p].gam;
           }
-          t = t + vn;
-          v = vn;
-          kg += rb.w;
         }
       }
     }

@@ -228,3 +228,47 @@ def test_repeatable_bitwise(D):
     ga = D.grad_fq(pos, sp, tab, 0.05).cpu().numpy()
     gb = D.grad_fq(pos, sp, tab, 0.05).cpu().numpy()
     assert np.array_equal(ga, gb)
+
+
+@pytest.mark.parametrize('kernel', ['fq', 'grad_fq'])
+def test_every_launch_variant_matches_oracle(D, kernel):
+    """All autotuner variants compute the same (correct) result."""
+    from pyiid_gb300 import autotune
+    from pyiid_gb300._native import context
+    pos = S.random_cube(70, 11.0, 21)
+    nums = list(np.random.default_rng(21).choice([78, 79], 70))
+    qbin, nb, kb = 0.05, 500, 3
+    sp, tab, _ = species_tables(nums, qbin, nb)
+    ctx = context()
+    old = ctx.get_variant(kernel)
+    want_f = O.fq(pos, per_atom(sp, tab), qbin)
+    want_g = O.grad_fq(pos, per_atom(sp, tab), qbin)
+    try:
+        for idx, info in autotune.variants(kernel):
+            ctx.set_variant(kernel, idx)
+            if kernel == 'fq':
+                got = D.fq(pos, sp, tab, qbin, k_begin=kb).cpu().numpy()
+                assert rel(got[kb:], want_f[kb:]) <= TOL_F, (idx, info)
+            else:
+                got = D.grad_fq(pos, sp, tab, qbin, k_begin=kb).cpu().numpy()
+                assert rel(got[:, :, kb:], want_g[:, :, kb:]) <= TOL_G, (idx, info)
+    finally:
+        ctx.set_variant(kernel, old)
+
+
+def test_autotune_selects_and_caches(D, tmp_path, monkeypatch):
+    from pyiid_gb300 import autotune
+    from pyiid_gb300._native import context
+    monkeypatch.setenv('PYIID_GB300_TUNE_CACHE', str(tmp_path / 't.json'))
+    pos = S.random_cube(200, 14.0, 8)
+    sp, tab, _ = species_tables([79] * 200, 0.05, 300)
+    res = autotune.tune(pos, sp, tab, 0.05, 0, reps=1)
+    ctx = context()
+    assert ctx.get_variant('fq') == res['fq']['best']
+    assert ctx.get_variant('grad_fq') == res['grad_fq']['best']
+    ctx.set_variant('fq', 0)
+    ctx.set_variant('grad_fq', 0)
+    got = autotune.apply_cached(200, 300, 1)
+    assert got == {'fq': res['fq']['best'], 'grad_fq': res['grad_fq']['best']}
+    ctx.set_variant('fq', 0)
+    ctx.set_variant('grad_fq', 0)
