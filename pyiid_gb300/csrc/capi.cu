@@ -61,7 +61,10 @@ struct GradEntry {
   GradKernel k;
 };
 
+// NP == 0 marks the packed (FP32x2) even/odd kernels
 const FqEntry kFqTable[] = {
+    {{32, 0}, fq_pair2_kernel<32>},   {{48, 0}, fq_pair2_kernel<48>},
+    {{64, 0}, fq_pair2_kernel<64>},   {{24, 0}, fq_pair2_kernel<24>},
     {{32, 1}, fq_pair_kernel<32, 1>}, {{32, 2}, fq_pair_kernel<32, 2>},
     {{16, 1}, fq_pair_kernel<16, 1>}, {{16, 2}, fq_pair_kernel<16, 2>},
     {{24, 1}, fq_pair_kernel<24, 1>}, {{24, 2}, fq_pair_kernel<24, 2>},
@@ -70,6 +73,10 @@ const FqEntry kFqTable[] = {
 // (the last template argument is the minimum resident CTAs per SM, i.e. the
 // register budget: 2 x 256 threads -> 128 registers, 3 x 256 -> 85)
 const GradEntry kGradTable[] = {
+    {{32, 8, 0}, gradfq2_kernel<32, 8, 2>},
+    {{24, 8, 0}, gradfq2_kernel<24, 8, 2>},
+    {{16, 8, 0}, gradfq2_kernel<16, 8, 3>},
+    {{32, 16, 0}, gradfq2_kernel<32, 16, 1>},
     {{32, 8, 1}, gradfq_kernel<32, 8, 1, 2>},
     {{32, 16, 1}, gradfq_kernel<32, 16, 1, 1>},
     {{32, 4, 1}, gradfq_kernel<32, 4, 1, 4>},
@@ -801,15 +808,15 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
   LAUNCH_CHECK(ctx);
   const int kb0 = kmin & ~1;
   const int kp = std::max(kAdjRS, ((n_bins - kb0 + kAdjRS - 1) / kAdjRS) * kAdjRS);
-  const size_t ntab = (size_t)n_configs * n_species * n_species * 2 * kp;
-  TRY(ensure(ctx, "b_tabs", ntab * sizeof(float2), &p));
-  float2 *tabs = static_cast<float2 *>(p);
+  const size_t ntab = (size_t)n_configs * n_species * n_species * kp;
+  TRY(ensure(ctx, "b_tabs", ntab * sizeof(float4), &p));
+  float4 *tabs = static_cast<float4 *>(p);
   adjoint_table_kernel<<<256, 256, 0, ctx->stream>>>(
       w, d_na, d_ftab, n_species, n_bins, kmin, kb0, kp, n_configs, tabs);
   LAUNCH_CHECK(ctx);
   float dq_hi, dq_lo;
   split_double(qstep, dq_hi, dq_lo);
-  const size_t smem = (size_t)n_species * 2 * kp * sizeof(float2);
+  const size_t smem = (size_t)n_species * kp * sizeof(float4);
   if (smem > 160 * 1024)
     return fail(ctx, PYIID_ERR_INVALID_ARG,
                 "adjoint tables (%zu bytes) exceed shared memory", smem);

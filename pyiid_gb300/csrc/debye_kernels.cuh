@@ -403,26 +403,301 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
   if (cur_sb >= 0) flush(cur_sb, true);
 }
 
+// ============================================ packed (FP32x2) pair kernels
+// Same work decomposition as the kernels above, on the even/odd formulation
+// of pair_math.cuh: one packed instruction advances bins k and k+1.
+// F(Q) per two bins and pair: FFMA2 + FFMA2 (recurrence) + FADD2/FFMA2.
+// Records: a = (th_hi, th_lo, kappa, sigma2), b = (ch/r, sh/r, 1/r, 0).
+template <int L>
+__global__ void __launch_bounds__(kBlock, 2)
+    fq_pair2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                    const int4 *__restrict__ tiles,
+                    const int4 *__restrict__ items, float dq_hi, float dq_lo,
+                    int kb0, int n_chunks, int n_groups, int n_bins,
+                    double *__restrict__ partial) {
+  static_assert(L % 2 == 0, "L must be even");
+  constexpr int M = L / 2;
+  extern __shared__ float4 smem[];
+  float4 *recA = smem;
+  float4 *recB = smem + kTile * kTile;
+  float *kS = reinterpret_cast<float *>(smem + 2 * kTile * kTile);
+  float *kC = kS + L * blockDim.x;
+  __shared__ float4 sI[kTile], sJ[kTile];
+
+  const int4 it = items[blockIdx.x];
+  const int4 ti = tiles[it.x];
+  const int tid = threadIdx.x;
+  const int c = tid % n_chunks;
+  const int g = tid / n_chunks;
+  const bool active = g < n_groups;
+  const int kbase = kb0 + (blockIdx.y * n_chunks + c) * L;
+  const float kf = (float)kbase;
+
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+#pragma unroll
+  for (int j = 0; j < L; ++j) {
+    kS[j * blockDim.x + tid] = 0.f;
+    kC[j * blockDim.x + tid] = 0.f;
+  }
+
+  for (int tj = it.y; tj < it.z; ++tj) {
+    const int4 tJ = tiles[tj];
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool diag = (tj == it.x);
+    const int np = diag ? ti.y * (ti.y - 1) / 2 : ti.y * tJ.y;
+    for (int q = tid; q < np; q += blockDim.x) {
+      int a, b;
+      if (diag) {
+        tri_index(q, a, b);
+      } else {
+        a = q / tJ.y;
+        b = q - a * tJ.y;
+      }
+      const float4 pa = sI[a];
+      const float4 pb = diag ? sI[b] : sJ[b];
+      float dx, dy, dz;
+      PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                 dq_lo, dx, dy, dz);
+      recA[q] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
+      recB[q] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
+    }
+    __syncthreads();
+    if (active && np > 0) {
+      float2 acc[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) acc[m] = f2(0.f);
+      for (int q = g; q < np; q += n_groups) {
+        const float4 ra = recA[q];
+        const float4 rb = recB[q];
+        float2 s, co;
+        seed_sincos2(kf, ra.x, ra.y, s, co);
+        float2 t = __fmul2_rn(f2(rb.z), s);
+        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+        const float2 kp = f2(ra.z), km = f2(-ra.z), sg = f2(ra.w);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          acc[m] = (m & 1) ? __ffma2_rn(t, sg, acc[m]) : __fadd2_rn(acc[m], t);
+          if (m + 1 < M) {
+            w = __ffma2_rn(km, t, w);
+            t = __ffma2_rn(kp, w, t);
+          }
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int j = 2 * m + e;
+          const float a = e ? acc[m].y : acc[m].x;
+          const float Sj = kS[j * blockDim.x + tid];
+          const float y = __fsub_rn(a, kC[j * blockDim.x + tid]);
+          const float sum = __fadd_rn(Sj, y);
+          kC[j * blockDim.x + tid] = __fsub_rn(__fsub_rn(sum, Sj), y);
+          kS[j * blockDim.x + tid] = sum;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  double *red = reinterpret_cast<double *>(smem);
+  for (int gg = 0; gg < n_groups; ++gg) {
+    if (active && g == gg) {
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const double v = (double)kS[j * blockDim.x + tid] -
+                         (double)kC[j * blockDim.x + tid];
+        red[c * L + j] = (gg == 0) ? v : red[c * L + j] + v;
+      }
+    }
+    __syncthreads();
+  }
+  const int nk = n_chunks * L;
+  const int kfirst = kb0 + blockIdx.y * nk;
+  double *out = partial + (size_t)blockIdx.x * n_bins;
+  for (int i = tid; i < nk; i += blockDim.x) {
+    const int k = kfirst + i;
+    if (k < n_bins) out[k] = red[i];
+  }
+}
+
+// dF/dx, packed.  Records per (a, b), stored [b][a]:
+//   a = (th_hi, th_lo, kappa, sigma2)
+//   b = (beta ch, beta sh, beta, gamma')   beta = -1/r^3, gamma' = -r dq/(2 ch)
+//   c = (dx, dy, dz, 0)
+// Per two bins and ordered pair: FFMA2 (w) + FADD2 (u) + FFMA2 (g) +
+// 3 FFMA2 (accumulate) + FFMA2 (t) + FADD2 (k gamma') = 8 instructions.
+template <int L, int CPC, int MINB>
+__global__ void __launch_bounds__(kTile * CPC, MINB)
+    gradfq2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                   const int4 *__restrict__ tiles,
+                   const int2 *__restrict__ cfg_tiles, float dq_hi,
+                   float dq_lo, int kb0, int chunks_total, int n_bins,
+                   const float *__restrict__ coef, int n_species,
+                   float *__restrict__ out) {
+  static_assert(L % 2 == 0, "L must be even");
+  constexpr int M = L / 2;
+  extern __shared__ float4 smem[];
+  float4 *recA = smem;
+  float4 *recB = smem + kTile * kTile;
+  float4 *recC = smem + 2 * kTile * kTile;
+  __shared__ float4 sI[kTile], sJ[kTile];
+
+  const int4 ti = tiles[blockIdx.x];
+  const int2 ct = cfg_tiles[ti.z];
+  const int tid = threadIdx.x;
+  const int al = tid / CPC;
+  const int chunk = blockIdx.y * CPC + tid % CPC;
+  const bool active = (al < ti.y) && (chunk < chunks_total);
+  const int kbase = kb0 + chunk * L;
+  const float kf = (float)kbase;
+
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+
+  float2 ax[M], ay[M], az[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    ax[m] = f2(0.f);
+    ay[m] = f2(0.f);
+    az[m] = f2(0.f);
+  }
+  int cur_sb = -1;
+  bool first_flush = true;
+  const int out_row = active ? perm[ti.x + al] : 0;
+
+  auto flush = [&](int sb, bool last) {
+    if (!active) return;
+    const float *cf =
+        coef + (((size_t)ti.z * n_species + ti.w) * n_species + sb) * n_bins;
+    float *o = out + (size_t)out_row * 3 * n_bins;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int k = kbase + 2 * m + e;
+        if (k < n_bins) {
+          const float w = cf[k];
+          float vx = w * (e ? ax[m].y : ax[m].x);
+          float vy = w * (e ? ay[m].y : ay[m].x);
+          float vz = w * (e ? az[m].y : az[m].x);
+          if (!first_flush) {
+            vx += o[k];
+            vy += o[n_bins + k];
+            vz += o[2 * n_bins + k];
+          }
+          if (last) {
+            vx = isnan(vx) ? 0.f : (isinf(vx) ? copysignf(3.402823466e38f, vx) : vx);
+            vy = isnan(vy) ? 0.f : (isinf(vy) ? copysignf(3.402823466e38f, vy) : vy);
+            vz = isnan(vz) ? 0.f : (isinf(vz) ? copysignf(3.402823466e38f, vz) : vz);
+          }
+          o[k] = vx;
+          o[n_bins + k] = vy;
+          o[2 * n_bins + k] = vz;
+        }
+      }
+      ax[m] = f2(0.f);
+      ay[m] = f2(0.f);
+      az[m] = f2(0.f);
+    }
+    first_flush = false;
+  };
+
+  for (int tj = ct.x; tj < ct.y; ++tj) {
+    const int4 tJ = tiles[tj];
+    if (cur_sb >= 0 && tJ.w != cur_sb) flush(cur_sb, false);
+    cur_sb = tJ.w;
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool same = (tj == (int)blockIdx.x);
+    for (int q = tid; q < kTile * kTile; q += blockDim.x) {
+      const int b = q / kTile, a = q % kTile;
+      float4 ra = make_float4(0.f, 0.f, 0.f, 1.f);
+      float4 rb = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (a < ti.y && b < tJ.y && !(same && a == b)) {
+        const float4 pa = sI[a];
+        const float4 pb = sJ[b];
+        float dx, dy, dz;
+        PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                   dq_lo, dx, dy, dz);
+        const float beta = -(p.inv_r * p.inv_r * p.inv_r);
+        const float gam = -p.r * dq_hi / (2.0f * p.ch);
+        ra = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
+        rb = make_float4(beta * p.ch, beta * p.sh, beta, gam);
+        rc = make_float4(dx, dy, dz, 0.f);
+      }
+      recA[q] = ra;
+      recB[q] = rb;
+      recC[q] = rc;
+    }
+    __syncthreads();
+    if (active) {
+      for (int b = 0; b < tJ.y; ++b) {
+        const int q = b * kTile + al;
+        const float4 ra = recA[q];
+        const float4 rb = recB[q];
+        const float4 rc = recC[q];
+        float2 s, co;
+        seed_sincos2(kf, ra.x, ra.y, s, co);
+        float2 t = __fmul2_rn(f2(rb.z), s);
+        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+        float2 kg = make_float2(kf * rb.w, (kf + 1.0f) * rb.w);
+        const float2 dkg = f2(2.0f * rb.w);
+        const float2 kp = f2(ra.z), km = f2(-ra.z);
+        const float2 dx2 = f2(rc.x), dy2 = f2(rc.y), dz2 = f2(rc.z);
+        const float2 sx2 = f2(ra.w * rc.x), sy2 = f2(ra.w * rc.y),
+                     sz2 = f2(ra.w * rc.z);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          const float2 wn = __ffma2_rn(km, t, w);
+          const float2 u = __fadd2_rn(w, wn);
+          const float2 gk = __ffma2_rn(kg, u, t);
+          if (m & 1) {
+            ax[m] = __ffma2_rn(gk, sx2, ax[m]);
+            ay[m] = __ffma2_rn(gk, sy2, ay[m]);
+            az[m] = __ffma2_rn(gk, sz2, az[m]);
+          } else {
+            ax[m] = __ffma2_rn(gk, dx2, ax[m]);
+            ay[m] = __ffma2_rn(gk, dy2, ay[m]);
+            az[m] = __ffma2_rn(gk, dz2, az[m]);
+          }
+          t = __ffma2_rn(kp, wn, t);
+          w = wn;
+          kg = __fadd2_rn(kg, dkg);
+        }
+      }
+    }
+  }
+  if (cur_sb >= 0) flush(cur_sb, true);
+}
+
 // =================================================================== adjoint
 // d(potential)/dx_a = sum_b (x_a - x_b) s_ab,  s_ab = sum_k W^{sa sb}_k g_k(r_ab)
 // with W_k = 2 w_k f_sa f_sb / na_k and w = T c the back-projected G(r)
 // adjoint.  Owner-computes: CTA = tile I, thread (atom a = lane, group =
 // warp); group gp handles b = gp, gp + 8, ... of every tile J, so the lanes of
 // a warp share b and the weight tables are broadcast reads.
-// Tables hold, for sigma = +1 and -1, A_k = k W_k sigma^k, B_k = W_k sigma^k as
-// float2, padded with zeros to kp bins (a multiple of the re-seed period RS):
-//   s_ab = gamma' sum_k A_k (v_k + v_{k+1}) + sum_k B_k t_k   (t, v scaled by beta)
-// Per bin and ordered pair: 2 (recurrence) + 1 (u) + 2 (accumulate) FP32
-// instructions and half an LDS.128.
+// Packed even/odd recurrence (pair_math.cuh); per re-seed block of RS bins
+// starting at kb0 + blk (RS a multiple of 4).  Tables hold, for sigma2 = +1
+// and -1 and every bin pair (kk, kk+1), kk = k - kb0 even:
+//   (A_kk, A_kk+1, B_kk, B_kk+1),  A_k = k W_k s_k, B_k = W_k s_k,
+//   s_k = sigma2^(kk/2)
+// so that, with t, w scaled by beta = -1/r^3 and gamma' = -r dq/(2 ch),
+//   s_ab = gamma' sum_k A_k (w_m + w_{m+1}) + sum_k B_k t_m.
+// Per two bins and ordered pair: FFMA2 + FADD2 + 2 FFMA2 + FFMA2 = 5 packed
+// instructions and one LDS.128.
 template <int RS>
 __global__ void __launch_bounds__(kBlock)
     adjoint_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                    const int4 *__restrict__ tiles,
                    const int2 *__restrict__ cfg_tiles, float dq_hi,
                    float dq_lo, int kb0, int kp,
-                   const float2 *__restrict__ tabs, int n_species,
+                   const float4 *__restrict__ tabs, int n_species,
                    float *__restrict__ grad) {
-  extern __shared__ float2 stab[];  // [n_species][2][kp]
+  static_assert(RS % 4 == 0, "RS must be a multiple of 4");
+  extern __shared__ float4 stab[];  // [n_species][2][kp/2]
   __shared__ float4 sI[kTile], sJ[kTile];
   __shared__ float sred[kBlock / kTile][kTile][3];
 
@@ -432,11 +707,11 @@ __global__ void __launch_bounds__(kBlock)
   const int lane = tid % kTile;
   const int grp = tid / kTile;
   const int ngrp = blockDim.x / kTile;
+  const int kh = kp / 2;
 
-  // this tile's tables: [sb][sigma][kp] for (config, sa)
-  const float2 *src =
-      tabs + ((size_t)ti.z * n_species + ti.w) * n_species * 2 * kp;
-  for (int i = tid; i < n_species * 2 * kp; i += blockDim.x) stab[i] = src[i];
+  const float4 *src =
+      tabs + ((size_t)ti.z * n_species + ti.w) * n_species * 2 * kh;
+  for (int i = tid; i < n_species * 2 * kh; i += blockDim.x) stab[i] = src[i];
   if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
 
   float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -446,46 +721,40 @@ __global__ void __launch_bounds__(kBlock)
     if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
     __syncthreads();
     const bool same = (tj == (int)blockIdx.x);
-    const float2 *tb = stab + (size_t)tJ.w * 2 * kp;
+    const float4 *tb = stab + (size_t)tJ.w * 2 * kh;
     if (lane < ti.y) {
       const float4 pa = sI[lane];
       for (int b = grp; b < tJ.y; b += ngrp) {
         if (same && b == lane) continue;
         const float4 pb = sJ[b];
         float dx, dy, dz;
-        PairPhase p = pair_phase(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
-                                 dq_lo, dx, dy, dz);
+        PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                   dq_lo, dx, dy, dz);
         const float beta = -(p.inv_r * p.inv_r * p.inv_r);
-        const float c1 = beta * p.sin_th;
-        const float c2 = -0.5f * p.lam * beta;
-        const float gam = -p.r * dq_hi / (2.0f * p.sin_th);
-        const float4 *tab4 = reinterpret_cast<const float4 *>(
-            tb + (p.sigma > 0.f ? 0 : kp));
-        float acc1 = 0.f, acc2 = 0.f;
+        const float2 c1 = f2(beta * p.ch), c2 = f2(beta * p.sh);
+        const float gam = -p.r * dq_hi / (2.0f * p.ch);
+        const float2 kpos = f2(p.kappa), kneg = f2(-p.kappa);
+        const float4 *tab = tb + (p.sigma2 > 0.f ? 0 : kh);
+        float2 a1 = f2(0.f), a2 = f2(0.f);
         for (int blk = 0; blk < kp; blk += RS) {
-          float s0, c0;
-          seed_sincos((float)(kb0 + blk), p.th_hi, p.th_lo, s0, c0);
-          float t = beta * s0;
-          float v = fmaf(c1, c0, c2 * s0);
+          float2 s, co;
+          seed_sincos2((float)(kb0 + blk), p.th_hi, p.th_lo, s, co);
+          float2 t = __fmul2_rn(f2(beta), s);
+          float2 w = __ffma2_rn(co, c1, __fmul2_rn(s, c2));
 #pragma unroll
-          for (int j = 0; j < RS; j += 2) {
-            const float4 w = tab4[(blk + j) >> 1];
-            float vn = fmaf(p.lam, t, v);
-            acc1 = fmaf(w.x, v + vn, acc1);
-            acc2 = fmaf(w.y, t, acc2);
-            t = t + vn;
-            v = vn;
-            vn = fmaf(p.lam, t, v);
-            acc1 = fmaf(w.z, v + vn, acc1);
-            acc2 = fmaf(w.w, t, acc2);
-            t = t + vn;
-            v = vn;
+          for (int m = 0; m < RS / 2; ++m) {
+            const float4 wt = tab[(blk >> 1) + m];
+            const float2 wn = __ffma2_rn(kneg, t, w);
+            a1 = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), a1);
+            a2 = __ffma2_rn(make_float2(wt.z, wt.w), t, a2);
+            t = __ffma2_rn(kpos, wn, t);
+            w = wn;
           }
         }
-        const float s = fmaf(gam, acc1, acc2);
-        gx = fmaf(s, dx, gx);
-        gy = fmaf(s, dy, gy);
-        gz = fmaf(s, dz, gz);
+        const float sab = fmaf(gam, a1.x + a1.y, a2.x + a2.y);
+        gx = fmaf(sab, dx, gx);
+        gy = fmaf(sab, dy, gy);
+        gz = fmaf(sab, dz, gz);
       }
     }
   }
@@ -495,9 +764,9 @@ __global__ void __launch_bounds__(kBlock)
   __syncthreads();
   if (tid < ti.y * 3) {
     const int a = tid / 3, cpt = tid % 3;
-    float s = 0.f;
-    for (int gg = 0; gg < ngrp; ++gg) s += sred[gg][a][cpt];
-    grad[(size_t)perm[ti.x + a] * 3 + cpt] = s;
+    float sum = 0.f;
+    for (int gg = 0; gg < ngrp; ++gg) sum += sred[gg][a][cpt];
+    grad[(size_t)perm[ti.x + a] * 3 + cpt] = sum;
   }
 }
 

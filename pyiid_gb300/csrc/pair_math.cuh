@@ -139,4 +139,87 @@ __device__ __forceinline__ void seed_sincos(float k0, float th_hi, float th_lo,
   __sincosf(x, &s, &c);
 }
 
+// ---------------------------------------------------------------------------
+// Packed even/odd formulation (FP32x2 instructions of sm_100+).
+//
+// The bins k = k0 + 2m + e (e = 0, 1) of one pair are two interleaved
+// sinusoids in m with step 2*theta.  Folding 2*theta = theta2 + M*pi with
+// theta2 in [-pi/2, pi/2] and sigma2 = (-1)^M gives
+//   sin(k theta) = sigma2^m sin(phi_e + m theta2),  phi_e = (k0 + e) theta,
+//   cos(k theta) = sigma2^m cos(phi_e + m theta2),
+// and both slots advance with one packed instruction pair of the Minsky
+// ("magic circle") recurrence with kappa = 2 sin(theta2/2):
+//   w_{m+1} = w_m - kappa t_m,   t_{m+1} = t_m + kappa w_{m+1},
+//   t_m = sin(phi + m theta2),   w_m = cos(phi + (m - 1/2) theta2).
+// Its matrix has determinant 1 (rounding does not grow the amplitude) and it
+// yields the cosine without any 1/sin(theta) factor:
+//   cos(phi + m theta2) = (w_m + w_{m+1}) / (2 cos(theta2/2)).
+struct PairPhase2 {
+  float th_hi, th_lo;   // theta = dq * r (unfolded), seeds use it
+  float sigma2;         // (-1)^M
+  float kappa;          // 2 sin(theta2 / 2)
+  float sh, ch;         // sin, cos of theta2 / 2
+  float r, inv_r;
+};
+
+__device__ __forceinline__ PairPhase2 pair_phase2(float ax, float ay, float az,
+                                                  float bx, float by, float bz,
+                                                  float dq_hi, float dq_lo,
+                                                  float &dx, float &dy,
+                                                  float &dz) {
+  PairPhase2 p;
+  float xl, yl, zl;
+  two_sum(ax, -bx, dx, xl);
+  two_sum(ay, -by, dy, yl);
+  two_sum(az, -bz, dz, zl);
+  float s0, e0, s1, e1, s2, e2;
+  two_prod(dx, dx, s0, e0);
+  two_prod(dy, dy, s1, e1);
+  two_prod(dz, dz, s2, e2);
+  float h, l, h2, l2;
+  two_sum(s0, s1, h, l);
+  two_sum(h, s2, h2, l2);
+  float lo = l + l2 + e0 + e1 + e2 + 2.0f * (dx * xl + dy * yl + dz * zl);
+  float r2h, r2l;
+  fast_two_sum(h2, lo, r2h, r2l);
+  float rh = __fsqrt_rn(r2h);
+  float res = __fmaf_rn(-rh, rh, r2h);
+  float rl = __fmul_rn(__fadd_rn(res, r2l), __fdiv_rn(0.5f, rh));
+  float th, tl;
+  two_prod(dq_hi, rh, th, tl);
+  tl = __fadd_rn(tl, __fmaf_rn(dq_hi, rl, __fmul_rn(dq_lo, rh)));
+  fast_two_sum(th, tl, th, tl);
+  p.th_hi = th;
+  p.th_lo = tl;
+  // theta2 = 2 theta - M pi (doubling is exact)
+  const float t2h = 2.0f * th, t2l = 2.0f * tl;
+  float m = rintf(__fmul_rn(t2h, kInvPi));
+  float x = __fmaf_rn(-m, kPiA, t2h);
+  float y = __fmaf_rn(-m, kPiC, __fmaf_rn(-m, kPiB, t2l));
+  float q_hi, q_lo;
+  two_sum(x, y, q_hi, q_lo);
+  int mi = (int)m;
+  p.sigma2 = (mi & 1) ? -1.0f : 1.0f;
+  float hs, hc;
+  sincosf(0.5f * q_hi, &hs, &hc);
+  const float hl = 0.5f * q_lo;
+  p.sh = __fmaf_rn(hc, hl, hs);
+  p.ch = __fmaf_rn(-hs, hl, hc);
+  p.kappa = 2.0f * p.sh;
+  p.r = rh;
+  p.inv_r = __frcp_rn(rh);
+  return p;
+}
+
+// Seeds of both slots: (sin, cos) of k0*theta and (k0+1)*theta, each phase a
+// float pair reduced modulo 2*pi as in seed_sincos.
+__device__ __forceinline__ void seed_sincos2(float k0, float th_hi,
+                                             float th_lo, float2 &s,
+                                             float2 &c) {
+  seed_sincos(k0, th_hi, th_lo, s.x, c.x);
+  seed_sincos(k0 + 1.0f, th_hi, th_lo, s.y, c.y);
+}
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
 }  // namespace pyiid

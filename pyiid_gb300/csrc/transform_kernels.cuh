@@ -140,38 +140,43 @@ __global__ void wvec_kernel(const float *__restrict__ T,
   if (lane == 0) w[(size_t)b * n_bins + k] = acc;
 }
 
-// Adjoint tables: tabs[b][sa][sb][sigma][kk] = (A, B),
-//   k = kb0 + kk, W = 2 w_k f_sa f_sb / na_k (0 outside [kmin, n_bins) or
-//   where na_k = 0), A = k W sigma^k, B = W sigma^k.
+// Adjoint tables: tabs[b][sa][sb][sigma2][m] = (A_kk, A_kk+1, B_kk, B_kk+1),
+//   kk = 2m, k = kb0 + kk, W = 2 w_k f_sa f_sb / na_k (0 outside
+//   [kmin, n_bins) or where na_k = 0), s_k = sigma2^m, A = k W s_k, B = W s_k.
 __global__ void adjoint_table_kernel(const double *__restrict__ w,
                                      const double *__restrict__ na,
                                      const float *__restrict__ ftab,
                                      int n_species, int n_bins, int kmin,
                                      int kb0, int kp, int n_configs,
-                                     float2 *__restrict__ tabs) {
-  const size_t total = (size_t)n_configs * n_species * n_species * kp;
+                                     float4 *__restrict__ tabs) {
+  const int kh = kp / 2;
+  const size_t total = (size_t)n_configs * n_species * n_species * kh;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
        idx += (size_t)gridDim.x * blockDim.x) {
-    const int kk = idx % kp;
-    size_t rest = idx / kp;
+    const int m = idx % kh;
+    size_t rest = idx / kh;
     const int sb = rest % n_species;
     rest /= n_species;
     const int sa = rest % n_species;
     const int b = (int)(rest / n_species);
-    const int k = kb0 + kk;
-    double W = 0.0;
-    if (k >= kmin && k < n_bins) {
-      const double nak = na[(size_t)b * n_bins + k];
-      if (nak != 0.0)
-        W = 2.0 * w[(size_t)b * n_bins + k] * (double)ftab[sa * n_bins + k] *
-            (double)ftab[sb * n_bins + k] / nak;
+    float A[2], B[2];
+    for (int e = 0; e < 2; ++e) {
+      const int k = kb0 + 2 * m + e;
+      double W = 0.0;
+      if (k >= kmin && k < n_bins) {
+        const double nak = na[(size_t)b * n_bins + k];
+        if (nak != 0.0)
+          W = 2.0 * w[(size_t)b * n_bins + k] * (double)ftab[sa * n_bins + k] *
+              (double)ftab[sb * n_bins + k] / nak;
+      }
+      A[e] = (float)((double)k * W);
+      B[e] = (float)W;
     }
-    const float Wp = (float)W;
-    const float Wm = (k & 1) ? -Wp : Wp;
-    const float kf = (float)k;
-    float2 *base = tabs + ((((size_t)b * n_species + sa) * n_species + sb) * 2) * kp;
-    base[kk] = make_float2(kf * Wp, Wp);
-    base[kp + kk] = make_float2(kf * Wm, Wm);
+    float4 *base =
+        tabs + ((((size_t)b * n_species + sa) * n_species + sb) * 2) * kh;
+    base[m] = make_float4(A[0], A[1], B[0], B[1]);
+    const float sg = (m & 1) ? -1.f : 1.f;
+    base[kh + m] = make_float4(sg * A[0], sg * A[1], sg * B[0], sg * B[1]);
   }
 }
 
