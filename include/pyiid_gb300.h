@@ -188,6 +188,30 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
                                double *energy, float *grad, double *gcalc,
                                float *fq);
 
+/* F(Q) without device allocation.
+ *
+ * Same arguments, result and error behaviour as pyiid_fq, for callers that
+ * cannot allocate device memory (a process whose device memory is owned by
+ * another framework's pool, code inside a stream capture of a pre-sized
+ * graph, hosts without a device allocator).  All device-side intermediates
+ * live in one fixed 32 MiB device array inside the library, which every GPU
+ * that loads the library holds until the process exits; the call performs no
+ * cudaMalloc or cudaFree.  Problems whose intermediates exceed the array
+ * (about 8 * n_bins bytes per work item, i.e. per pair of 32-atom tiles
+ * spanning up to 32 tiles, plus small per-atom tables) are rejected with
+ * PYIID_ERR_INVALID_ARG and a message naming the size needed.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The call returns when fq is ready (it synchronizes the context stream).
+ * Every call reuses the same array and overwrites everything it reads, so
+ * results never depend on earlier calls, but calls that overlap on the GPU
+ * (other streams or threads) race on it: serialize them.
+ * No counterpart in the reference (its processors allocate per call). */
+int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
+                     const int32_t *species, int n_atoms, const float *scatter,
+                     int n_species, int n_bins, double qbin, int k_begin,
+                     float *fq);
+
 /* ------------------------------------------------------------------------ *
  * Launch-shape variants (autotuning).
  *

@@ -46,6 +46,8 @@ _SIGNATURES = {
     'pyiid_batch_potential_grad': (_c_int, [
         _vp, _vp, _i32p, _i32p, _c_int, _f32p, _c_int, _c_int, _c_dbl,
         _c_dbl, _f64p, _c_int, _c_dbl, _vp, _c_int, _vp, _vp, _vp, _vp]),
+    'pyiid_fq_noalloc': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
+                                  _c_int, _c_dbl, _c_int, _vp]),
     'pyiid_variant_count': (_c_int, [_c_int]),
     'pyiid_variant_info': (_c_int, [_c_int, _c_int, _i32p, _c_int]),
     'pyiid_set_variant': (_c_int, [_vp, _c_int, _c_int]),

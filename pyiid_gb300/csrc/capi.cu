@@ -881,3 +881,182 @@ int pyiid_get_variant(const pyiid_ctx *ctx, int kernel) {
 }
 
 }  // extern "C"
+
+// ===================================================================== F(Q)
+// without device allocation.
+//
+// Some callers cannot allocate device memory: code running inside a CUDA
+// graph capture or a pre-reserved memory pool, inference servers whose
+// allocator owns all device memory, or embedded hosts without a device
+// allocator at all.  pyiid_fq_noalloc computes exactly what pyiid_fq computes
+// but keeps every device-side intermediate (atom order, tiles, work items,
+// form factors, normalisation, per-item partial sums) in one file-scope
+// device array of fixed size instead of context workspace buffers.
+namespace {
+
+constexpr size_t kNoAllocBytes = 32u << 20;  // 32 MiB, held per loaded device
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};  // device address of the array, per device
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
+                                const int32_t *species, int n_atoms,
+                                const float *scatter, int n_species,
+                                int n_bins, double qbin, int k_begin,
+                                float *fq) {
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  const int32_t offsets[2] = {0, n_atoms};
+  TRY(check_common(ctx, 1, offsets, n_species, n_bins, qbin, k_begin));
+  if (ctx->device < 0 || ctx->device >= 64)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "device id %d >= 64", ctx->device);
+  for (int i = 0; i < n_atoms; ++i)
+    if (species[i] < 0 || species[i] >= n_species)
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "species[%d] = %d outside [0, %d)", i, species[i], n_species);
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  // one-time set-up per device: the device address of the scratch array
+  void *base;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[ctx->device]) {
+      void *p = nullptr;
+      CUDA_TRY(ctx, cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      g_noalloc_ptr[ctx->device] = p;
+    }
+    base = g_noalloc_ptr[ctx->device];
+  }
+  // host-side layout of the single configuration (same rules as get_layout)
+  const int n_spairs = n_species * (n_species + 1) / 2;
+  std::vector<int> count(n_species, 0), start(n_species, 0), perm(n_atoms);
+  for (int i = 0; i < n_atoms; ++i) count[species[i]]++;
+  for (int s = 1; s < n_species; ++s) start[s] = start[s - 1] + count[s - 1];
+  {
+    std::vector<int> fillp = start;
+    for (int i = 0; i < n_atoms; ++i) perm[fillp[species[i]]++] = i;
+  }
+  std::vector<int4> tiles;
+  for (int s = 0; s < n_species; ++s)
+    for (int a = 0; a < count[s]; a += kTile)
+      tiles.push_back(make_int4(start[s] + a, std::min(kTile, count[s] - a), 0, s));
+  std::vector<int4> items;
+  for (int I = 0; I < (int)tiles.size(); ++I) {
+    int J = 0;
+    while (J <= I) {
+      const int sJ = tiles[J].w;
+      int Je = J;
+      while (Je <= I && tiles[Je].w == sJ && Je - J < kJMax) ++Je;
+      const int sI = tiles[I].w;
+      items.push_back(make_int4(I, J, Je, sI * (sI + 1) / 2 + sJ));
+      J = Je;
+    }
+  }
+  std::stable_sort(items.begin(), items.end(),
+                   [](const int4 &a, const int4 &b) { return a.w < b.w; });
+  std::vector<int> key_begin(n_spairs + 1, 0);
+  for (const int4 &it : items) key_begin[it.w + 1]++;
+  for (int k = 0; k < n_spairs; ++k) key_begin[k + 1] += key_begin[k];
+  std::vector<int2> spair;
+  for (int sa = 0; sa < n_species; ++sa)
+    for (int sb = 0; sb <= sa; ++sb) spair.push_back(make_int2(sa, sb));
+  std::vector<double> na(n_bins);
+  {
+    const double n = n_atoms, P = n * (n - 1) / 2;
+    for (int k = 0; k < n_bins; ++k) {
+      double s = 0.0;
+      for (int sp = 0; sp < n_spairs; ++sp) {
+        const int sa = spair[sp].x, sb = spair[sp].y;
+        const double pc = (sa == sb) ? (double)count[sa] * (count[sa] - 1) / 2
+                                     : (double)count[sa] * count[sb];
+        s += pc * (double)scatter[(size_t)sa * n_bins + k] *
+             (double)scatter[(size_t)sb * n_bins + k];
+      }
+      na[k] = (P > 0) ? n * s / P : NAN;
+    }
+  }
+  // carve the scratch array
+  const int n_items = (int)items.size();
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = align256(off + std::max<size_t>(bytes, 1));
+    return o;
+  };
+  const size_t o_perm = carve(sizeof(int) * perm.size());
+  const size_t o_tiles = carve(sizeof(int4) * tiles.size());
+  const size_t o_items = carve(sizeof(int4) * items.size());
+  const size_t o_keys = carve(sizeof(int) * key_begin.size());
+  const size_t o_spair = carve(sizeof(int2) * spair.size());
+  const size_t o_ftab = carve(sizeof(float) * (size_t)n_species * n_bins);
+  const size_t o_na = carve(sizeof(double) * (size_t)n_bins);
+  const size_t o_part = carve(sizeof(double) * (size_t)n_items * n_bins);
+  if (off > kNoAllocBytes)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "pyiid_fq_noalloc needs %zu bytes of scratch for %d atoms x %d "
+                "bins; the fixed scratch array holds %zu bytes (use pyiid_fq)",
+                off, n_atoms, n_bins, kNoAllocBytes);
+  unsigned char *sb = static_cast<unsigned char *>(base);
+  int *d_perm = reinterpret_cast<int *>(sb + o_perm);
+  int4 *d_tiles = reinterpret_cast<int4 *>(sb + o_tiles);
+  int4 *d_items = reinterpret_cast<int4 *>(sb + o_items);
+  int *d_keys = reinterpret_cast<int *>(sb + o_keys);
+  int2 *d_spair = reinterpret_cast<int2 *>(sb + o_spair);
+  float *d_ftab = reinterpret_cast<float *>(sb + o_ftab);
+  double *d_na = reinterpret_cast<double *>(sb + o_na);
+  double *d_part = reinterpret_cast<double *>(sb + o_part);
+  cudaStream_t st = ctx->stream;
+  // synchronous-to-host copies: the host vectors die at return
+  if (!perm.empty())
+    CUDA_TRY(ctx, cudaMemcpyAsync(d_perm, perm.data(), sizeof(int) * perm.size(),
+                                  cudaMemcpyHostToDevice, st));
+  if (!tiles.empty())
+    CUDA_TRY(ctx, cudaMemcpyAsync(d_tiles, tiles.data(),
+                                  sizeof(int4) * tiles.size(),
+                                  cudaMemcpyHostToDevice, st));
+  if (!items.empty())
+    CUDA_TRY(ctx, cudaMemcpyAsync(d_items, items.data(),
+                                  sizeof(int4) * items.size(),
+                                  cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_keys, key_begin.data(),
+                                sizeof(int) * key_begin.size(),
+                                cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_spair, spair.data(),
+                                sizeof(int2) * spair.size(),
+                                cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_ftab, scatter,
+                                sizeof(float) * (size_t)n_species * n_bins,
+                                cudaMemcpyHostToDevice, st));
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_na, na.data(), sizeof(double) * na.size(),
+                                cudaMemcpyHostToDevice, st));
+  // pair sums into the partial rows, then the FP64 finish (as run_fq does)
+  float dq_hi, dq_lo;
+  split_double(qbin, dq_hi, dq_lo);
+  const int kb0 = std::min(k_begin, n_bins) & ~1;
+  if (n_items > 0 && kb0 < n_bins) {
+    const FqEntry &E = kFqTable[ctx->fq_variant];
+    const int Lb = E.v.L;
+    const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    const int max_chunks = std::min(128, 32768 / (8 * Lb));
+    const int n_cb = (chunks_total + max_chunks - 1) / max_chunks;
+    const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
+    const int n_groups = kBlock / n_chunks;
+    dim3 grid(n_items, n_cb);
+    E.k<<<grid, kBlock, fq_smem(E.v), st>>>(positions, d_perm, d_tiles,
+                                            d_items, dq_hi, dq_lo, kb0,
+                                            n_chunks, n_groups, n_bins, d_part);
+    LAUNCH_CHECK(ctx);
+  }
+  dim3 g2((n_bins + 127) / 128, 1);
+  const int kb_out = (n_items > 0) ? std::min(k_begin, n_bins) : n_bins;
+  fq_finish_kernel<<<g2, 128, 0, st>>>(d_part, d_keys, d_ftab, d_spair, d_na,
+                                       n_spairs, n_bins, kb_out, fq, nullptr);
+  LAUNCH_CHECK(ctx);
+  // the host vectors are released on return: wait for the copies only
+  CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  return PYIID_OK;
+}
