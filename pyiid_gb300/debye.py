@@ -27,6 +27,9 @@ def _ptr(a, ctype):
 
 def as_positions(x, device=None):
     """float32 contiguous CUDA tensor [N, 3] from an array or tensor."""
+    if not torch.cuda.is_available():
+        raise NativeError('no CUDA device is visible; pyiid_gb300 runs only '
+                          'on a GB300 (sm_103a) GPU')
     if isinstance(x, torch.Tensor):
         t = x.detach()
         if not t.is_cuda:

@@ -1,0 +1,201 @@
+"""The drop-in layer on the GPU against the reference's own outputs.
+
+Mirrors pyiid/tests/test_scatter.py (processor pairs compared at rtol 5e-4,
+atol 5e-5, :9-10), test_scatter_state.py (cache invalidation on atom
+add/delete) and test_calc/*.py (Calc1D energies and forces), with the
+'GB300' processor on one side and the reference's recorded outputs
+(tests/golden) on the other.
+"""
+import numpy as np
+import pytest
+
+from pyiid_gb300.atoms import Atoms, Atom
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 5e-4, 5e-5   # pyiid/tests/test_scatter.py:9-10
+EXPS = {
+    'default': None,
+    'short': {'qmin': 0.6, 'qmax': 22.0, 'qbin': 0.13, 'rmin': 0.5,
+              'rmax': 12.0, 'rstep': 0.05, 'sampling': 'full'},
+    'ns': {'qmin': 1.1, 'qmax': 20.0, 'qbin': 0.1, 'rmin': 1.0,
+           'rmax': 15.0, 'rstep': 0.02, 'sampling': 'ns'},
+}
+
+
+def ES(exp_name):
+    from pyiid_gb300.experiments.elasticscatter import ElasticScatter
+    e = EXPS[exp_name]
+    return ElasticScatter(exp_dict=None if e is None else dict(e))
+
+
+def close(a, b, rtol=RTOL, atol=ATOL):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    assert a.shape == b.shape
+    np.testing.assert_allclose(np.nan_to_num(a), np.nan_to_num(b), rtol=rtol,
+                               atol=atol)
+
+
+def relerr(a, b):
+    a, b = np.nan_to_num(np.asarray(a, float)), np.nan_to_num(np.asarray(b, float))
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize('exp_name', ['default', 'short', 'ns'])
+@pytest.mark.parametrize('tag', ['au2', 'square', 'rand20', 'alloy16'])
+def test_scatter_getters_match_reference(golden, tag, exp_name):
+    key = f'{tag}__{exp_name}'
+    s = ES(exp_name)
+    assert s.processor == 'GB300'
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    fq = s.get_fq(atoms)
+    close(fq, golden[key + '__fq'])
+    assert relerr(fq, golden[key + '__fq']) < 5e-5
+    fq2 = s.get_fq(atoms)
+    assert fq is not fq2 and np.array_equal(fq, fq2)
+    close(s.get_sq(atoms), golden[key + '__sq'])
+    close(s.get_iq(atoms), golden[key + '__iq'], atol=5e-3)
+    pdf = s.get_pdf(atoms)
+    close(pdf, golden[key + '__pdf'])
+    assert relerr(pdf, golden[key + '__pdf']) < 5e-5
+    g = s.get_grad_fq(atoms)
+    assert g.dtype == np.float32
+    close(g, golden[key + '__grad_fq'])
+    assert relerr(g, golden[key + '__grad_fq']) < 1e-4
+    if key + '__grad_pdf' in golden.files:
+        gp = s.get_grad_pdf(atoms)
+        assert gp.dtype == np.float64
+        close(gp, golden[key + '__grad_pdf'])
+        assert relerr(gp, golden[key + '__grad_pdf']) < 1e-4
+    assert np.allclose(s.get_r(), golden[key + '__r'])
+    assert np.allclose(s.get_scatter_vector(), golden[key + '__q'])
+
+
+def test_scatter_tables_follow_reference_quirks(golden):
+    """Per-atom tables equal the reference's (PDF table evaluated at qbin,
+    alloy row labelling), so results match for alloys too."""
+    key = 'alloy16__short'
+    s = ES('short')
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    s.get_fq(atoms)
+    assert np.allclose(atoms.get_array('F(Q) scatter'),
+                       golden[key + '__fq_table'], rtol=1e-6)
+    assert np.allclose(atoms.get_array('PDF scatter'),
+                       golden[key + '__pdf_table'], rtol=1e-6)
+
+
+@pytest.mark.parametrize('change', ['add', 'delete'])
+def test_scatter_state_invalidation(change):
+    """pyiid/tests/test_scatter_state.py:11-71."""
+    rng = np.random.default_rng(7)
+    atoms = Atoms('Au30', rng.random((30, 3)) * 10)
+    s = ES('default')
+    assert s._check_wrap_atoms_state(atoms) is False
+    a1 = s.get_fq(atoms)
+    assert s._check_wrap_atoms_state(atoms) is True
+    assert np.any(a1)
+    if change == 'add':
+        atoms2 = atoms + Atom('Au', [0, 0, 0])
+    else:
+        atoms2 = atoms.copy()
+        del atoms2[3]
+    assert s._check_wrap_atoms_state(atoms2) is False
+    a2 = s.get_fq(atoms2)
+    assert s._check_wrap_atoms_state(atoms2) is True
+    assert np.any(a2) and not np.allclose(a1, a2) and a1 is not a2
+
+
+def _calc(golden, key, fused):
+    from pyiid_gb300.calc.calc_1d import Calc1D
+    exp_name = key.split('__')[-1]
+    s = ES(exp_name)
+    target = golden[key + '__target']
+    if fused:
+        f, g = s.get_pdf, s.get_grad_pdf
+    else:  # wrapped callables take the reference's generic path
+        f = lambda a: s.get_pdf(a)  # noqa: E731
+        g = lambda a: s.get_grad_pdf(a)  # noqa: E731
+    calc = Calc1D(target_data=target, exp_function=f, exp_grad_function=g,
+                  potential='rw')
+    assert (calc._fused is not None) == fused
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    atoms.set_calculator(calc)
+    return atoms
+
+
+@pytest.mark.parametrize('fused', [True, False])
+def test_calc1d_energy_forces_match_reference(golden, fused):
+    keys = sorted({k.rsplit('__', 1)[0] for k in golden.files
+                   if k.startswith('pot')})
+    for key in keys:
+        atoms = _calc(golden, key, fused)
+        e = atoms.get_potential_energy()
+        assert abs(e - golden[key + '__rw'][0]) <= 1e-5 * abs(
+            golden[key + '__rw'][0]) + 1e-9, key
+        f = atoms.get_forces()
+        want = golden[key + '__grad_rw']
+        assert relerr(f, want) < 1e-4, (key, relerr(f, want))
+
+
+def test_calc1d_chi_sq_and_true_forces(golden):
+    from pyiid_gb300.calc.calc_1d import Calc1D
+    key = 'pot__rand20_rand20p__short'
+    s = ES('short')
+    target = golden[key + '__target']
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    atoms.set_calculator(Calc1D(target_data=target, exp_function=s.get_pdf,
+                                exp_grad_function=s.get_grad_pdf,
+                                potential='chi_sq', conv=2.0))
+    assert abs(atoms.get_potential_energy() -
+               2.0 * golden[key + '__chi_sq'][0]) < 1e-5 * 2 * golden[
+                   key + '__chi_sq'][0]
+    assert relerr(atoms.get_forces(), 2.0 * golden[key + '__grad_chi_sq']) < 1e-4
+    calc = Calc1D(target_data=target, exp_function=s.get_pdf,
+                  exp_grad_function=s.get_grad_pdf, true_forces=True)
+    atoms.set_calculator(calc)
+    # physical forces are -dE/dx = 2x the reference's (which carry 1/2)
+    assert relerr(atoms.get_forces(), 2 * golden[key + '__grad_rw']) < 1e-4
+
+
+def test_calc1d_forces_vs_numerical(golden):
+    """Central differences of the energy (h = 1e-3 A) against the true forces."""
+    from pyiid_gb300.calc.calc_1d import Calc1D
+    key = 'pot__rand20_rand20p__short'
+    s = ES('short')
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'].astype(np.float64))
+    calc = Calc1D(target_data=golden[key + '__target'],
+                  exp_function=s.get_pdf, exp_grad_function=s.get_grad_pdf,
+                  true_forces=True)
+    atoms.set_calculator(calc)
+    f = atoms.get_forces()
+    fd = calc.calculate_numerical_forces(atoms, d=1e-3)
+    # float32 positions limit the finite-difference accuracy
+    assert relerr(f, fd) < 5e-3, relerr(f, fd)
+
+
+def test_pdfcalc_fqcalc_names():
+    from pyiid_gb300.calc.pdfcalc import PDFCalc
+    from pyiid_gb300.calc.fqcalc import FQCalc
+    rng = np.random.default_rng(3)
+    a1 = Atoms('Au12', rng.random((12, 3)) * 8)
+    a2 = Atoms('Au12', a1.positions + rng.normal(0, .05, (12, 3)))
+    s = ES('short')
+    for C, fn in ((PDFCalc, s.get_pdf), (FQCalc, s.get_fq)):
+        calc = C(obs_data=fn(a1), scatter=s, conv=1., potential='rw')
+        a2.set_calculator(calc)
+        e = a2.get_potential_energy()
+        f = a2.get_forces()
+        assert 0 < e < 1 and f.shape == (12, 3) and np.all(np.isfinite(f))
+
+
+def test_set_processor_contract():
+    s = ES('default')
+    assert s.set_processor('GB300') is True
+    assert s.set_processor('CPU') is None       # not provided: no CPU fallback
+    assert s.set_processor('Multi-GPU') is None
+    assert s.processor == 'GB300' and s.alg == 'flat'
