@@ -269,7 +269,10 @@ def run_gpu(args, rank, world, local):
                 'h2d_bytes_per_step': int(h_pos.numel() * 4),
                 'd2h_bytes_per_step': int(h_fq.numel() * 4 + h_grad.numel() * 4)},
         'roofline': {
-            'bound': 'fp32', 'kernel': 'gradfq_kernel',
+            'bound': 'fp32',
+            'kernel': ('gradfq2_kernel' if (tuned is None or
+                                            tuned['grad_fq']['pairs_per_thread']
+                                            == 0) else 'gradfq_kernel'),
             'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
             'frac': achieved / peak if peak else None,
             'peak_source': 'measured live: cuBLAS SGEMM 8192^3 (TF32 off)',
@@ -283,7 +286,7 @@ def run_gpu(args, rank, world, local):
 
 def traffic_from_profile():
     """DRAM bytes per gradfq launch from the committed ncu summary, if any."""
-    p = os.path.join(REPO, 'profiles', 'gradfq_kernel_pt20000.md')
+    p = os.path.join(REPO, 'profiles', 'gradfq2_kernel_pt20000.md')
     if not os.path.exists(p):
         return None
     for line in open(p):
