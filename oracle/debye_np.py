@@ -100,13 +100,21 @@ def _pairs(n):
     return i, j
 
 
-def pair_sums(pos, scatter, qbin, chunk=20000):
+def _pos64(pos, cast32):
+    """Positions as FP64; rounded through float32 first (as the reference
+    casts them) unless cast32 is False (finite-difference checks)."""
+    if cast32:
+        return np.asarray(pos, dtype=np.float32).astype(np.float64)
+    return np.asarray(pos, dtype=np.float64)
+
+
+def pair_sums(pos, scatter, qbin, chunk=20000, cast32=True):
     """S_k = sum_{i>j} f_i f_j sin(Q_k r_ij) / r_ij in FP64.
 
     kernels/cpu_flat.py:16-114 (d, r, norm, omega, fq) summed over pairs as
     cpu_wrappers/flat_serial_cpu_wrap.py:61.  Q_k = k * qbin.
     """
-    q = np.asarray(pos, dtype=np.float32).astype(np.float64)
+    q = _pos64(pos, cast32)
     f = np.asarray(scatter, dtype=np.float64)
     n, kmax = f.shape
     Q = np.arange(kmax) * float(qbin)
@@ -133,24 +141,25 @@ def normalization(scatter):
     return n * pairsum / (n * (n - 1) / 2)
 
 
-def fq(pos, scatter, qbin):
+def fq(pos, scatter, qbin, cast32=True):
     """F(Q) from Q = 0 (the plug-in's return value before slicing).
 
     2 * nan_to_num(S / na): cpu_wrappers/flat_multi_cpu_wrap.py:44-60.
     """
-    s = pair_sums(pos, scatter, qbin)
+    s = pair_sums(pos, scatter, qbin, cast32=cast32)
     with np.errstate(all='ignore'):
         return 2 * np.nan_to_num(s / normalization(scatter))
 
 
-def grad_fq(pos, scatter, qbin, convention='reference', chunk=20000):
+def grad_fq(pos, scatter, qbin, convention='reference', chunk=20000,
+            cast32=True):
     """Gradient of F(Q), [N, 3, K].
 
     'reference': -(1/na) dS/dx (= -1/2 dF/dx), the value of wrap_fq_grad
     (kernels/cpu_flat.py:122-194, kernels/cpu_experimental.py:8-15,
     cpu_wrappers/flat_serial_cpu_wrap.py:124-133).  'true': dF/dx.
     """
-    q = np.asarray(pos, dtype=np.float32).astype(np.float64)
+    q = _pos64(pos, cast32)
     f = np.asarray(scatter, dtype=np.float64)
     n, kmax = f.shape
     Q = np.arange(kmax) * float(qbin)
@@ -335,6 +344,16 @@ def potential_adjoint_vector(gobs, gcalc, potential='rw'):
         pre = -2.0
     dscale = (gobs - 2 * a * gcalc) / np.dot(gcalc, gcalc)
     return pre * (s * e + ga_on * np.dot(gcalc, e) * dscale)
+
+
+def potential_value(pos, pdf_table, exp, gobs, potential='rw', cast32=True):
+    """Rw or chi^2 of one configuration on the PDF grid (FP64)."""
+    qb = pdf_qbin(exp)
+    gcalc = pdf_tmatrix(fq(pos, pdf_table, qb, cast32=cast32), exp['rstep'],
+                        qb, r_grid(exp), exp['qmin'])
+    if potential == 'rw':
+        return get_rw(gobs, gcalc)[0]
+    return get_chi_sq(gobs, gcalc)[0]
 
 
 def true_grad_potential(pos, pdf_table, exp, gobs, potential='rw'):
