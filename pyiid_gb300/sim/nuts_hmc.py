@@ -94,10 +94,12 @@ class NUTSCanonicalEnsemble(Ensemble):
             atoms.set_momenta(self.random_state.normal(0, 1, (len(atoms), 3)))
         atoms_prime = leapfrog(atoms, step_size)
         with np.errstate(over='ignore'):
-            a = 2 * (np.exp(-1 * atoms_prime.get_total_energy() +
-                            atoms.get_total_energy()) > 0.5) - 1
+            # a = +1 (grow) or -1 (shrink), kept a Python float so that the
+            # threshold 2^-a is well defined for both signs
+            a = 1.0 if np.exp(-1 * atoms_prime.get_total_energy() +
+                              atoms.get_total_energy()) > 0.5 else -1.0
             while (np.exp(-1 * atoms_prime.get_total_energy() +
-                          atoms.get_total_energy())) ** a > 2 ** -a:
+                          atoms.get_total_energy())) ** a > 2.0 ** -a:
                 step_size *= 2 ** a
                 if self.verbose:
                     print('trying step size', step_size)
