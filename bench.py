@@ -244,6 +244,14 @@ def run_gpu(args, rank, world, local):
     # correctness guard on what was timed: finite, nonzero
     assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
 
+    workloads = {}
+    if rank == 0 and not args.no_workloads:
+        for name, fn in (('batched_fq_256_alloys', run_batched),
+                         ('hmc_64_chains_au1000', run_hmc)):
+            try:
+                workloads[name] = fn(torch)
+            except Exception as e:  # noqa: BLE001 -- reported, not fatal
+                workloads[name] = {'error': f'{type(e).__name__}: {e}'}
     peak = fp32_peak_tflops(torch, dev) if rank == 0 else None
     if pg:
         pg.barrier()
@@ -281,6 +289,8 @@ def run_gpu(args, rank, world, local):
         },
         'clocks': clk.summary(),
     }
+    if workloads:
+        line['workloads'] = workloads
     return line
 
 
@@ -296,6 +306,104 @@ def traffic_from_profile():
             except ValueError:
                 return None
     return None
+
+
+# ----------------------------------------------------- secondary workloads
+def batched_workload():
+    """256 fcc Au/Pt random alloys, N ~ U{55..2000} (seed 3), a = 4.0 A,
+    sigma = 0.05 A, Q 0.1-25 1/A step 0.05."""
+    from pyiid_gb300 import structures
+    from pyiid_gb300.scatter_factors import species_tables
+    sizes = np.random.default_rng(3).integers(55, 2001, 256)
+    sites = structures.fcc_nearest(4.0, int(sizes.max()))
+    pos, nums = [], []
+    for b, n in enumerate(sizes):
+        r = np.random.default_rng(3 + b)
+        nums.append(np.where(r.random(n) < 0.5, 78, 79))
+        pos.append((sites[:n] + r.normal(0, 0.05, (n, 3))).astype(np.float32))
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    sp, tab, _ = species_tables(np.concatenate(nums), 0.05, 500)
+    return np.concatenate(pos), sp, offsets, tab, sizes
+
+
+def run_batched(torch, steps=5):
+    """Configuration 3: F(Q) of all 256 configurations per step, one graph
+    replay (one pair-sum launch + one finishing launch)."""
+    from pyiid_gb300 import debye
+    pos, sp, off, tab, sizes = batched_workload()
+    p = torch.as_tensor(pos, device='cuda')
+    out = torch.empty((len(sizes), 500), dtype=torch.float32, device='cuda')
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out)
+    g.replay()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(steps):
+        g.replay()
+    ev1.record()
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    pairs = int(np.sum(sizes.astype(np.int64) * (sizes - 1) // 2))
+    assert torch.isfinite(out).all()
+    return {'workload': '256 fcc Au/Pt alloys, N~U{55..2000}, Q 0.1-25 step 0.05',
+            'atoms': int(sizes.sum()), 'pairs': pairs,
+            'ms_per_batch': ms, 'configs_per_s': len(sizes) / (ms * 1e-3),
+            'pair_bin_terms_per_s': pairs * 498 / (ms * 1e-3),
+            'launch': 'CUDA graph replay: 1 pair-sum + 1 finishing kernel'}
+
+
+def run_hmc(torch, iters=6):
+    """Configuration 4: 1,000-atom fcc Au, 64 chains, 10 leapfrog steps,
+    dt = 1e-3, T = 300 K, E = 100 * Rw against the undisplaced G(r); one
+    CUDA-graph replay per HMC iteration of all chains."""
+    from pyiid_gb300 import structures
+    from pyiid_gb300.sampling import PDFPotential, BatchedHMC, experiment_grids
+    from pyiid_gb300.scatter_factors import species_tables
+    from pyiid_gb300 import debye
+    exp, qb, nb, rg = experiment_grids(None)
+    ref = structures.fcc_nearest(4.08, 1000).astype(np.float32)
+    sp, tab, _ = species_tables([79] * 1000, qb, nb)
+    f = debye.fq(ref, sp, tab, qb)
+    gobs = debye.pdf(f, qb, exp['rstep'], rg, exp['qmin']).cpu().numpy()
+    pot = PDFPotential([79] * 1000, gobs, None, conv=100.0, n_configs=64)
+    xs = np.stack([structures.displaced(ref, 0.05, 4 + c) for c in range(64)])
+    hmc = BatchedHMC(pot, xs, temperature=300.0, dt=1e-3, n_steps=10, seed=4,
+                     graph=True)
+    hmc.step(2)
+    torch.cuda.synchronize()
+    hmc.accepted.zero_()
+    hmc.proposed = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    hmc.step(iters)
+    ev1.record()
+    ev1.synchronize()
+    s = ev0.elapsed_time(ev1) * 1e-3
+    acc = int(hmc.accepted.sum().item())
+    # one force evaluation of all 64 chains, for reference
+    x = hmc.positions()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pot.evaluate(x)
+    e0.record()
+    for _ in range(3):
+        pot.evaluate(x)
+    e1.record()
+    e1.synchronize()
+    return {'workload': '1000-atom fcc Au, 64 chains, 10 leapfrog x dt 1e-3, 300 K, E = 100 Rw',
+            'hmc_iterations_per_s': iters / s,
+            'accepted_steps_per_s': acc / s,
+            'acceptance': acc / (iters * 64),
+            'ms_per_iteration': 1e3 * s / iters,
+            'ms_per_force_eval_64_chains': e0.elapsed_time(e1) / 3,
+            'launch': 'CUDA graph replay per HMC iteration (11 batched exact evaluations)'}
 
 
 # ------------------------------------------------------------- CPU arm
@@ -375,6 +483,8 @@ def main():
                          'smaller sizes are for profiling)')
     ap.add_argument('--no-cpu', action='store_true',
                     help='skip the CPU baseline sample')
+    ap.add_argument('--no-workloads', action='store_true',
+                    help='skip the batched and HMC secondary workloads')
     ap.add_argument('--no-tune', action='store_true',
                     help='use the default launch shapes (no autotuning)')
     args = ap.parse_args()

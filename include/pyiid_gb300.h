@@ -94,6 +94,21 @@ int pyiid_fq(pyiid_ctx *ctx, const float *positions, const int32_t *species,
              int n_atoms, const float *scatter, int n_species, int n_bins,
              double qbin, int k_begin, float *fq);
 
+/* F(Q) of many configurations in one pass (one pair-sum launch over the
+ * work items of every configuration, then one finishing launch).
+ * Configuration b owns atoms offsets[b] .. offsets[b+1]-1 of the packed
+ * positions/species; all share one Q grid and one species table.
+ *   positions : device float [total_atoms][3]
+ *   species   : host int32   [total_atoms]
+ *   offsets   : host int32   [n_configs + 1]
+ *   fq        : device float [n_configs][n_bins]
+ * Replaces a Python loop of wrap_fq calls (flat_multi_cpu_wrap.py:22-60), one
+ * per configuration. */
+int pyiid_batch_fq(pyiid_ctx *ctx, const float *positions,
+                   const int32_t *species, const int32_t *offsets,
+                   int n_configs, const float *scatter, int n_species,
+                   int n_bins, double qbin, int k_begin, float *fq);
+
 /* Gradient of F(Q) in the reference's convention:
  *   grad[a][c][k] = -(1/na_k) * d S_k / d x_{a,c}  ( = -1/2 * dF_k/dx_{a,c} ),
  * k in [k_begin, n_bins), NaN -> 0 per element as the reference does.

@@ -36,6 +36,8 @@ _SIGNATURES = {
                           _c_dbl, _c_int, _vp]),
     'pyiid_grad_fq': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
                                _c_int, _c_dbl, _c_int, _vp]),
+    'pyiid_batch_fq': (_c_int, [_vp, _vp, _i32p, _i32p, _c_int, _f32p,
+                                _c_int, _c_int, _c_dbl, _c_int, _vp]),
     'pyiid_pdf': (_c_int, [_vp, _vp, _c_int, _c_int, _c_dbl, _c_dbl, _f64p,
                            _c_int, _c_dbl, _vp]),
     'pyiid_grad_pdf': (_c_int, [_vp, _vp, _c_int, _c_int, _c_dbl, _c_dbl,

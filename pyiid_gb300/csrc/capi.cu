@@ -627,6 +627,16 @@ int pyiid_fq(pyiid_ctx *ctx, const float *positions, const int32_t *species,
                   n_bins, qbin, k_begin, fq);
 }
 
+int pyiid_batch_fq(pyiid_ctx *ctx, const float *positions,
+                   const int32_t *species, const int32_t *offsets,
+                   int n_configs, const float *scatter, int n_species,
+                   int n_bins, double qbin, int k_begin, float *fq) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (!offsets) return fail(ctx, PYIID_ERR_INVALID_ARG, "null offsets");
+  return batch_fq(ctx, positions, species, offsets, n_configs, scatter,
+                  n_species, n_bins, qbin, k_begin, fq);
+}
+
 int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
                   const int32_t *species, int n_atoms, const float *scatter,
                   int n_species, int n_bins, double qbin, int k_begin,

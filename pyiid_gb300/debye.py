@@ -10,7 +10,7 @@ import torch
 
 from ._native import context, POTENTIALS, NativeError
 
-__all__ = ['fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
+__all__ = ['fq', 'batch_fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
            'batch_potential_grad', 'as_positions']
 
 _f32p = None
@@ -63,6 +63,28 @@ def fq(positions, species, scatter, qbin, k_begin=0, out=None):
              _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
              tab.shape[0], tab.shape[1], float(qbin), int(k_begin),
              ctypes.c_void_p(out.data_ptr()))
+    return out
+
+
+def batch_fq(positions, species, offsets, scatter, qbin, k_begin=0,
+             out=None):
+    """F(Q) rows [B, K] of packed configurations (offsets [B+1])."""
+    import ctypes
+    pos = as_positions(positions)
+    sp = _np(species, np.int32)
+    off = _np(offsets, np.int32)
+    tab = _np(scatter, np.float32)
+    b = len(off) - 1
+    if out is None:
+        out = torch.empty((b, tab.shape[1]), dtype=torch.float32,
+                          device=pos.device)
+    else:
+        _check_dev(out, 'out', torch.float32)
+    ctx = context(pos.device.index)
+    ctx.call('pyiid_batch_fq', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
+             _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
+             float(qbin), int(k_begin), ctypes.c_void_p(out.data_ptr()))
     return out
 
 

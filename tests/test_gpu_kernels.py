@@ -272,3 +272,27 @@ def test_autotune_selects_and_caches(D, tmp_path, monkeypatch):
     assert got == {'fq': res['fq']['best'], 'grad_fq': res['grad_fq']['best']}
     ctx.set_variant('fq', 0)
     ctx.set_variant('grad_fq', 0)
+
+
+def test_batch_fq_uneven_alloys_matches_oracle(D):
+    rng = np.random.default_rng(17)
+    sizes = [1, 55, 2, 130, 0, 77]
+    pos, nums, off = [], [], [0]
+    for i, n in enumerate(sizes):
+        pos.append(S.random_cube(n, 12.0, 50 + i))
+        nums.append(rng.choice([78, 79], n))
+        off.append(off[-1] + n)
+    pos = np.concatenate(pos)
+    allnum = np.concatenate(nums)
+    sp, tab, _ = species_tables(allnum, 0.05, 500)
+    got = D.batch_fq(pos, sp, np.array(off), tab, 0.05, 2).cpu().numpy()
+    for i in range(len(sizes)):
+        a, b = off[i], off[i + 1]
+        want = O.fq(pos[a:b], tab[sp[a:b]], 0.05) if b - a else np.zeros(500)
+        assert np.all(got[i, :2] == 0)
+        if b - a < 2:
+            assert np.all(got[i] == 0)
+        else:
+            assert rel(got[i, 2:], want[2:]) <= TOL_F
+        single = D.fq(pos[a:b], sp[a:b], tab, 0.05, 2).cpu().numpy()
+        assert np.array_equal(single, got[i])
