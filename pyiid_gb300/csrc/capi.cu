@@ -32,7 +32,7 @@ namespace {
 
 constexpr int kVersion = 10000;  // 1.0.0
 constexpr int kJMax = 32;        // max J tiles per F(Q) work item
-constexpr int kAdjRS = 64;       // adjoint re-seed period (bins)
+constexpr int kAdjRS = 128;      // adjoint re-seed period (bins)
 
 // ---------------------------------------------------------------- variants
 // Launch shapes of the two pair kernels; pyiid_tune selects one per context.
@@ -817,8 +817,10 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
       T->d_T, cvec, n_bins, n_r, kmin, n_configs, w);
   LAUNCH_CHECK(ctx);
   const int kb0 = kmin & ~1;
-  const int kp = std::max(kAdjRS, ((n_bins - kb0 + kAdjRS - 1) / kAdjRS) * kAdjRS);
-  const size_t ntab = (size_t)n_configs * n_species * n_species * kp;
+  // table length: bins [kb0, n_bins) rounded up to a multiple of 4 (two
+  // packed steps); the kernel runs full re-seed blocks, then the remainder
+  const int kp = std::max(4, ((n_bins - kb0 + 3) / 4) * 4);
+  const size_t ntab = (size_t)n_configs * n_species * n_species * (kp / 2);
   TRY(ensure(ctx, "b_tabs", ntab * sizeof(float4), &p));
   float4 *tabs = static_cast<float4 *>(p);
   adjoint_table_kernel<<<256, 256, 0, ctx->stream>>>(
@@ -826,7 +828,7 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
   LAUNCH_CHECK(ctx);
   float dq_hi, dq_lo;
   split_double(qstep, dq_hi, dq_lo);
-  const size_t smem = (size_t)n_species * kp * sizeof(float4);
+  const size_t smem = (size_t)n_species * (kp / 2) * sizeof(float4);
   if (smem > 160 * 1024)
     return fail(ctx, PYIID_ERR_INVALID_ARG,
                 "adjoint tables (%zu bytes) exceed shared memory", smem);

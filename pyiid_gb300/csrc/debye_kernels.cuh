@@ -678,16 +678,17 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
 // with W_k = 2 w_k f_sa f_sb / na_k and w = T c the back-projected G(r)
 // adjoint.  Owner-computes: CTA = tile I, thread (atom a = lane, group =
 // warp); group gp handles b = gp, gp + 8, ... of every tile J, so the lanes of
-// a warp share b and the weight tables are broadcast reads.
-// Packed even/odd recurrence (pair_math.cuh); per re-seed block of RS bins
-// starting at kb0 + blk (RS a multiple of 4).  Tables hold, for sigma2 = +1
-// and -1 and every bin pair (kk, kk+1), kk = k - kb0 even:
-//   (A_kk, A_kk+1, B_kk, B_kk+1),  A_k = k W_k s_k, B_k = W_k s_k,
-//   s_k = sigma2^(kk/2)
-// so that, with t, w scaled by beta = -1/r^3 and gamma' = -r dq/(2 ch),
-//   s_ab = gamma' sum_k A_k (w_m + w_{m+1}) + sum_k B_k t_m.
-// Per two bins and ordered pair: FFMA2 + FADD2 + 2 FFMA2 + FFMA2 = 5 packed
-// instructions and one LDS.128.
+// a warp share b and every table read is a broadcast of one address.
+// Packed even/odd recurrence (pair_math.cuh), re-seeded every RS bins from
+// kb0 (RS a multiple of 4); the last block runs only up to the last bin.
+// Tables hold, for every bin pair (kk, kk+1), kk = k - kb0 even,
+//   (A_kk, A_kk+1, B_kk, B_kk+1),  A_k = k W_k, B_k = W_k,
+// and the sign sigma2^m of step m is applied by accumulating even and odd
+// steps separately, so with t, w scaled by beta = -1/r^3 and
+// gamma' = -r dq/(2 ch):
+//   s_ab = gamma' (Ae + sigma2 Ao) + (Be + sigma2 Bo),
+//   Ae = sum_{m even} A (w_m + w_{m+1}),  Be = sum_{m even} B t_m, ...
+// Per two bins and ordered pair: 5 packed FP32x2 instructions + 1 LDS.128.
 template <int RS>
 __global__ void __launch_bounds__(kBlock)
     adjoint_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
@@ -697,7 +698,7 @@ __global__ void __launch_bounds__(kBlock)
                    const float4 *__restrict__ tabs, int n_species,
                    float *__restrict__ grad) {
   static_assert(RS % 4 == 0, "RS must be a multiple of 4");
-  extern __shared__ float4 stab[];  // [n_species][2][kp/2]
+  extern __shared__ float4 stab[];  // [n_species][kp/2]
   __shared__ float4 sI[kTile], sJ[kTile];
   __shared__ float sred[kBlock / kTile][kTile][3];
 
@@ -707,11 +708,10 @@ __global__ void __launch_bounds__(kBlock)
   const int lane = tid % kTile;
   const int grp = tid / kTile;
   const int ngrp = blockDim.x / kTile;
-  const int kh = kp / 2;
+  const int kh = kp / 2;  // packed steps (bin pairs) in the table
 
-  const float4 *src =
-      tabs + ((size_t)ti.z * n_species + ti.w) * n_species * 2 * kh;
-  for (int i = tid; i < n_species * 2 * kh; i += blockDim.x) stab[i] = src[i];
+  const float4 *src = tabs + ((size_t)ti.z * n_species + ti.w) * n_species * kh;
+  for (int i = tid; i < n_species * kh; i += blockDim.x) stab[i] = src[i];
   if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
 
   float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(kBlock)
     if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
     __syncthreads();
     const bool same = (tj == (int)blockIdx.x);
-    const float4 *tb = stab + (size_t)tJ.w * 2 * kh;
+    const float4 *tab = stab + (size_t)tJ.w * kh;
     if (lane < ti.y) {
       const float4 pa = sI[lane];
       for (int b = grp; b < tJ.y; b += ngrp) {
@@ -734,24 +734,51 @@ __global__ void __launch_bounds__(kBlock)
         const float2 c1 = f2(beta * p.ch), c2 = f2(beta * p.sh);
         const float gam = -p.r * dq_hi / (2.0f * p.ch);
         const float2 kpos = f2(p.kappa), kneg = f2(-p.kappa);
-        const float4 *tab = tb + (p.sigma2 > 0.f ? 0 : kh);
-        float2 a1 = f2(0.f), a2 = f2(0.f);
-        for (int blk = 0; blk < kp; blk += RS) {
+        float2 ae = f2(0.f), ao = f2(0.f), be = f2(0.f), bo = f2(0.f);
+        for (int blk = 0; blk < kh; blk += RS / 2) {
           float2 s, co;
-          seed_sincos2((float)(kb0 + blk), p.th_hi, p.th_lo, s, co);
+          seed_sincos2((float)(kb0 + 2 * blk), p.th_hi, p.th_lo, s, co);
           float2 t = __fmul2_rn(f2(beta), s);
           float2 w = __ffma2_rn(co, c1, __fmul2_rn(s, c2));
+          const float4 *tb = tab + blk;
+          if (blk + RS / 2 <= kh) {
 #pragma unroll
-          for (int m = 0; m < RS / 2; ++m) {
-            const float4 wt = tab[(blk >> 1) + m];
-            const float2 wn = __ffma2_rn(kneg, t, w);
-            a1 = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), a1);
-            a2 = __ffma2_rn(make_float2(wt.z, wt.w), t, a2);
-            t = __ffma2_rn(kpos, wn, t);
-            w = wn;
+            for (int m = 0; m < RS / 2; m += 2) {
+              float4 wt = tb[m];
+              float2 wn = __ffma2_rn(kneg, t, w);
+              ae = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ae);
+              be = __ffma2_rn(make_float2(wt.z, wt.w), t, be);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+              wt = tb[m + 1];
+              wn = __ffma2_rn(kneg, t, w);
+              ao = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ao);
+              bo = __ffma2_rn(make_float2(wt.z, wt.w), t, bo);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+            }
+          } else {
+            const int nm = kh - blk;  // even: kp is a multiple of 4
+            for (int m = 0; m < nm; m += 2) {
+              float4 wt = tb[m];
+              float2 wn = __ffma2_rn(kneg, t, w);
+              ae = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ae);
+              be = __ffma2_rn(make_float2(wt.z, wt.w), t, be);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+              wt = tb[m + 1];
+              wn = __ffma2_rn(kneg, t, w);
+              ao = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ao);
+              bo = __ffma2_rn(make_float2(wt.z, wt.w), t, bo);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+            }
           }
         }
-        const float sab = fmaf(gam, a1.x + a1.y, a2.x + a2.y);
+        const float sg = p.sigma2;
+        const float A = (ae.x + ae.y) + sg * (ao.x + ao.y);
+        const float B = (be.x + be.y) + sg * (bo.x + bo.y);
+        const float sab = fmaf(gam, A, B);
         gx = fmaf(sab, dx, gx);
         gy = fmaf(sab, dy, gy);
         gz = fmaf(sab, dz, gz);

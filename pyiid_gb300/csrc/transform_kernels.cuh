@@ -140,9 +140,9 @@ __global__ void wvec_kernel(const float *__restrict__ T,
   if (lane == 0) w[(size_t)b * n_bins + k] = acc;
 }
 
-// Adjoint tables: tabs[b][sa][sb][sigma2][m] = (A_kk, A_kk+1, B_kk, B_kk+1),
+// Adjoint tables: tabs[b][sa][sb][m] = (A_kk, A_kk+1, B_kk, B_kk+1),
 //   kk = 2m, k = kb0 + kk, W = 2 w_k f_sa f_sb / na_k (0 outside
-//   [kmin, n_bins) or where na_k = 0), s_k = sigma2^m, A = k W s_k, B = W s_k.
+//   [kmin, n_bins) or where na_k = 0), A = k W, B = W.
 __global__ void adjoint_table_kernel(const double *__restrict__ w,
                                      const double *__restrict__ na,
                                      const float *__restrict__ ftab,
@@ -172,11 +172,8 @@ __global__ void adjoint_table_kernel(const double *__restrict__ w,
       A[e] = (float)((double)k * W);
       B[e] = (float)W;
     }
-    float4 *base =
-        tabs + ((((size_t)b * n_species + sa) * n_species + sb) * 2) * kh;
-    base[m] = make_float4(A[0], A[1], B[0], B[1]);
-    const float sg = (m & 1) ? -1.f : 1.f;
-    base[kh + m] = make_float4(sg * A[0], sg * A[1], sg * B[0], sg * B[1]);
+    tabs[(((size_t)b * n_species + sa) * n_species + sb) * kh + m] =
+        make_float4(A[0], A[1], B[0], B[1]);
   }
 }
 
