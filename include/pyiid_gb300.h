@@ -235,11 +235,13 @@ int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
  * kernel; pyiid_gb300's autotuner times them on the caller's sizes and sets
  * the fastest.  No reference counterpart (the reference's numba launches are
  * fixed, atomics/gpu_atomics.py:120-184).
- *   kernel: PYIID_KERNEL_FQ (pyiid_fq and the F(Q) part of the batched call)
- *           or PYIID_KERNEL_GRAD_FQ (pyiid_grad_fq).
+ *   kernel: PYIID_KERNEL_FQ (pyiid_fq and the F(Q) part of the batched call),
+ *           PYIID_KERNEL_GRAD_FQ (pyiid_grad_fq) or PYIID_KERNEL_ADJOINT
+ *           (the gradient of pyiid_batch_potential_grad: variant 0 evaluates
+ *           each unordered pair once, variant 1 twice).
  *   params (pyiid_variant_info): {bins per thread, pairs per thread, threads
  *   per CTA}. */
-enum { PYIID_KERNEL_FQ = 0, PYIID_KERNEL_GRAD_FQ = 1 };
+enum { PYIID_KERNEL_FQ = 0, PYIID_KERNEL_GRAD_FQ = 1, PYIID_KERNEL_ADJOINT = 2 };
 int pyiid_variant_count(int kernel);
 int pyiid_variant_info(int kernel, int variant, int *params, int n_params);
 int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant);

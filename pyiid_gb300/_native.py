@@ -56,7 +56,7 @@ _SIGNATURES = {
     'pyiid_get_variant': (_c_int, [_vp, _c_int]),
 }
 
-KERNELS = {'fq': 0, 'grad_fq': 1}
+KERNELS = {'fq': 0, 'grad_fq': 1, 'adjoint': 2}
 
 
 class NativeError(RuntimeError):

@@ -31,7 +31,7 @@ using namespace pyiid;
 namespace {
 
 constexpr int kVersion = 10000;  // 1.0.0
-constexpr int kJMax = 32;        // max J tiles per F(Q) work item
+constexpr int kJMax = kJMaxTiles;  // max J tiles per F(Q) work item
 constexpr int kAdjRS = 128;      // adjoint re-seed period (bins)
 
 // ---------------------------------------------------------------- variants
@@ -123,6 +123,15 @@ struct Layout {
   std::vector<int2> spair_species;
   std::vector<double> pair_counts;  // [n_configs][n_spairs]
   std::vector<int> natoms;          // per configuration
+  // symmetric adjoint: per item the float offsets of its i-side [32][3] and
+  // j-side [(J1-J0)*32][3] partial rows; per tile the CSR list of the
+  // [32][3] blocks that sum to its gradient rows
+  std::vector<int> adj_ioff, adj_joff, adj_tile_ptr, adj_entries;
+  size_t adj_total = 0;
+  int *d_adj_ioff = nullptr;
+  int *d_adj_joff = nullptr;
+  int *d_adj_tile_ptr = nullptr;
+  int *d_adj_entries = nullptr;
   // device copies
   int *d_perm = nullptr;
   int4 *d_tiles = nullptr;
@@ -162,6 +171,7 @@ struct pyiid_ctx {
   bool attrs_set = false;
   int fq_variant = 0;
   int grad_variant = 0;
+  int adj_variant = 0;  // 0: symmetric (each pair once), 1: owner-computes
 };
 
 namespace {
@@ -241,6 +251,10 @@ void free_layout(Layout *L) {
   cudaFree(L->d_items);
   cudaFree(L->d_key_item_begin);
   cudaFree(L->d_spair);
+  cudaFree(L->d_adj_ioff);
+  cudaFree(L->d_adj_joff);
+  cudaFree(L->d_adj_tile_ptr);
+  cudaFree(L->d_adj_entries);
 }
 
 // Builds (or finds) the layout of a packed batch.
@@ -317,6 +331,36 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
   L->key_item_begin.assign(nkeys + 1, 0);
   for (const int4 &it : L->items) L->key_item_begin[it.w + 1]++;
   for (int k = 0; k < nkeys; ++k) L->key_item_begin[k + 1] += L->key_item_begin[k];
+  {
+    const int ni = (int)L->items.size(), nt = (int)L->tiles.size();
+    L->adj_ioff.resize(ni);
+    L->adj_joff.resize(ni);
+    std::vector<std::vector<int>> per_tile(nt);
+    size_t off = 0;
+    for (int i = 0; i < ni; ++i) {
+      const int4 it = L->items[i];
+      L->adj_ioff[i] = (int)off;
+      per_tile[it.x].push_back((int)off);
+      off += kTile * 3;
+      L->adj_joff[i] = (int)off;
+      for (int T = it.y; T < it.z; ++T)
+        per_tile[T].push_back((int)(off + (size_t)(T - it.y) * kTile * 3));
+      off += (size_t)(it.z - it.y) * kTile * 3;
+    }
+    if (off > (size_t)INT32_MAX)
+      return fail(ctx, PYIID_ERR_INVALID_ARG, "batch too large for the adjoint");
+    L->adj_total = off;
+    L->adj_tile_ptr.assign(nt + 1, 0);
+    for (int t = 0; t < nt; ++t) {
+      L->adj_tile_ptr[t + 1] = L->adj_tile_ptr[t] + (int)per_tile[t].size();
+      L->adj_entries.insert(L->adj_entries.end(), per_tile[t].begin(),
+                            per_tile[t].end());
+    }
+  }
+  TRY(upload(ctx, &L->d_adj_ioff, L->adj_ioff));
+  TRY(upload(ctx, &L->d_adj_joff, L->adj_joff));
+  TRY(upload(ctx, &L->d_adj_tile_ptr, L->adj_tile_ptr));
+  TRY(upload(ctx, &L->d_adj_entries, L->adj_entries));
   TRY(upload(ctx, &L->d_perm, L->perm));
   TRY(upload(ctx, &L->d_tiles, L->tiles));
   TRY(upload(ctx, &L->d_cfg_tiles, L->cfg_tiles));
@@ -468,6 +512,9 @@ int set_attrs(pyiid_ctx *ctx) {
                       kFqTable[i].k,
                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                       (int)fq_smem(kFqTable[i].v)));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(adjoint_sym_kernel<kAdjRS>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     160 * 1024));
   CUDA_TRY(ctx, cudaFuncSetAttribute(adjoint_kernel<kAdjRS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      160 * 1024));
@@ -832,11 +879,26 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
   if (smem > 160 * 1024)
     return fail(ctx, PYIID_ERR_INVALID_ARG,
                 "adjoint tables (%zu bytes) exceed shared memory", smem);
-  if (!L->tiles.empty()) {
+  if (!L->tiles.empty() && ctx->adj_variant == 1) {
     adjoint_kernel<kAdjRS><<<(unsigned)L->tiles.size(), kBlock, smem,
                              ctx->stream>>>(positions, L->d_perm, L->d_tiles,
                                             L->d_cfg_tiles, dq_hi, dq_lo, kb0,
                                             kp, tabs, n_species, grad);
+    LAUNCH_CHECK(ctx);
+  } else if (!L->tiles.empty()) {
+    TRY(ensure(ctx, "b_adjpart", std::max<size_t>(L->adj_total, 1) * sizeof(float),
+               &p));
+    float *part = static_cast<float *>(p);
+    if (!L->items.empty()) {
+      adjoint_sym_kernel<kAdjRS><<<(unsigned)L->items.size(), kBlock,
+                                   (kp / 2) * sizeof(float4), ctx->stream>>>(
+          positions, L->d_perm, L->d_tiles, L->d_items, dq_hi, dq_lo, kb0, kp,
+          tabs, n_species, L->d_adj_ioff, L->d_adj_joff, part);
+      LAUNCH_CHECK(ctx);
+    }
+    adjoint_reduce_kernel<<<(unsigned)L->tiles.size(), 96, 0, ctx->stream>>>(
+        part, L->d_adj_tile_ptr, L->d_adj_entries, L->d_tiles, L->d_perm,
+        (int)L->tiles.size(), grad);
     LAUNCH_CHECK(ctx);
   }
   return PYIID_OK;
@@ -848,6 +910,8 @@ int pyiid_variant_count(int kernel) {
       return kNumFq;
     case PYIID_KERNEL_GRAD_FQ:
       return kNumGrad;
+    case PYIID_KERNEL_ADJOINT:
+      return 2;
     default:
       return -1;
   }
@@ -868,6 +932,12 @@ int pyiid_variant_info(int kernel, int variant, int *params, int n_params) {
     params[2] = kTile * kGradTable[variant].v.CPC;
     return PYIID_OK;
   }
+  if (kernel == PYIID_KERNEL_ADJOINT && (variant == 0 || variant == 1)) {
+    params[0] = kAdjRS;               // bins between re-seeds
+    params[1] = variant == 0 ? 1 : 2; // evaluations per unordered pair
+    params[2] = kBlock;
+    return PYIID_OK;
+  }
   return fail(nullptr, PYIID_ERR_INVALID_ARG, "unknown kernel %d variant %d",
               kernel, variant);
 }
@@ -880,8 +950,10 @@ int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant) {
                 kernel, variant);
   if (kernel == PYIID_KERNEL_FQ)
     ctx->fq_variant = variant;
-  else
+  else if (kernel == PYIID_KERNEL_GRAD_FQ)
     ctx->grad_variant = variant;
+  else
+    ctx->adj_variant = variant;
   return PYIID_OK;
 }
 
@@ -889,6 +961,7 @@ int pyiid_get_variant(const pyiid_ctx *ctx, int kernel) {
   if (!ctx) return -1;
   if (kernel == PYIID_KERNEL_FQ) return ctx->fq_variant;
   if (kernel == PYIID_KERNEL_GRAD_FQ) return ctx->grad_variant;
+  if (kernel == PYIID_KERNEL_ADJOINT) return ctx->adj_variant;
   return -1;
 }
 

@@ -16,6 +16,7 @@ namespace pyiid {
 
 constexpr int kTile = 32;    // atoms per tile
 constexpr int kBlock = 256;  // threads per CTA of the pair kernels
+constexpr int kJMaxTiles = 32;  // max J tiles per F(Q) work item
 
 // Tile descriptor: start (in sorted order), atom count, configuration, species.
 // (stored as int4)
@@ -795,6 +796,173 @@ __global__ void __launch_bounds__(kBlock)
     for (int gg = 0; gg < ngrp; ++gg) sum += sred[gg][a][cpt];
     grad[(size_t)perm[ti.x + a] * 3 + cpt] = sum;
   }
+}
+
+// ======================================================= symmetric adjoint
+// Each unordered pair once.  CTA = F(Q) work item (tile I, tiles [J0, J1) with
+// J <= I); lane a of tile I, warp (group) gp handles b = gp, gp + 8, ... of
+// each tile J (for the diagonal tile only b < a).  The i-side
+// s_ab (x_a - x_b) accumulates in the lane's registers; the j-side
+// -s_ab (x_a - x_b) of atom b is summed over the warp's 32 lanes with
+// shuffles and kept in shared memory per (J, b).  Each CTA writes its i-side
+// rows [32][3] at part[ioff[item]] and its j-side rows [(J1-J0)*32][3] at
+// part[joff[item]]; adjoint_reduce_kernel adds them per atom in a fixed
+// order (bitwise reproducible).  Table layout and recurrence as in
+// adjoint_kernel.
+template <int RS>
+__global__ void __launch_bounds__(kBlock)
+    adjoint_sym_kernel(const float *__restrict__ pos,
+                       const int *__restrict__ perm,
+                       const int4 *__restrict__ tiles,
+                       const int4 *__restrict__ items, float dq_hi,
+                       float dq_lo, int kb0, int kp,
+                       const float4 *__restrict__ tabs, int n_species,
+                       const int *__restrict__ ioff,
+                       const int *__restrict__ joff,
+                       float *__restrict__ part) {
+  static_assert(RS % 4 == 0, "RS must be a multiple of 4");
+  extern __shared__ float4 stab[];  // [kp/2] for this item's species pair
+  __shared__ float4 sI[kTile], sJ[kTile];
+  __shared__ float sred[kBlock / kTile][kTile][3];
+  __shared__ float sjac[kJMaxTiles][kTile][3];
+
+  const int4 it = items[blockIdx.x];
+  const int4 ti = tiles[it.x];
+  const int tid = threadIdx.x;
+  const int lane = tid % kTile;
+  const int grp = tid / kTile;
+  const int ngrp = blockDim.x / kTile;
+  const int kh = kp / 2;
+  const int sa = ti.w;
+  const int sbs = tiles[it.y].w;  // every tile of the item has this species
+
+  const float4 *src =
+      tabs + (((size_t)ti.z * n_species + sa) * n_species + sbs) * kh;
+  for (int i = tid; i < kh; i += blockDim.x) stab[i] = src[i];
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+  for (int i = tid; i < (it.z - it.y) * kTile * 3; i += blockDim.x)
+    (&sjac[0][0][0])[i] = 0.f;
+
+  float gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int tj = it.y; tj < it.z; ++tj) {
+    const int4 tJ = tiles[tj];
+    const int jl = tj - it.y;
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool diag = (tj == it.x);
+    const float4 pa = sI[lane < ti.y ? lane : 0];
+    for (int b = grp; b < tJ.y; b += ngrp) {
+      const bool valid = (lane < ti.y) && (!diag || b < lane);
+      float jx = 0.f, jy = 0.f, jz = 0.f;
+      if (valid) {
+        const float4 pb = sJ[b];
+        float dx, dy, dz;
+        PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                   dq_lo, dx, dy, dz);
+        const float beta = -(p.inv_r * p.inv_r * p.inv_r);
+        const float2 c1 = f2(beta * p.ch), c2 = f2(beta * p.sh);
+        const float gam = -p.r * dq_hi / (2.0f * p.ch);
+        const float2 kpos = f2(p.kappa), kneg = f2(-p.kappa);
+        float2 ae = f2(0.f), ao = f2(0.f), be = f2(0.f), bo = f2(0.f);
+        for (int blk = 0; blk < kh; blk += RS / 2) {
+          float2 s, co;
+          seed_sincos2((float)(kb0 + 2 * blk), p.th_hi, p.th_lo, s, co);
+          float2 t = __fmul2_rn(f2(beta), s);
+          float2 w = __ffma2_rn(co, c1, __fmul2_rn(s, c2));
+          const float4 *tb = stab + blk;
+          if (blk + RS / 2 <= kh) {
+#pragma unroll
+            for (int m = 0; m < RS / 2; m += 2) {
+              float4 wt = tb[m];
+              float2 wn = __ffma2_rn(kneg, t, w);
+              ae = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ae);
+              be = __ffma2_rn(make_float2(wt.z, wt.w), t, be);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+              wt = tb[m + 1];
+              wn = __ffma2_rn(kneg, t, w);
+              ao = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ao);
+              bo = __ffma2_rn(make_float2(wt.z, wt.w), t, bo);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+            }
+          } else {
+            const int nm = kh - blk;
+            for (int m = 0; m < nm; m += 2) {
+              float4 wt = tb[m];
+              float2 wn = __ffma2_rn(kneg, t, w);
+              ae = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ae);
+              be = __ffma2_rn(make_float2(wt.z, wt.w), t, be);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+              wt = tb[m + 1];
+              wn = __ffma2_rn(kneg, t, w);
+              ao = __ffma2_rn(make_float2(wt.x, wt.y), __fadd2_rn(w, wn), ao);
+              bo = __ffma2_rn(make_float2(wt.z, wt.w), t, bo);
+              t = __ffma2_rn(kpos, wn, t);
+              w = wn;
+            }
+          }
+        }
+        const float sg = p.sigma2;
+        const float A = (ae.x + ae.y) + sg * (ao.x + ao.y);
+        const float B = (be.x + be.y) + sg * (bo.x + bo.y);
+        const float sab = fmaf(gam, A, B);
+        gx = fmaf(sab, dx, gx);
+        gy = fmaf(sab, dy, gy);
+        gz = fmaf(sab, dz, gz);
+        jx = -sab * dx;
+        jy = -sab * dy;
+        jz = -sab * dz;
+      }
+      // j-side: sum over the warp's lanes (all 32 lanes take part)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        jx += __shfl_xor_sync(0xffffffffu, jx, o);
+        jy += __shfl_xor_sync(0xffffffffu, jy, o);
+        jz += __shfl_xor_sync(0xffffffffu, jz, o);
+      }
+      if (lane == 0) {
+        sjac[jl][b][0] += jx;
+        sjac[jl][b][1] += jy;
+        sjac[jl][b][2] += jz;
+      }
+    }
+  }
+  sred[grp][lane][0] = gx;
+  sred[grp][lane][1] = gy;
+  sred[grp][lane][2] = gz;
+  __syncthreads();
+  float *pi = part + ioff[blockIdx.x];
+  for (int i = tid; i < kTile * 3; i += blockDim.x) {
+    const int a = i / 3, c = i % 3;
+    float sum = 0.f;
+    for (int gg = 0; gg < ngrp; ++gg) sum += sred[gg][a][c];
+    pi[i] = sum;
+  }
+  float *pj = part + joff[blockIdx.x];
+  for (int i = tid; i < (it.z - it.y) * kTile * 3; i += blockDim.x)
+    pj[i] = (&sjac[0][0][0])[i];
+}
+
+// grad[perm[t.start + a]][c] = sum of the partial rows listed for tile t
+// (CSR: entries tile_ptr[t] .. tile_ptr[t+1]-1 are float offsets of
+// [32][3] blocks), in list order.
+__global__ void adjoint_reduce_kernel(const float *__restrict__ part,
+                                      const int *__restrict__ tile_ptr,
+                                      const int *__restrict__ entries,
+                                      const int4 *__restrict__ tiles,
+                                      const int *__restrict__ perm,
+                                      int n_tiles, float *__restrict__ grad) {
+  const int t = blockIdx.x;
+  if (t >= n_tiles) return;
+  const int4 ti = tiles[t];
+  const int i = threadIdx.x;  // 0 .. 95
+  if (i >= ti.y * 3) return;
+  float s = 0.f;
+  for (int e = tile_ptr[t]; e < tile_ptr[t + 1]; ++e) s += part[entries[e] + i];
+  grad[(size_t)perm[ti.x + i / 3] * 3 + i % 3] = s;
 }
 
 }  // namespace pyiid

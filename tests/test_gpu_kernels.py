@@ -296,3 +296,38 @@ def test_batch_fq_uneven_alloys_matches_oracle(D):
             assert rel(got[i, 2:], want[2:]) <= TOL_F
         single = D.fq(pos[a:b], sp[a:b], tab, 0.05, 2).cpu().numpy()
         assert np.array_equal(single, got[i])
+
+
+@pytest.mark.parametrize('variant', [0, 1])
+def test_adjoint_variants_match_oracle(D, variant):
+    """Symmetric (each pair once) and owner-computes adjoints agree with the
+    oracle on a multi-tile alloy batch (diagonal and off-diagonal tiles)."""
+    import torch
+    from pyiid_gb300._native import context
+    exp = O.update_experiment({'qmin': 0.6, 'qmax': 22.0, 'rmin': 0.5,
+                               'rmax': 14.0, 'rstep': 0.02})
+    qb = O.pdf_qbin(exp)
+    rg = O.r_grid(exp)
+    nb = int(np.floor(exp['qmax'] / qb))
+    sizes = [70, 33, 97]
+    rng = np.random.default_rng(5)
+    pos = np.concatenate([S.random_cube(n, 11.0, 200 + i)
+                          for i, n in enumerate(sizes)])
+    nums = rng.choice([78, 79], sum(sizes))
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    sp, tab, _ = species_tables(nums, qb, nb)
+    gobs = O.pdf_fft(O.fq(S.random_cube(50, 9.0, 3), np.repeat(tab[1:], 50, 0),
+                          qb), exp['rstep'], qb, rg, exp['qmin'])
+    ctx = context()
+    old = ctx.get_variant('adjoint')
+    try:
+        ctx.set_variant('adjoint', variant)
+        out = D.batch_potential_grad(pos, sp, offs, tab, qb, exp['rstep'], rg,
+                                     exp['qmin'], torch.as_tensor(gobs))
+    finally:
+        ctx.set_variant('adjoint', old)
+    g = out['grad'].cpu().numpy()
+    for i in range(len(sizes)):
+        a, b = offs[i], offs[i + 1]
+        _, tg = O.true_grad_potential(pos[a:b], tab[sp[a:b]], exp, gobs)
+        assert rel(g[a:b], tg) <= TOL_G, (variant, i, rel(g[a:b], tg))
