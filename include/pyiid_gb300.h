@@ -228,6 +228,47 @@ int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
                      float *fq);
 
 /* ------------------------------------------------------------------------ *
+ * Learned surrogate of the potential (first stage of delayed acceptance).
+ *
+ * No counterpart in the reference: these serve the delayed-acceptance
+ * sampler that cheaply screens proposals before the exact Debye potential.
+ *
+ * Radial-basis descriptors of every atom of a packed batch:
+ *   feat[a][c] = sum_{b != a, same configuration, r < r_cut}
+ *                exp(-(r_ab - mu_c)^2 / (2 sigma^2)) (1 + cos(pi r_ab/r_cut))/2,
+ *   mu_c = c r_cut / (n_centres - 1),  2 <= n_centres <= 64.
+ *   positions : device float [total][3];  offsets : host int32 [n_configs+1]
+ *   feat_bf16 : device bfloat16 [total][n_centres]
+ *   feat_f32  : device float [total][n_centres] or NULL */
+int pyiid_rbf_features(pyiid_ctx *ctx, const float *positions,
+                       const int32_t *offsets, int n_configs, int n_centres,
+                       float r_cut, float sigma, void *feat_bf16,
+                       float *feat_f32);
+
+/* Per-atom MLP  y_a = w3 . silu(W2^T silu(W1^T x_a + b1) + b2) + b3  summed
+ * per configuration: energy[c] = sum_{a in c} y_a (FP64).  The two hidden
+ * layers are BF16 tensor-core GEMMs with FP32 accumulation.
+ *   feat_bf16 : device bf16 [n_atoms][n_in]
+ *   w1_bf16   : device bf16 [n_in][n_hidden],  b1 : device float [n_hidden]
+ *   w2_bf16   : device bf16 [n_hidden][n_hidden], b2 : device float [n_hidden]
+ *   w3        : device float [n_hidden],       b3 : device float [1]
+ *   energy    : device double [n_configs]
+ * The activations are kept in the context for pyiid_mlp_backward. */
+int pyiid_mlp_forward(pyiid_ctx *ctx, const void *feat_bf16, int n_atoms,
+                      int n_in, const int32_t *offsets, int n_configs,
+                      const void *w1_bf16, const float *b1,
+                      const void *w2_bf16, const float *b2, const float *w3,
+                      const float *b3, int n_hidden, double *energy);
+
+/* Gradients of L with respect to the MLP parameters for the most recent
+ * pyiid_mlp_forward on this context, given d_energy = dL/denergy (device
+ * double [n_configs]).  Outputs are device float arrays shaped like the
+ * parameters (overwritten). */
+int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy, float *g_w1,
+                       float *g_b1, float *g_w2, float *g_b2, float *g_w3,
+                       float *g_b3);
+
+/* ------------------------------------------------------------------------ *
  * Launch-shape variants (autotuning).
  *
  * The pair kernels come in several launch shapes (bins per thread, pairs

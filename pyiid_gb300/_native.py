@@ -50,6 +50,14 @@ _SIGNATURES = {
         _c_dbl, _f64p, _c_int, _c_dbl, _vp, _c_int, _vp, _vp, _vp, _vp]),
     'pyiid_fq_noalloc': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
                                   _c_int, _c_dbl, _c_int, _vp]),
+    'pyiid_rbf_features': (_c_int, [_vp, _vp, _i32p, _c_int, _c_int,
+                                    ctypes.c_float, ctypes.c_float, _vp,
+                                    _vp]),
+    'pyiid_mlp_forward': (_c_int, [_vp, _vp, _c_int, _c_int, _i32p, _c_int,
+                                   _vp, _vp, _vp, _vp, _vp, _vp, _c_int,
+                                   _vp]),
+    'pyiid_mlp_backward': (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    _vp]),
     'pyiid_variant_count': (_c_int, [_c_int]),
     'pyiid_variant_info': (_c_int, [_c_int, _c_int, _i32p, _c_int]),
     'pyiid_set_variant': (_c_int, [_vp, _c_int, _c_int]),

@@ -368,7 +368,7 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
   TRY(upload(ctx, &L->d_key_item_begin, L->key_item_begin));
   TRY(upload(ctx, &L->d_spair, L->spair_species));
   ctx->layouts.insert(ctx->layouts.begin(), std::move(L));
-  while (ctx->layouts.size() > 4) {
+  while (ctx->layouts.size() > 64) {
     free_layout(ctx->layouts.back().get());
     ctx->layouts.pop_back();
   }
@@ -424,7 +424,7 @@ int get_na(pyiid_ctx *ctx, const Layout *L, const float *scatter, int n_bins,
   T->key = key;
   TRY(upload(ctx, &T->d_na, na));
   ctx->nas.insert(ctx->nas.begin(), std::move(T));
-  while (ctx->nas.size() > 4) {
+  while (ctx->nas.size() > 64) {
     cudaFree(ctx->nas.back()->d_na);
     ctx->nas.pop_back();
   }
@@ -631,8 +631,15 @@ int pyiid_create(pyiid_ctx **out, int device) {
   return PYIID_OK;
 }
 
+}  // extern "C"
+namespace {
+void mlp_forget(const pyiid_ctx *ctx);
+}
+extern "C" {
+
 int pyiid_destroy(pyiid_ctx *ctx) {
   if (!ctx) return PYIID_OK;
+  mlp_forget(ctx);
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto &kv : ctx->bufs) cudaFree(kv.second.p);
@@ -1143,5 +1150,237 @@ extern "C" int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
   LAUNCH_CHECK(ctx);
   // the host vectors are released on return: wait for the copies only
   CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  return PYIID_OK;
+}
+
+// =============================================================== surrogate
+// Radial-basis descriptors and the per-atom MLP of the delayed-acceptance
+// surrogate.  The forward pass keeps its activations in the context
+// workspace; pyiid_mlp_backward differentiates the most recent forward.
+#include "surrogate_kernels.cuh"
+
+namespace {
+
+struct MlpState {
+  int n_atoms = 0, n_in = 0, n_hidden = 0, n_configs = 0;
+  const __nv_bfloat16 *feat = nullptr, *w1 = nullptr, *w2 = nullptr;
+  const float *w3 = nullptr;
+  int *atom_cfg = nullptr;
+  uint64_t cfg_key = 0;
+};
+std::mutex g_mlp_mu;
+std::unordered_map<const pyiid_ctx *, MlpState> g_mlp;
+
+void mlp_forget(const pyiid_ctx *ctx) {
+  std::lock_guard<std::mutex> lk(g_mlp_mu);
+  g_mlp.erase(ctx);
+}
+
+// atom -> configuration map and offsets on the device (cached by content)
+int config_map(pyiid_ctx *ctx, const int32_t *offsets, int n_configs,
+               int **d_cfg, int **d_off) {
+  const int total = offsets[n_configs];
+  uint64_t key = fnv1a(offsets, sizeof(int32_t) * (n_configs + 1));
+  void *p;
+  TRY(ensure(ctx, "sg_cfg", sizeof(int) * std::max(total, 1), &p));
+  *d_cfg = static_cast<int *>(p);
+  TRY(ensure(ctx, "sg_off", sizeof(int) * (n_configs + 1), &p));
+  *d_off = static_cast<int *>(p);
+  std::lock_guard<std::mutex> lk(g_mlp_mu);
+  MlpState &S = g_mlp[ctx];
+  if (S.cfg_key != key || S.atom_cfg != *d_cfg) {
+    std::vector<int> cfg(std::max(total, 1), 0);
+    for (int c = 0; c < n_configs; ++c)
+      for (int a = offsets[c]; a < offsets[c + 1]; ++a) cfg[a] = c;
+    CUDA_TRY(ctx, cudaMemcpy(*d_cfg, cfg.data(), sizeof(int) * cfg.size(),
+                             cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMemcpy(*d_off, offsets, sizeof(int) * (n_configs + 1),
+                             cudaMemcpyHostToDevice));
+    S.cfg_key = key;
+    S.atom_cfg = *d_cfg;
+  }
+  return PYIID_OK;
+}
+
+template <bool TA, bool TB>
+int gemm(pyiid_ctx *ctx, const __nv_bfloat16 *A, int lda,
+         const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
+         int K, int accumulate) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  gemm_bf16_kernel<TA, TB><<<grid, 128, 0, ctx->stream>>>(A, lda, B, ldb, C,
+                                                          ldc, M, N, K,
+                                                          accumulate);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int check_offsets(pyiid_ctx *ctx, const int32_t *offsets, int n_configs) {
+  if (!offsets || n_configs < 1 || offsets[0] != 0)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad offsets");
+  for (int c = 0; c < n_configs; ++c)
+    if (offsets[c + 1] < offsets[c])
+      return fail(ctx, PYIID_ERR_INVALID_ARG, "offsets must be non-decreasing");
+  return PYIID_OK;
+}
+
+}  // namespace
+
+extern "C" int pyiid_rbf_features(pyiid_ctx *ctx, const float *positions,
+                                  const int32_t *offsets, int n_configs,
+                                  int n_centres, float r_cut, float sigma,
+                                  void *feat_bf16, float *feat_f32) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  TRY(check_offsets(ctx, offsets, n_configs));
+  if (n_centres < 2 || n_centres > 64)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "n_centres must be in [2, 64]");
+  if (!(r_cut > 0) || !(sigma > 0))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "r_cut and sigma must be > 0");
+  const int total = offsets[n_configs];
+  if (total == 0) return PYIID_OK;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  int *d_cfg, *d_off;
+  TRY(config_map(ctx, offsets, n_configs, &d_cfg, &d_off));
+  const int warps = 8;
+  rbf_features_kernel<<<(total + warps - 1) / warps, 32 * warps, 0,
+                        ctx->stream>>>(
+      positions, d_cfg, d_off, total, n_centres, r_cut, sigma,
+      static_cast<__nv_bfloat16 *>(feat_bf16), feat_f32);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+extern "C" int pyiid_mlp_forward(pyiid_ctx *ctx, const void *feat_bf16,
+                                 int n_atoms, int n_in, const int32_t *offsets,
+                                 int n_configs, const void *w1_bf16,
+                                 const float *b1, const void *w2_bf16,
+                                 const float *b2, const float *w3,
+                                 const float *b3, int n_hidden,
+                                 double *energy) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  TRY(check_offsets(ctx, offsets, n_configs));
+  if (offsets[n_configs] != n_atoms)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "offsets[n_configs] != n_atoms");
+  if (n_in < 1 || n_hidden < 1)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad layer sizes");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  int *d_cfg, *d_off;
+  TRY(config_map(ctx, offsets, n_configs, &d_cfg, &d_off));
+  const size_t nh = (size_t)std::max(n_atoms, 1) * n_hidden;
+  void *p;
+  TRY(ensure(ctx, "sg_h1", nh * sizeof(float), &p));
+  float *h1 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_pre1", nh * sizeof(float), &p));
+  float *pre1 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_h1b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *h1b = static_cast<__nv_bfloat16 *>(p);
+  TRY(ensure(ctx, "sg_h2", nh * sizeof(float), &p));
+  float *h2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_pre2", nh * sizeof(float), &p));
+  float *pre2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_h2b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *h2b = static_cast<__nv_bfloat16 *>(p);
+  TRY(ensure(ctx, "sg_y", sizeof(float) * std::max(n_atoms, 1), &p));
+  float *y = static_cast<float *>(p);
+  const __nv_bfloat16 *X = static_cast<const __nv_bfloat16 *>(feat_bf16);
+  const __nv_bfloat16 *W1 = static_cast<const __nv_bfloat16 *>(w1_bf16);
+  const __nv_bfloat16 *W2 = static_cast<const __nv_bfloat16 *>(w2_bf16);
+  if (n_atoms > 0) {
+    TRY((gemm<false, false>(ctx, X, n_in, W1, n_hidden, h1, n_hidden, n_atoms,
+                            n_hidden, n_in, 0)));
+    bias_silu_kernel<<<512, 256, 0, ctx->stream>>>(h1, b1, n_atoms, n_hidden,
+                                                   h1b, pre1);
+    LAUNCH_CHECK(ctx);
+    TRY((gemm<false, false>(ctx, h1b, n_hidden, W2, n_hidden, h2, n_hidden,
+                            n_atoms, n_hidden, n_hidden, 0)));
+    bias_silu_kernel<<<512, 256, 0, ctx->stream>>>(h2, b2, n_atoms, n_hidden,
+                                                   h2b, pre2);
+    LAUNCH_CHECK(ctx);
+    head_kernel<<<(n_atoms * 32 + 255) / 256, 256, 0, ctx->stream>>>(
+        h2, w3, b3, n_atoms, n_hidden, y);
+    LAUNCH_CHECK(ctx);
+  }
+  reduce_by_config_kernel<<<n_configs, 256, 0, ctx->stream>>>(y, d_off,
+                                                              n_configs, energy);
+  LAUNCH_CHECK(ctx);
+  std::lock_guard<std::mutex> lk(g_mlp_mu);
+  MlpState &S = g_mlp[ctx];
+  S.n_atoms = n_atoms;
+  S.n_in = n_in;
+  S.n_hidden = n_hidden;
+  S.n_configs = n_configs;
+  S.feat = X;
+  S.w1 = W1;
+  S.w2 = W2;
+  S.w3 = w3;
+  return PYIID_OK;
+}
+
+extern "C" int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy,
+                                  float *g_w1, float *g_b1, float *g_w2,
+                                  float *g_b2, float *g_w3, float *g_b3) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  MlpState S;
+  {
+    std::lock_guard<std::mutex> lk(g_mlp_mu);
+    auto it = g_mlp.find(ctx);
+    if (it == g_mlp.end() || !it->second.feat)
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "pyiid_mlp_backward needs a preceding pyiid_mlp_forward");
+    S = it->second;
+  }
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  const int n = S.n_atoms, H = S.n_hidden, I = S.n_in;
+  if (n == 0) {
+    CUDA_TRY(ctx, cudaMemsetAsync(g_w1, 0, sizeof(float) * I * H, ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(g_b1, 0, sizeof(float) * H, ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(g_w2, 0, sizeof(float) * H * H, ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(g_b2, 0, sizeof(float) * H, ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(g_w3, 0, sizeof(float) * H, ctx->stream));
+    CUDA_TRY(ctx, cudaMemsetAsync(g_b3, 0, sizeof(float), ctx->stream));
+    return PYIID_OK;
+  }
+  const size_t nh = (size_t)n * H;
+  void *p;
+  TRY(ensure(ctx, "sg_h1b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *h1b = static_cast<__nv_bfloat16 *>(p);
+  TRY(ensure(ctx, "sg_pre1", nh * sizeof(float), &p));
+  float *pre1 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_h2", nh * sizeof(float), &p));
+  float *h2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_pre2", nh * sizeof(float), &p));
+  float *pre2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_d1", nh * sizeof(float), &p));
+  float *d1 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_d2", nh * sizeof(float), &p));
+  float *d2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sg_d1b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *d1b = static_cast<__nv_bfloat16 *>(p);
+  TRY(ensure(ctx, "sg_d2b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *d2b = static_cast<__nv_bfloat16 *>(p);
+  const int *cfg = g_mlp[ctx].atom_cfg;
+  // head: dw3 = sum_a de h2[a], db3 = sum_a de, dh2 = de w3
+  column_sum_kernel<<<H, 256, 0, ctx->stream>>>(h2, n, H, d_energy, cfg, g_w3);
+  LAUNCH_CHECK(ctx);
+  column_sum_kernel<<<1, 256, 0, ctx->stream>>>(nullptr, n, 1, d_energy, cfg,
+                                                g_b3);
+  LAUNCH_CHECK(ctx);
+  head_backward_kernel<<<512, 256, 0, ctx->stream>>>(d_energy, cfg, h2, S.w3,
+                                                     n, H, d2, d2b);
+  LAUNCH_CHECK(ctx);
+  // layer 2: dz2 = dh2 silu'(pre2); dW2 = h1^T dz2; db2 = colsum; dh1 = dz2 W2^T
+  silu_backward_kernel<<<512, 256, 0, ctx->stream>>>(d2, pre2, nh, d2b, d2);
+  LAUNCH_CHECK(ctx);
+  TRY((gemm<true, false>(ctx, h1b, H, d2b, H, g_w2, H, H, H, n, 0)));
+  column_sum_kernel<<<H, 256, 0, ctx->stream>>>(d2, n, H, nullptr, nullptr,
+                                                g_b2);
+  LAUNCH_CHECK(ctx);
+  TRY((gemm<false, true>(ctx, d2b, H, S.w2, H, d1, H, n, H, H, 0)));
+  // layer 1: dz1 = dh1 silu'(pre1); dW1 = X^T dz1; db1 = colsum
+  silu_backward_kernel<<<512, 256, 0, ctx->stream>>>(d1, pre1, nh, d1b, d1);
+  LAUNCH_CHECK(ctx);
+  TRY((gemm<true, false>(ctx, S.feat, I, d1b, H, g_w1, H, I, H, n, 0)));
+  column_sum_kernel<<<H, 256, 0, ctx->stream>>>(d1, n, H, nullptr, nullptr,
+                                                g_b1);
+  LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }

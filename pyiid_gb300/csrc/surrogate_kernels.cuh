@@ -1,0 +1,276 @@
+// surrogate_kernels.cuh -- the learned first stage of delayed acceptance.
+//
+// Per-atom radial-basis descriptors and a small MLP whose summed per-atom
+// outputs estimate a configuration's Rw.  The MLP layers are BF16 GEMMs on
+// the tensor cores (mma.sync m16n8k16, FP32 accumulate); the descriptors and
+// activations are plain FP32 kernels.  Shapes are small (32 -> 128 -> 128 ->
+// 1 per atom), so the GEMM favours simplicity: 64 x 64 CTA tiles staged in
+// shared memory, one K step of 16 per iteration.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace pyiid {
+
+// ------------------------------------------------------------- descriptors
+// feat[a][c] = sum_{b != a, same configuration} exp(-(r - mu_c)^2 / (2 s^2))
+//              * fc(r),   mu_c = c * rc / (C - 1),  fc(r) = (1 + cos(pi r/rc))/2
+// for r < rc (0 beyond).  One warp per atom a; lane l owns centres l, l+32
+// (C <= 64), every lane walks all b of the configuration (uniform branches,
+// broadcast loads), so no atomics are needed.  Written as BF16 (the MLP
+// input) and optionally FP32.
+__global__ void rbf_features_kernel(const float *__restrict__ pos,
+                                    const int *__restrict__ atom_cfg,
+                                    const int *__restrict__ offsets,
+                                    int n_atoms, int n_centres, float rc,
+                                    float sigma, __nv_bfloat16 *__restrict__ fb,
+                                    float *__restrict__ ff) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (a >= n_atoms) return;
+  const int cfg = atom_cfg[a];
+  const int b0 = offsets[cfg], b1 = offsets[cfg + 1];
+  const float ax = pos[3 * a], ay = pos[3 * a + 1], az = pos[3 * a + 2];
+  const float step = rc / (float)(n_centres - 1);
+  const float inv2s2 = 0.5f / (sigma * sigma);
+  const float mu0 = lane * step, mu1 = (lane + 32) * step;
+  const float rc2 = rc * rc;
+  float acc0 = 0.f, acc1 = 0.f;
+  for (int b = b0; b < b1; ++b) {
+    const float dx = pos[3 * b] - ax, dy = pos[3 * b + 1] - ay,
+                dz = pos[3 * b + 2] - az;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (b == a || r2 >= rc2) continue;
+    const float r = sqrtf(r2);
+    const float fc = 0.5f * (1.f + cospif(r / rc));
+    const float d0 = r - mu0, d1 = r - mu1;
+    acc0 = fmaf(fc, __expf(-d0 * d0 * inv2s2), acc0);
+    acc1 = fmaf(fc, __expf(-d1 * d1 * inv2s2), acc1);
+  }
+  if (lane < n_centres) {
+    fb[(size_t)a * n_centres + lane] = __float2bfloat16_rn(acc0);
+    if (ff) ff[(size_t)a * n_centres + lane] = acc0;
+  }
+  if (lane + 32 < n_centres) {
+    fb[(size_t)a * n_centres + lane + 32] = __float2bfloat16_rn(acc1);
+    if (ff) ff[(size_t)a * n_centres + lane + 32] = acc1;
+  }
+}
+
+// ------------------------------------------------------------------- GEMM
+// C[M][N] (+)= op(A) op(B), BF16 inputs, FP32 accumulate and output.
+//   TA = false: A is [M][K] row-major (lda); TA = true: A is stored [K][M].
+//   TB = false: B is [K][N] row-major (ldb); TB = true: B is stored [N][K].
+// CTA tile 64 x 64, 4 warps each owning a 32 x 32 sub-tile (2 x 4 mma tiles
+// of 16 x 8), K stepped by 16 through shared memory.  Out-of-range elements
+// are loaded as zero and never stored.
+//
+// mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 fragments (per lane,
+// g = lane / 4, q = lane % 4):
+//   A: a0 = (g, 2q..2q+1), a1 = (g+8, 2q..), a2 = (g, 2q+8..), a3 = (g+8, 2q+8..)
+//   B: b0 = (k 2q..2q+1, n g), b1 = (k 2q+8.., n g)
+//   C: c0 = (g, 2q), c1 = (g, 2q+1), c2 = (g+8, 2q), c3 = (g+8, 2q+1)
+__device__ __forceinline__ unsigned pack_bf16(__nv_bfloat16 lo,
+                                              __nv_bfloat16 hi) {
+  const unsigned short l = __bfloat16_as_ushort(lo);
+  const unsigned short h = __bfloat16_as_ushort(hi);
+  return (unsigned)l | ((unsigned)h << 16);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const unsigned (&a)[4],
+                                               const unsigned (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128)
+    gemm_bf16_kernel(const __nv_bfloat16 *__restrict__ A, int lda,
+                     const __nv_bfloat16 *__restrict__ B, int ldb,
+                     float *__restrict__ C, int ldc, int M, int N, int K,
+                     int accumulate) {
+  __shared__ __nv_bfloat16 sA[64][16 + 8];  // [m][k]
+  __shared__ __nv_bfloat16 sB[64][16 + 8];  // [n][k]
+  const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int g = lane >> 2, q = lane & 3;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+  const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int e = tid; e < 64 * 16; e += 128) {
+      const int r = e / 16, kk = e % 16;
+      const int gm = m0 + r, gk = k0 + kk;
+      __nv_bfloat16 v = z;
+      if (gm < M && gk < K)
+        v = TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      sA[r][kk] = v;
+      const int gn = n0 + r;
+      __nv_bfloat16 w = z;
+      if (gn < N && gk < K)
+        w = TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+      sB[r][kk] = w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int r = wm + i * 16;
+      unsigned af[4];
+      af[0] = pack_bf16(sA[r + g][2 * q], sA[r + g][2 * q + 1]);
+      af[1] = pack_bf16(sA[r + g + 8][2 * q], sA[r + g + 8][2 * q + 1]);
+      af[2] = pack_bf16(sA[r + g][2 * q + 8], sA[r + g][2 * q + 9]);
+      af[3] = pack_bf16(sA[r + g + 8][2 * q + 8], sA[r + g + 8][2 * q + 9]);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int cn = wn + j * 8;
+        unsigned bf[2];
+        bf[0] = pack_bf16(sB[cn + g][2 * q], sB[cn + g][2 * q + 1]);
+        bf[1] = pack_bf16(sB[cn + g][2 * q + 8], sB[cn + g][2 * q + 9]);
+        mma_bf16_16816(acc[i][j], af, bf);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int gm = m0 + wm + i * 16 + g + (e >= 2 ? 8 : 0);
+        const int gn = n0 + wn + j * 8 + 2 * q + (e & 1);
+        if (gm < M && gn < N) {
+          float *p = C + (size_t)gm * ldc + gn;
+          *p = accumulate ? *p + acc[i][j][e] : acc[i][j][e];
+        }
+      }
+}
+
+// --------------------------------------------------------- elementwise ops
+// h = silu(z + bias) for z [rows][n] (FP32 in place), also as BF16.
+//   silu(x) = x / (1 + e^-x)
+__global__ void bias_silu_kernel(float *__restrict__ z,
+                                 const float *__restrict__ bias, int rows,
+                                 int n, __nv_bfloat16 *__restrict__ hb,
+                                 float *__restrict__ pre) {
+  const size_t total = (size_t)rows * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float x = z[i] + bias[i % n];
+    if (pre) pre[i] = x;
+    const float h = x / (1.f + __expf(-x));
+    z[i] = h;
+    hb[i] = __float2bfloat16_rn(h);
+  }
+}
+
+// dz = dh * silu'(pre),  silu'(x) = s (1 + x (1 - s)),  s = 1 / (1 + e^-x);
+// written as BF16 for the next GEMMs and FP32.
+__global__ void silu_backward_kernel(const float *__restrict__ dh,
+                                     const float *__restrict__ pre,
+                                     size_t total,
+                                     __nv_bfloat16 *__restrict__ dzb,
+                                     float *__restrict__ dz) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float x = pre[i];
+    const float s = 1.f / (1.f + __expf(-x));
+    const float v = dh[i] * s * (1.f + x * (1.f - s));
+    dz[i] = v;
+    dzb[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// Output layer and per-configuration sum: y[a] = h2[a] . w3 + b3,
+// e[cfg] = sum_a y[a] (FP64).  One warp per atom; per-configuration sums
+// are reduced by reduce_by_config_kernel.
+__global__ void head_kernel(const float *__restrict__ h2,
+                            const float *__restrict__ w3, const float *b3,
+                            int rows, int n, float *__restrict__ y) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= rows) return;
+  float s = 0.f;
+  for (int i = lane; i < n; i += 32) s = fmaf(h2[(size_t)warp * n + i], w3[i], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[warp] = s + b3[0];
+}
+
+__global__ void reduce_by_config_kernel(const float *__restrict__ y,
+                                        const int *__restrict__ offsets,
+                                        int n_configs,
+                                        double *__restrict__ e) {
+  const int c = blockIdx.x;
+  if (c >= n_configs) return;
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int a = offsets[c] + threadIdx.x; a < offsets[c + 1]; a += blockDim.x)
+    s += (double)y[a];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) e[c] = sm[0];
+}
+
+// Head backward: given dL/de[cfg] (FP64), dy[a] = dL/de[cfg(a)];
+//   dh2[a][i] = dy[a] w3[i]  (FP32 and BF16), dw3[i] = sum_a dy[a] h2[a][i],
+//   db3 = sum_a dy[a].
+__global__ void head_backward_kernel(const double *__restrict__ de,
+                                     const int *__restrict__ atom_cfg,
+                                     const float *__restrict__ h2,
+                                     const float *__restrict__ w3, int rows,
+                                     int n, float *__restrict__ dh2,
+                                     __nv_bfloat16 *__restrict__ dh2b) {
+  const size_t total = (size_t)rows * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int a = (int)(i / n), j = (int)(i % n);
+    const float v = (float)de[atom_cfg[a]] * w3[j];
+    dh2[i] = v;
+    dh2b[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// Column sums over rows: out[j] = sum_a M[a][j] * (scale ? scale[a] : 1)
+// (bias gradients; dw3 with scale = dy per row).  One block per column.
+__global__ void column_sum_kernel(const float *__restrict__ Mx, int rows,
+                                  int n, const double *__restrict__ de,
+                                  const int *__restrict__ atom_cfg,
+                                  float *__restrict__ out) {
+  const int j = blockIdx.x;
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int a = threadIdx.x; a < rows; a += blockDim.x) {
+    const double w = de ? de[atom_cfg[a]] : 1.0;
+    s += w * (Mx ? (double)Mx[(size_t)a * n + j] : 1.0);
+  }
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[j] = (float)sm[0];
+}
+
+__global__ void to_bf16_kernel(const float *__restrict__ x, size_t n,
+                               __nv_bfloat16 *__restrict__ y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+
+}  // namespace pyiid

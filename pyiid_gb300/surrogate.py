@@ -1,0 +1,267 @@
+"""Learned surrogate of Rw and the delayed-acceptance Metropolis sampler.
+
+Surrogate: per-atom Gaussian radial-basis descriptors (32 centres on
+[0, 8] A with a cosine cutoff, ``pyiid_rbf_features``) feed a per-atom MLP
+32 -> 128 -> 128 -> 1 (SiLU; BF16 tensor-core GEMMs, FP32 accumulate,
+``pyiid_mlp_forward`` / ``pyiid_mlp_backward``) whose outputs summed over a
+configuration estimate its Rw.  It is trained online on (configuration,
+exact Rw) pairs produced by the exact sampler; the parameter update (Adam)
+is a handful of elementwise torch ops on the FP32 master copy.
+
+Delayed acceptance (Christen & Fox, J. Comput. Graph. Stat. 14, 2005):
+a proposal x' is first accepted with probability
+    a1 = min(1, exp(-(E~(x') - E~(x)) / kT))       (surrogate E~ = conv Rw~)
+and only then with
+    a2 = min(1, exp(-(E(x') - E(x)) / kT + (E~(x') - E~(x)) / kT))
+using the exact Debye energy E.  The product kernel satisfies detailed
+balance with respect to exp(-E/kT): the chain's target is unchanged and the
+exact potential remains the judge of every accepted move.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import debye
+from ._native import context
+from .atoms import kB
+
+__all__ = ['RBFMLPSurrogate', 'DelayedAcceptanceMH', 'ExactSingleAtomMH',
+           'da_stage1', 'da_stage2']
+
+
+def da_stage1(log_u1, ds, kT):
+    """First-stage acceptance on the surrogate energy change ds."""
+    return log_u1 < -ds / kT
+
+
+def da_stage2(log_u2, de, ds, kT):
+    """Second-stage acceptance on the exact change de, corrected by the
+    surrogate change ds (Christen & Fox 2005, eq. 2)."""
+    return log_u2 < -(de - ds) / kT
+
+
+def _vp(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _i32(a):
+    a = np.ascontiguousarray(np.asarray(a, np.int32))
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class RBFMLPSurrogate:
+    """Sum over atoms of an MLP of radial-basis descriptors.
+
+    Inputs are standardised with statistics of the first training batch,
+    folded into the first layer (W1' = W1 / s, b1' = b1 - (mu / s) W1).
+    """
+
+    def __init__(self, n_centres=32, r_cut=8.0, sigma=None, n_hidden=128,
+                 lr=2e-3, seed=0, device=None):
+        self.C = int(n_centres)
+        self.rc = float(r_cut)
+        self.sigma = float(sigma if sigma is not None else
+                           r_cut / (n_centres - 1))
+        self.H = int(n_hidden)
+        self.dev = torch.device('cuda' if device is None else device)
+        g = torch.Generator(device='cpu').manual_seed(int(seed))
+        C, H = self.C, self.H
+        self.params = {
+            'w1': torch.randn(C, H, generator=g) * (1.0 / np.sqrt(C)),
+            'b1': torch.zeros(H),
+            'w2': torch.randn(H, H, generator=g) * (1.0 / np.sqrt(H)),
+            'b2': torch.zeros(H),
+            'w3': torch.randn(H, generator=g) * (0.1 / np.sqrt(H)),
+            'b3': torch.zeros(1),
+        }
+        self.params = {k: v.to(self.dev).float().contiguous()
+                       for k, v in self.params.items()}
+        self.m = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.v = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.t = 0
+        self.lr = float(lr)
+        self.mu = None
+        self.scale = None
+        self.ctx = context(self.dev.index)
+
+    # ------------------------------------------------------------ kernels
+    def features(self, positions, offsets, want_f32=False):
+        """BF16 descriptors [N, C] (and FP32 when asked) of packed positions."""
+        pos = debye.as_positions(positions)
+        off, offp = _i32(offsets)
+        n = int(off[-1])
+        fb = torch.empty((n, self.C), dtype=torch.bfloat16, device=self.dev)
+        ff = (torch.empty((n, self.C), dtype=torch.float32, device=self.dev)
+              if want_f32 else None)
+        self.ctx.call('pyiid_rbf_features', _vp(pos), offp, len(off) - 1,
+                      self.C, ctypes.c_float(self.rc),
+                      ctypes.c_float(self.sigma), _vp(fb), _vp(ff))
+        return (fb, ff) if want_f32 else fb
+
+    def _effective(self):
+        p = self.params
+        if self.mu is None:
+            w1, b1 = p['w1'], p['b1']
+        else:
+            w1 = p['w1'] / self.scale[:, None]
+            b1 = p['b1'] - (self.mu / self.scale) @ p['w1']
+        return (w1.to(torch.bfloat16).contiguous(), b1.contiguous(),
+                p['w2'].to(torch.bfloat16).contiguous())
+
+    def forward(self, feat_bf16, offsets):
+        """Rw estimates [B] (FP64) for descriptor rows of packed configs."""
+        off, offp = _i32(offsets)
+        w1b, b1, w2b = self._effective()
+        self._last = (w1b, b1, w2b)  # keep alive for backward
+        e = torch.empty(len(off) - 1, dtype=torch.float64, device=self.dev)
+        p = self.params
+        self.ctx.call('pyiid_mlp_forward', _vp(feat_bf16), int(off[-1]),
+                      self.C, offp, len(off) - 1, _vp(w1b), _vp(b1),
+                      _vp(w2b), _vp(p['b2']), _vp(p['w3']), _vp(p['b3']),
+                      self.H, _vp(e))
+        return e
+
+    def backward(self, d_energy):
+        """Parameter gradients (in the standardised parametrisation) of the
+        last forward for dL/dE = d_energy [B]."""
+        g = {k: torch.empty_like(v) for k, v in self.params.items()}
+        self.ctx.call('pyiid_mlp_backward', _vp(d_energy.double().contiguous()),
+                      _vp(g['w1']), _vp(g['b1']), _vp(g['w2']), _vp(g['b2']),
+                      _vp(g['w3']), _vp(g['b3']))
+        if self.mu is not None:
+            # back through W1' = W1 / s, b1' = b1 - (mu / s) W1
+            g['w1'] = g['w1'] / self.scale[:, None] - \
+                (self.mu / self.scale)[:, None] * g['b1'][None, :]
+        return g
+
+    # ------------------------------------------------------------ training
+    def fit_normalisation(self, feat_bf16):
+        f = feat_bf16.float()
+        self.mu = f.mean(0)
+        self.scale = f.std(0).clamp_min(1e-3)
+
+    def predict(self, positions, offsets):
+        return self.forward(self.features(positions, offsets), offsets)
+
+    def train_step(self, feat_bf16, offsets, target):
+        """One Adam step on the mean squared error; returns the loss."""
+        if self.mu is None:
+            self.fit_normalisation(feat_bf16)
+        e = self.forward(feat_bf16, offsets)
+        t = target.to(device=self.dev, dtype=torch.float64)
+        r = e - t
+        loss = float((r * r).mean().item())
+        g = self.backward(2.0 * r / len(r))
+        self.t += 1
+        b1, b2, eps = 0.9, 0.999, 1e-8
+        for k, p in self.params.items():
+            gk = g[k].float()
+            self.m[k].mul_(b1).add_(gk, alpha=1 - b1)
+            self.v[k].mul_(b2).addcmul_(gk, gk, value=1 - b2)
+            mh = self.m[k] / (1 - b1 ** self.t)
+            vh = self.v[k] / (1 - b2 ** self.t)
+            p.sub_(self.lr * mh / (vh.sqrt() + eps))
+        return loss
+
+
+class ExactSingleAtomMH:
+    """Lock-step single-atom Metropolis on the exact potential (one move per
+    chain per iteration).  The comparator of the delayed-acceptance chain."""
+
+    def __init__(self, pot, positions, temperature=300.0, step=0.1, seed=0):
+        self.pot = pot
+        self.kT = kB * float(temperature)
+        self.step = float(step)
+        self.n = int(np.diff(pot.offsets)[0])
+        assert np.all(np.diff(pot.offsets) == self.n), 'equal-size chains'
+        self.B = pot.n_configs
+        self.x = torch.as_tensor(np.asarray(positions, np.float32),
+                                 device=pot.device).reshape(self.B, self.n, 3
+                                                            ).clone()
+        self.gen = torch.Generator(device=pot.device).manual_seed(int(seed))
+        self.e = pot.evaluate(self.x.reshape(-1, 3), want_grad=False)[0].clone()
+        self.accepted = 0
+        self.proposed = 0
+        self.exact_evals = 0
+
+    def _propose(self):
+        d = self.pot.device
+        idx = torch.randint(0, self.n, (self.B,), generator=self.gen, device=d)
+        xp = self.x.clone()
+        ar = torch.arange(self.B, device=d)
+        xp[ar, idx] += self.step * torch.randn((self.B, 3), generator=self.gen,
+                                               device=d)
+        return xp
+
+    def iterate(self):
+        xp = self._propose()
+        ep = self.pot.evaluate(xp.reshape(-1, 3), want_grad=False)[0]
+        self.exact_evals += self.B
+        logu = torch.log(torch.rand(self.B, generator=self.gen,
+                                    device=self.x.device, dtype=torch.float64))
+        acc = logu < -(ep - self.e) / self.kT
+        self.x = torch.where(acc[:, None, None], xp, self.x)
+        self.e = torch.where(acc, ep, self.e)
+        self.accepted += int(acc.sum().item())
+        self.proposed += self.B
+
+
+class DelayedAcceptanceMH(ExactSingleAtomMH):
+    """Single-atom delayed-acceptance Metropolis: surrogate first stage,
+    exact Debye second stage (only for proposals that pass the first)."""
+
+    def __init__(self, pot, surrogate, positions, temperature=300.0, step=0.1,
+                 seed=0):
+        super().__init__(pot, positions, temperature, step, seed)
+        self.sur = surrogate
+        self.off = pot.offsets
+        self.es = self._surrogate(self.x)
+        self.stage1_passed = 0
+
+    def _surrogate(self, x):
+        return self.pot.conv * self.sur.predict(x.reshape(-1, 3), self.off)
+
+    def iterate(self):
+        xp = self._propose()
+        esp = self._surrogate(xp)
+        d = self.x.device
+        u = torch.rand((2, self.B), generator=self.gen, device=d,
+                       dtype=torch.float64)
+        ds = esp - self.es
+        pass1 = da_stage1(torch.log(u[0]), ds, self.kT)
+        sel = torch.nonzero(pass1).flatten()
+        k = int(sel.numel())
+        self.proposed += self.B
+        self.stage1_passed += k
+        if k == 0:
+            return
+        # exact energies of the proposals that passed, as one batch of k
+        # configurations of the same atoms
+        ep = self._exact_subset(xp[sel])
+        self.exact_evals += k
+        acc = da_stage2(torch.log(u[1][sel]), ep - self.e[sel], ds[sel],
+                        self.kT)
+        take = sel[acc]
+        self.x[take] = xp[take]
+        self.e[take] = ep[acc]
+        self.es[take] = esp[take]
+        self.accepted += int(acc.sum().item())
+
+    def _exact_subset(self, xs):
+        from .sampling import PDFPotential
+        k = xs.shape[0]
+        sub = getattr(self, '_subpots', {}).get(k)
+        if sub is None:
+            p = self.pot
+            sub = PDFPotential.__new__(PDFPotential)
+            sub.__dict__.update(p.__dict__)
+            sub.n_configs = k
+            sub.offsets = (np.arange(k + 1) * self.n).astype(np.int32)
+            sub.species = p.species[:k * self.n]
+            sub.n_total = k * self.n
+            sub.masses = p.masses[:k * self.n]
+            sub._out = None
+            self._subpots = getattr(self, '_subpots', {})
+            self._subpots[k] = sub
+        return sub.evaluate(xs.reshape(-1, 3), want_grad=False)[0]
