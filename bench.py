@@ -247,7 +247,8 @@ def run_gpu(args, rank, world, local):
     workloads = {}
     if rank == 0 and not args.no_workloads:
         for name, fn in (('batched_fq_256_alloys', run_batched),
-                         ('hmc_64_chains_au1000', run_hmc)):
+                         ('hmc_64_chains_au1000', run_hmc),
+                         ('delayed_acceptance_au1000', run_delayed_acceptance)):
             try:
                 workloads[name] = fn(torch)
             except Exception as e:  # noqa: BLE001 -- reported, not fatal
@@ -404,6 +405,66 @@ def run_hmc(torch, iters=6):
             'ms_per_iteration': 1e3 * s / iters,
             'ms_per_force_eval_64_chains': e0.elapsed_time(e1) / 3,
             'launch': 'CUDA graph replay per HMC iteration (11 batched exact evaluations)'}
+
+
+def run_delayed_acceptance(torch, iters=20):
+    """Configuration 5: 1,000-atom Au, 64 chains, single-atom moves
+    sigma = 0.1 A, E = 100 Rw at 300 K.  The surrogate is pre-trained on 256
+    exact (configuration, Rw) pairs of displaced particles and trained online
+    from the second-stage exact evaluations during the timed run.  Compared
+    with exact single-atom Metropolis on the same chains."""
+    from pyiid_gb300 import structures, debye
+    from pyiid_gb300.sampling import PDFPotential, experiment_grids
+    from pyiid_gb300.scatter_factors import species_tables
+    from pyiid_gb300.surrogate import (RBFMLPSurrogate, DelayedAcceptanceMH,
+                                       ExactSingleAtomMH)
+    exp, qb, nb, rg = experiment_grids(None)
+    ref = structures.fcc_nearest(4.08, 1000).astype(np.float32)
+    sp, tab, _ = species_tables([79] * 1000, qb, nb)
+    gobs = debye.pdf(debye.fq(ref, sp, tab, qb), qb, exp['rstep'], rg,
+                     exp['qmin']).cpu().numpy()
+    # exact training pool
+    sig = np.random.default_rng(5).uniform(0.01, 0.2, 256)
+    pool = np.stack([structures.displaced(ref, s, 5000 + i)
+                     for i, s in enumerate(sig)])
+    ppot = PDFPotential([79] * 1000, gobs, None, n_configs=256)
+    t0 = time.perf_counter()
+    rw = ppot.evaluate(torch.as_tensor(pool.reshape(-1, 3), device='cuda'),
+                       want_grad=False)[0].clone()
+    sur = RBFMLPSurrogate(seed=0, lr=3e-3)
+    fb = sur.features(pool.reshape(-1, 3), ppot.offsets)
+    for _ in range(200):
+        loss = sur.train_step(fb, ppot.offsets, rw)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    start = np.stack([structures.displaced(ref, 0.05, 4 + c) for c in range(64)])
+    pot = PDFPotential([79] * 1000, gobs, None, conv=100.0, n_configs=64)
+    out = {'workload': '1000-atom fcc Au, 64 chains, single-atom moves 0.1 A, '
+                       '300 K, E = 100 Rw; surrogate RBF(32, 8 A) -> MLP '
+                       '32-128-128-1 BF16',
+           'pretrain_s': t_train, 'pretrain_final_mse': loss}
+    for name, mk in (
+            ('delayed_acceptance', lambda: DelayedAcceptanceMH(
+                pot, sur, start, temperature=300, step=0.1, seed=6,
+                train_every=5, train_steps=1, train_batch=32)),
+            ('exact_single_atom_mh', lambda: ExactSingleAtomMH(
+                pot, start, temperature=300, step=0.1, seed=6))):
+        ch = mk()
+        for _ in range(3):
+            ch.iterate()
+        torch.cuda.synchronize()
+        a0, e0, p0 = ch.accepted, ch.exact_evals, ch.proposed
+        t = time.perf_counter()
+        for _ in range(iters):
+            ch.iterate()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        acc = ch.accepted - a0
+        out[name] = {'accepted_steps_per_s': acc / dt,
+                     'proposals_per_s': (ch.proposed - p0) / dt,
+                     'acceptance': acc / max(ch.proposed - p0, 1),
+                     'exact_evals_per_accepted': (ch.exact_evals - e0) / max(acc, 1)}
+    return out
 
 
 # ------------------------------------------------------------- CPU arm

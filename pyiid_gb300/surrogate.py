@@ -209,20 +209,62 @@ class ExactSingleAtomMH:
 
 class DelayedAcceptanceMH(ExactSingleAtomMH):
     """Single-atom delayed-acceptance Metropolis: surrogate first stage,
-    exact Debye second stage (only for proposals that pass the first)."""
+    exact Debye second stage (only for proposals that pass the first).
+
+    Online training: every exact second-stage evaluation is stored in a
+    replay buffer of (configuration, exact Rw) pairs; every ``train_every``
+    iterations the surrogate takes ``train_steps`` Adam steps on a random
+    batch of ``train_batch`` buffered pairs.  Surrogate energies of the
+    current states are refreshed after training (the first stage compares
+    both ends with the same network, as detailed balance requires).
+    """
 
     def __init__(self, pot, surrogate, positions, temperature=300.0, step=0.1,
-                 seed=0):
+                 seed=0, train_every=0, train_steps=1, train_batch=64,
+                 buffer_size=512):
         super().__init__(pot, positions, temperature, step, seed)
         self.sur = surrogate
         self.off = pot.offsets
         self.es = self._surrogate(self.x)
         self.stage1_passed = 0
+        self.train_every = int(train_every)
+        self.train_steps = int(train_steps)
+        self.train_batch = int(train_batch)
+        self.buf_x = torch.empty((int(buffer_size), self.n, 3),
+                                 dtype=torch.float32, device=pot.device)
+        self.buf_e = torch.empty(int(buffer_size), dtype=torch.float64,
+                                 device=pot.device)
+        self.buf_n = 0
+        self.buf_i = 0
+        self.iters = 0
+
+    def _remember(self, xs, rw):
+        cap = self.buf_x.shape[0]
+        for j in range(xs.shape[0]):
+            self.buf_x[self.buf_i] = xs[j]
+            self.buf_e[self.buf_i] = rw[j]
+            self.buf_i = (self.buf_i + 1) % cap
+            self.buf_n = min(self.buf_n + 1, cap)
+
+    def _train(self):
+        if self.buf_n < 2:
+            return
+        b = min(self.train_batch, self.buf_n)
+        off = (np.arange(b + 1) * self.n).astype(np.int32)
+        for _ in range(self.train_steps):
+            idx = torch.randint(0, self.buf_n, (b,), generator=self.gen,
+                                device=self.x.device)
+            fb = self.sur.features(self.buf_x[idx].reshape(-1, 3), off)
+            self.sur.train_step(fb, off, self.buf_e[idx])
+        self.es = self._surrogate(self.x)
 
     def _surrogate(self, x):
         return self.pot.conv * self.sur.predict(x.reshape(-1, 3), self.off)
 
     def iterate(self):
+        self.iters += 1
+        if self.train_every and self.iters % self.train_every == 0:
+            self._train()
         xp = self._propose()
         esp = self._surrogate(xp)
         d = self.x.device
@@ -240,6 +282,8 @@ class DelayedAcceptanceMH(ExactSingleAtomMH):
         # configurations of the same atoms
         ep = self._exact_subset(xp[sel])
         self.exact_evals += k
+        if self.train_every:
+            self._remember(xp[sel], ep / self.pot.conv)
         acc = da_stage2(torch.log(u[1][sel]), ep - self.e[sel], ds[sel],
                         self.kT)
         take = sel[acc]
