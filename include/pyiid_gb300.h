@@ -203,6 +203,61 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
                                double *energy, float *grad, double *gcalc,
                                float *fq);
 
+/* ------------------------------------------------------------------------ *
+ * Single-atom Metropolis moves with O(N K) exact energy changes.
+ *
+ * Each chain (configuration) keeps its raw Debye sums
+ *   S_k = sum_{a>b} f_a(Q_k) f_b(Q_k) sin(Q_k r_ab) / r_ab   (PDF grid, FP64)
+ * on the device.  A step proposes, for every chain, one atom and a Gaussian
+ * displacement, computes the exact change of S from the N-1 pair terms of
+ * that atom, the proposed F, G(r) and potential V', and accepts with
+ * probability min(1, exp(-conv (V' - V) / kT)).  This is the exact energy
+ * difference the reference's single-move samplers obtain by re-evaluating
+ * the whole configuration (sim/gcmc.py:13-114 add_atom / del_atom call
+ * get_potential_energy on a copy; hmc.py:95-209 the same for HMC moves),
+ * at O(N K) instead of O(N^2 K) per proposal.
+ *
+ * pyiid_mh_init: full exact evaluation of every chain (the states' S and
+ * potential); call it to start and whenever positions were changed by
+ * anything else (it also bounds the FP64 drift of the running sums).
+ *   positions : device float  [total][3]
+ *   species, offsets, scatter, grids, gobs, potential: as
+ *               pyiid_batch_potential_grad (scatter on the PDF grid)
+ *   sraw      : device double [n_configs][n_bins]  (out: S_k, 0 below qmin)
+ *   energy    : device double [n_configs][2]       (out: V, scale)
+ *
+ * pyiid_mh_steps: n_steps Metropolis steps of every chain, enqueued without
+ * host synchronisation (4 kernels per step; capturable in a CUDA graph once
+ * a first call has sized the context's buffers).
+ *   positions : device float [total][3], updated in place
+ *   conv, kT  : energy = conv * V; kT > 0 in the same unit
+ *   sigma     : displacement standard deviation per coordinate
+ *   seed      : generator key.  Proposal t of chain c depends only on
+ *               (seed, c, t): Philox4x32-10 counters (t, c, 0/1)
+ *   sraw, energy : the state from pyiid_mh_init (updated)
+ *   counter   : device uint64 [n_configs], proposals made so far per chain
+ *               (start at 0; advanced by one per step)
+ *   accepted  : device int64  [n_configs], incremented on acceptance
+ *   trace     : device double [n_steps][n_configs][8] or NULL:
+ *               atom (index within its configuration), proposed x, y, z,
+ *               log u, V', accepted (0/1), V before the step
+ * A proposal that makes two atoms coincide, or any NaN potential, is
+ * rejected.  Chains with fewer than two atoms never move. */
+int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
+                  const int32_t *species, const int32_t *offsets,
+                  int n_configs, const float *scatter, int n_species,
+                  int n_bins, double qstep, double rstep, const double *rgrid,
+                  int n_r, double qmin, const double *gobs, int potential,
+                  double *sraw, double *energy);
+int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
+                   const int32_t *offsets, int n_configs, const float *scatter,
+                   int n_species, int n_bins, double qstep, double rstep,
+                   const double *rgrid, int n_r, double qmin,
+                   const double *gobs, int potential, double conv, double kT,
+                   float sigma, uint64_t seed, int n_steps, double *sraw,
+                   double *energy, uint64_t *counter, int64_t *accepted,
+                   double *trace);
+
 /* F(Q) without device allocation.
  *
  * Same arguments, result and error behaviour as pyiid_fq, for callers that

@@ -24,6 +24,7 @@
 
 #include "../../include/pyiid_gb300.h"
 #include "debye_kernels.cuh"
+#include "move_kernels.cuh"
 #include "transform_kernels.cuh"
 
 using namespace pyiid;
@@ -128,6 +129,14 @@ struct Layout {
   // [32][3] blocks that sum to its gradient rows
   std::vector<int> adj_ioff, adj_joff, adj_tile_ptr, adj_entries;
   size_t adj_total = 0;
+  // single-atom moves: items (configuration, species, tile run [t0, t1)) of
+  // at most kMoveTiles tiles, CSR by configuration
+  std::vector<int4> mitems;
+  std::vector<int> mitem_begin;
+  int4 *d_mitems = nullptr;
+  int *d_mitem_begin = nullptr;
+  int *d_offsets = nullptr;
+  int *d_species = nullptr;
   int *d_adj_ioff = nullptr;
   int *d_adj_joff = nullptr;
   int *d_adj_tile_ptr = nullptr;
@@ -255,6 +264,10 @@ void free_layout(Layout *L) {
   cudaFree(L->d_adj_joff);
   cudaFree(L->d_adj_tile_ptr);
   cudaFree(L->d_adj_entries);
+  cudaFree(L->d_mitems);
+  cudaFree(L->d_mitem_begin);
+  cudaFree(L->d_offsets);
+  cudaFree(L->d_species);
 }
 
 // Builds (or finds) the layout of a packed batch.
@@ -305,6 +318,14 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
             make_int4(start[s] + a, std::min(kTile, count[s] - a), c, s));
     const int t1 = (int)L->tiles.size();
     L->cfg_tiles[c] = make_int2(t0, t1);
+    L->mitem_begin.push_back((int)L->mitems.size());
+    for (int t = t0; t < t1;) {
+      int te = t;
+      while (te < t1 && L->tiles[te].w == L->tiles[t].w && te - t < kMoveTiles)
+        ++te;
+      L->mitems.push_back(make_int4(c, L->tiles[t].w, t, te));
+      t = te;
+    }
     for (int sa = 0; sa < n_species; ++sa)
       for (int sb = 0; sb <= sa; ++sb) {
         const double na = count[sa], nb = count[sb];
@@ -367,6 +388,14 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
   TRY(upload(ctx, &L->d_items, L->items));
   TRY(upload(ctx, &L->d_key_item_begin, L->key_item_begin));
   TRY(upload(ctx, &L->d_spair, L->spair_species));
+  L->mitem_begin.push_back((int)L->mitems.size());
+  TRY(upload(ctx, &L->d_mitems, L->mitems));
+  TRY(upload(ctx, &L->d_mitem_begin, L->mitem_begin));
+  TRY(upload(ctx, &L->d_offsets, L->offsets));
+  {
+    std::vector<int> sp(species, species + total);
+    TRY(upload(ctx, &L->d_species, sp));
+  }
   ctx->layouts.insert(ctx->layouts.begin(), std::move(L));
   while (ctx->layouts.size() > 64) {
     free_layout(ctx->layouts.back().get());
@@ -906,6 +935,137 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
     adjoint_reduce_kernel<<<(unsigned)L->tiles.size(), 96, 0, ctx->stream>>>(
         part, L->d_adj_tile_ptr, L->d_adj_entries, L->d_tiles, L->d_perm,
         (int)L->tiles.size(), grad);
+    LAUNCH_CHECK(ctx);
+  }
+  return PYIID_OK;
+}
+
+// ------------------------------------------------- single-atom Metropolis
+// Shared validation and cached tables of pyiid_mh_init / pyiid_mh_steps.
+static int mh_prepare(pyiid_ctx *ctx, const int32_t *species,
+                      const int32_t *offsets, int n_configs,
+                      const float *scatter, int n_species, int n_bins,
+                      double qstep, double rstep, const double *rgrid,
+                      int n_r, double qmin, int potential, Layout **L,
+                      float **ftab, double **na, TMatrix **T) {
+  TRY(check_common(ctx, n_configs, offsets, n_species, n_bins, qstep, 0));
+  if (n_r < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_r < 1");
+  if (n_bins > 12288)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "n_bins > 12288 is not supported");
+  if (potential != PYIID_POTENTIAL_RW && potential != PYIID_POTENTIAL_CHI_SQ)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "unknown potential %d", potential);
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  TRY(get_layout(ctx, species, offsets, n_configs, n_species, L));
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, ftab));
+  TRY(get_na(ctx, *L, scatter, n_bins, na));
+  TRY(get_tmatrix(ctx, n_bins, qstep, rstep, rgrid, n_r, qmin, T));
+  return PYIID_OK;
+}
+
+int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
+                  const int32_t *species, const int32_t *offsets,
+                  int n_configs, const float *scatter, int n_species,
+                  int n_bins, double qstep, double rstep, const double *rgrid,
+                  int n_r, double qmin, const double *gobs, int potential,
+                  double *sraw, double *energy) {
+  Layout *L;
+  float *d_ftab;
+  double *d_na;
+  TMatrix *T;
+  TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
+                 qstep, rstep, rgrid, n_r, qmin, potential, &L, &d_ftab, &d_na,
+                 &T));
+  void *p;
+  TRY(ensure(ctx, "mh_fq", (size_t)n_configs * n_bins * sizeof(float), &p));
+  float *d_fq = static_cast<float *>(p);
+  TRY(ensure(ctx, "mh_gcalc", (size_t)n_configs * n_r * sizeof(double), &p));
+  double *d_gc = static_cast<double *>(p);
+  TRY(run_fq(ctx, L, positions, d_ftab, d_na, n_bins, qstep, T->kmin, d_fq,
+             sraw));
+  dim3 gp((n_r + 255) / 256, n_configs);
+  pdf_kernel<<<gp, 256, n_bins * sizeof(float), ctx->stream>>>(
+      d_fq, T->d_T, n_bins, n_r, T->kmin, d_gc);
+  LAUNCH_CHECK(ctx);
+  potential_kernel<<<n_configs, 256, 0, ctx->stream>>>(gobs, d_gc, n_r,
+                                                       potential, energy,
+                                                       nullptr);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
+                   const int32_t *offsets, int n_configs, const float *scatter,
+                   int n_species, int n_bins, double qstep, double rstep,
+                   const double *rgrid, int n_r, double qmin,
+                   const double *gobs, int potential, double conv, double kT,
+                   float sigma, uint64_t seed, int n_steps, double *sraw,
+                   double *energy, uint64_t *counter, int64_t *accepted,
+                   double *trace) {
+  if (!(kT > 0) || !std::isfinite(kT))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "kT must be a positive number");
+  if (!std::isfinite(conv))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "conv must be finite");
+  if (!(sigma >= 0) || !std::isfinite(sigma))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "sigma must be >= 0");
+  if (n_steps < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_steps < 0");
+  Layout *L;
+  float *d_ftab;
+  double *d_na;
+  TMatrix *T;
+  TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
+                 qstep, rstep, rgrid, n_r, qmin, potential, &L, &d_ftab, &d_na,
+                 &T));
+  const int n_mi = (int)L->mitems.size();
+  const int kmin = T->kmin;
+  const int kb0 = kmin & ~1;
+  void *p;
+  TRY(ensure(ctx, "mh_fq", (size_t)n_configs * n_bins * sizeof(float), &p));
+  float *d_fq = static_cast<float *>(p);
+  TRY(ensure(ctx, "mh_gcalc", (size_t)n_configs * n_r * sizeof(double), &p));
+  double *d_gc = static_cast<double *>(p);
+  TRY(ensure(ctx, "mh_ds", (size_t)n_configs * n_bins * sizeof(double), &p));
+  double *d_ds = static_cast<double *>(p);
+  TRY(ensure(ctx, "mh_prop", (size_t)n_configs * sizeof(MoveProposal), &p));
+  MoveProposal *d_prop = static_cast<MoveProposal *>(p);
+  TRY(ensure(ctx, "mh_partial",
+             (size_t)std::max(n_mi, 1) * n_bins * sizeof(double), &p));
+  double *d_part = static_cast<double *>(p);
+  // chunks of kMoveL bins; at most 16 chunks per CTA (>= 16 atom groups)
+  const int chunks_total = std::max(1, (n_bins - kb0 + kMoveL - 1) / kMoveL);
+  const int n_cb = (chunks_total + 15) / 16;
+  const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
+  const int n_groups = kBlock / n_chunks;
+  const size_t smem = 4 * kMoveTiles * kTile * sizeof(float4) +
+                      (size_t)n_groups * n_chunks * kMoveL * sizeof(float);
+  float dq_hi, dq_lo;
+  split_double(qstep, dq_hi, dq_lo);
+  const uint32_t seed_lo = (uint32_t)seed, seed_hi = (uint32_t)(seed >> 32);
+  for (int step = 0; step < n_steps; ++step) {
+    if (n_mi > 0) {
+      dim3 g1(n_mi, n_cb);
+      move_delta_kernel<<<g1, kBlock, smem, ctx->stream>>>(
+          positions, L->d_perm, L->d_tiles, L->d_mitems, L->d_mitem_begin,
+          L->d_offsets, reinterpret_cast<const unsigned long long *>(counter),
+          seed_lo, seed_hi, sigma, dq_hi, dq_lo, kb0, n_chunks, n_groups,
+          n_bins, d_prop, d_part);
+      LAUNCH_CHECK(ctx);
+    }
+    dim3 g2((n_bins + 127) / 128, n_configs);
+    move_fq_kernel<<<g2, 128, 0, ctx->stream>>>(
+        d_part, L->d_mitems, L->d_mitem_begin, L->d_offsets, L->d_species,
+        d_prop, d_ftab, d_na, sraw, n_bins, kmin, d_fq, d_ds);
+    LAUNCH_CHECK(ctx);
+    dim3 gp((n_r + 255) / 256, n_configs);
+    pdf_kernel<<<gp, 256, n_bins * sizeof(float), ctx->stream>>>(
+        d_fq, T->d_T, n_bins, n_r, kmin, d_gc);
+    LAUNCH_CHECK(ctx);
+    mh_accept_kernel<<<n_configs, 256, 0, ctx->stream>>>(
+        positions, L->d_offsets, d_prop, gobs, d_gc, n_r, potential, conv, kT,
+        d_ds, sraw, n_bins, energy,
+        reinterpret_cast<unsigned long long *>(counter),
+        reinterpret_cast<long long *>(accepted),
+        trace ? trace + (size_t)step * n_configs * 8 : nullptr);
     LAUNCH_CHECK(ctx);
   }
   return PYIID_OK;

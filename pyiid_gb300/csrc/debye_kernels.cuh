@@ -188,6 +188,17 @@ __global__ void __launch_bounds__(kBlock, 2)
   }
 }
 
+// F_k = 2 * nan_to_num(float(S_k) / float(na_k)): the reference divides
+// float32 by float32 and nan_to_num's the result (+-inf -> +-FLT_MAX).
+__device__ __forceinline__ float fq_value(double s, double na) {
+  float v = (float)s / (float)na;
+  if (isnan(v)) v = 0.f;
+  if (isinf(v)) v = v > 0.f ? 3.402823466e38f : -3.402823466e38f;
+  float outv = 2.0f * v;
+  if (isinf(outv)) outv = outv > 0.f ? 3.402823466e38f : -3.402823466e38f;
+  return outv;
+}
+
 // Finishing kernel for F(Q): for configuration b and bin k
 //   S_k  = sum_sp f_sa f_sb sum_{items of key (b, sp)} partial[item][k]
 //   F_k  = 2 * nan_to_num(float(S_k / na_k))
@@ -218,13 +229,7 @@ __global__ void fq_finish_kernel(const double *__restrict__ partial,
            d;
     }
     sraw = s;
-    const double nak = na[(size_t)b * n_bins + k];
-    // the reference divides float32 by float32 and nan_to_num's the result
-    float v = (float)s / (float)nak;
-    if (isnan(v)) v = 0.f;
-    if (isinf(v)) v = v > 0.f ? 3.402823466e38f : -3.402823466e38f;
-    outv = 2.0f * v;
-    if (isinf(outv)) outv = outv > 0.f ? 3.402823466e38f : -3.402823466e38f;
+    outv = fq_value(s, na[(size_t)b * n_bins + k]);
   }
   if (fq) fq[(size_t)b * n_bins + k] = outv;
   if (fq_raw) fq_raw[(size_t)b * n_bins + k] = sraw;

@@ -67,13 +67,16 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *scratch) {
 // the scale uses the raw a even when the value used scale 1):
 //   c_i = pre [s E_i + (gc.E) (go_i - 2 a gc_i)/(gc.gc)],  E = go - s gc,
 //   pre = -Rw/|E|^2 (Rw) or -2 (chi^2).
-__global__ void potential_kernel(const double *__restrict__ gobs,
-                                 const double *__restrict__ gcalc, int n_r,
-                                 int potential, double *__restrict__ out,
-                                 float *__restrict__ cvec) {
-  __shared__ double scratch[32 * 3];
-  const int b = blockIdx.x;
-  const double *gc = gcalc + (size_t)b * n_r;
+struct PotentialValue {
+  double value, scale;  // potential and the scale it used
+  double a, gcc, ee, gce;
+};
+
+// The potential of one configuration, computed by the whole CTA (every
+// thread returns the same values).  scratch: 32 * 3 doubles of shared memory.
+__device__ __forceinline__ PotentialValue potential_value(
+    const double *__restrict__ gobs, const double *__restrict__ gc, int n_r,
+    int potential, double *scratch) {
   double v3[3] = {0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < n_r; i += blockDim.x) {
     const double c = gc[i], o = gobs[i];
@@ -93,19 +96,30 @@ __global__ void potential_kernel(const double *__restrict__ gobs,
     v2[1] += gc[i] * e;
   }
   block_sum<2>(v2, scratch);
-  const double ee = v2[0], gce = v2[1];
-  double value, pre;
-  if (potential == 0) {
-    if (a <= 0.0) {
-      value = 1.0;
-    } else {
-      value = sqrt(ee / goo);
-    }
-    pre = -value / ee;
-  } else {
-    value = ee;
-    pre = -2.0;
-  }
+  PotentialValue r;
+  r.ee = v2[0];
+  r.gce = v2[1];
+  r.a = a;
+  r.gcc = gcc;
+  r.scale = s;
+  if (potential == 0)
+    r.value = (a <= 0.0) ? 1.0 : sqrt(r.ee / goo);
+  else
+    r.value = r.ee;
+  return r;
+}
+
+__global__ void potential_kernel(const double *__restrict__ gobs,
+                                 const double *__restrict__ gcalc, int n_r,
+                                 int potential, double *__restrict__ out,
+                                 float *__restrict__ cvec) {
+  __shared__ double scratch[32 * 3];
+  const int b = blockIdx.x;
+  const double *gc = gcalc + (size_t)b * n_r;
+  const PotentialValue pv = potential_value(gobs, gc, n_r, potential, scratch);
+  const double value = pv.value, s = pv.scale, a = pv.a, gcc = pv.gcc;
+  const double ee = pv.ee, gce = pv.gce;
+  const double pre = (potential == 0) ? -value / ee : -2.0;
   if (threadIdx.x == 0) {
     out[2 * b] = value;
     out[2 * b + 1] = s;

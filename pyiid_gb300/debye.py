@@ -11,7 +11,7 @@ import torch
 from ._native import context, POTENTIALS, NativeError
 
 __all__ = ['fq', 'batch_fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
-           'batch_potential_grad', 'as_positions']
+           'batch_potential_grad', 'as_positions', 'mh_init', 'mh_steps']
 
 _f32p = None
 
@@ -217,3 +217,81 @@ def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
              ctypes.c_void_p(out['gcalc'].data_ptr()),
              ctypes.c_void_p(out['fq'].data_ptr()))
     return out
+
+
+def mh_init(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
+            gobs, kind='rw', state=None):
+    """Full exact evaluation that starts (or re-synchronises) single-atom
+    Metropolis chains: fills state['sraw'] [B, K] f64 (raw Debye sums on the
+    PDF grid) and state['energy'] [B, 2] f64 (potential, scale)."""
+    import ctypes
+    pos = as_positions(positions)
+    sp = _np(species, np.int32)
+    off = _np(offsets, np.int32)
+    tab = _np(scatter, np.float32)
+    rg = _np(rgrid, np.float64)
+    b = len(off) - 1
+    dev = pos.device
+    go = gobs.to(device=dev, dtype=torch.float64).contiguous()
+    if state is None:
+        state = {}
+    if state.get('sraw') is None:
+        state['sraw'] = torch.empty((b, tab.shape[1]), dtype=torch.float64,
+                                    device=dev)
+    if state.get('energy') is None:
+        state['energy'] = torch.empty((b, 2), dtype=torch.float64, device=dev)
+    ctx = context(dev.index)
+    ctx.call('pyiid_mh_init', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
+             _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
+             float(qstep), float(rstep), _ptr(rg, ctypes.c_double), len(rg),
+             float(qmin), ctypes.c_void_p(go.data_ptr()), POTENTIALS[kind],
+             ctypes.c_void_p(state['sraw'].data_ptr()),
+             ctypes.c_void_p(state['energy'].data_ptr()))
+    return state
+
+
+def mh_steps(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
+             gobs, state, n_steps, conv, kT, sigma, seed, kind='rw',
+             trace=None):
+    """Enqueue n_steps single-atom Metropolis steps of every chain.
+
+    positions [sum N, 3] f32 CUDA tensor, updated in place.  ``state`` holds
+    'sraw' and 'energy' (from mh_init), 'counter' (uint64 proposals per
+    chain, as int64 tensor) and 'accepted' (int64).  ``trace`` may be a
+    float64 CUDA tensor [n_steps, B, 8] receiving every proposal (atom,
+    x', y', z', log u, V', accepted, V)."""
+    import ctypes
+    pos = positions
+    if not (isinstance(pos, torch.Tensor) and pos.is_cuda and
+            pos.dtype == torch.float32 and pos.is_contiguous()):
+        raise NativeError('positions must be a contiguous float32 CUDA tensor '
+                          '(updated in place)')
+    sp = _np(species, np.int32)
+    off = _np(offsets, np.int32)
+    tab = _np(scatter, np.float32)
+    rg = _np(rgrid, np.float64)
+    b = len(off) - 1
+    dev = pos.device
+    go = gobs.to(device=dev, dtype=torch.float64).contiguous()
+    for key in ('counter', 'accepted'):
+        if state.get(key) is None:
+            state[key] = torch.zeros(b, dtype=torch.int64, device=dev)
+    if trace is not None:
+        _check_dev(trace, 'trace', torch.float64)
+        if trace.numel() < n_steps * b * 8:
+            raise NativeError('trace must hold n_steps * B * 8 values')
+    ctx = context(dev.index)
+    ctx.call('pyiid_mh_steps', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
+             _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
+             float(qstep), float(rstep), _ptr(rg, ctypes.c_double), len(rg),
+             float(qmin), ctypes.c_void_p(go.data_ptr()), POTENTIALS[kind],
+             float(conv), float(kT), float(sigma),
+             int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_steps),
+             ctypes.c_void_p(state['sraw'].data_ptr()),
+             ctypes.c_void_p(state['energy'].data_ptr()),
+             ctypes.c_void_p(state['counter'].data_ptr()),
+             ctypes.c_void_p(state['accepted'].data_ptr()),
+             ctypes.c_void_p(trace.data_ptr() if trace is not None else 0))
+    return state

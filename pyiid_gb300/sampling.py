@@ -12,6 +12,10 @@
   pyiid/sim/hmc.py:33-63), Metropolis accept/reject at temperature T.  With
   ``graph=True`` one whole iteration (momenta, trajectory, accept) is
   captured once in a CUDA graph and replayed.
+* :class:`SingleAtomMC` -- single-atom Metropolis chains whose exact energy
+  change costs O(N K) per proposal (``pyiid_mh_steps``): the raw Debye sums
+  of every chain stay on the device and only the moved atom's pair terms
+  are recomputed.
 
 Units are ASE's: Angstrom, eV, amu; time unit Angstrom * sqrt(amu / eV).
 The form factors of this API are species-correct (f evaluated at the PDF
@@ -28,7 +32,7 @@ from .atoms import kB
 from .scatter_factors import atomic_mass, form_factor_array
 
 __all__ = ['PDFPotential', 'potential_energy', 'BatchedHMC',
-           'experiment_grids']
+           'SingleAtomMC', 'experiment_grids']
 
 
 def experiment_grids(exp_dict=None):
@@ -237,3 +241,103 @@ class BatchedHMC:
 
     def positions(self):
         return self.x.reshape(-1, 3)
+
+
+class SingleAtomMC:
+    """Single-atom Metropolis chains over the configurations of a
+    PDFPotential, all on the device.
+
+    Every step proposes, in every chain, one uniformly chosen atom and a
+    displacement N(0, sigma^2) per coordinate, and accepts with probability
+    min(1, exp(-(E' - E) / kT)), E = conv * potential -- the acceptance rule
+    of the reference's Monte Carlo moves (pyiid/sim/hmc.py:66-92,
+    pyiid/sim/gcmc.py:13-114) with the exact energy difference, obtained in
+    O(N K) from the moved atom's pair terms instead of a full re-evaluation.
+
+    graph : capture ``steps_per_replay`` steps once in a CUDA graph and
+            replay it (the proposals depend only on (seed, chain, step), so
+            graph and eager runs give identical chains).
+    resync_every : steps between full exact re-evaluations of the running
+            sums (bounds their FP64 drift; None disables).
+    """
+
+    def __init__(self, pot, positions, temperature=300.0, sigma=0.1, seed=0,
+                 graph=False, steps_per_replay=32, resync_every=4096):
+        self.pot = pot
+        d = pot.device
+        self.kT = kB * float(temperature)
+        self.sigma = float(sigma)
+        self.seed = int(seed)
+        self.x = torch.as_tensor(np.asarray(positions, np.float32),
+                                 device=d).reshape(-1, 3).clone()
+        if self.x.shape[0] != pot.n_total:
+            raise ValueError(f'{self.x.shape[0]} positions for '
+                             f'{pot.n_total} atoms')
+        self.state = {}
+        self.resync_every = resync_every
+        self.steps_per_replay = int(steps_per_replay)
+        self.steps_done = 0
+        self._since_sync = 0
+        self.resync()
+        self.state['counter'] = torch.zeros(pot.n_configs, dtype=torch.int64,
+                                            device=d)
+        self.state['accepted'] = torch.zeros(pot.n_configs,
+                                             dtype=torch.int64, device=d)
+        self._enqueue(0)  # sizes the context's buffers
+        self.graph = None
+        if graph:
+            self._capture()
+
+    def _enqueue(self, n, trace=None):
+        p = self.pot
+        debye.mh_steps(self.x, p.species, p.offsets, p.table, p.qstep,
+                       p.exp['rstep'], p.rgrid, p.exp['qmin'], p.gobs,
+                       self.state, n, p.conv, self.kT, self.sigma, self.seed,
+                       kind=p.kind, trace=trace)
+
+    def _capture(self):
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._enqueue(self.steps_per_replay)
+
+    def resync(self):
+        """Recompute the running sums and energies of the current positions
+        by a full exact evaluation."""
+        p = self.pot
+        debye.mh_init(self.x, p.species, p.offsets, p.table, p.qstep,
+                      p.exp['rstep'], p.rgrid, p.exp['qmin'], p.gobs,
+                      kind=p.kind, state=self.state)
+        self._since_sync = 0
+
+    def step(self, n=1, trace=None):
+        """Advance every chain by n proposals.  ``trace`` (float64 CUDA
+        tensor [n, B, 8]) records each proposal; it disables the graph."""
+        done = 0
+        while done < n:
+            if self.resync_every and self._since_sync >= self.resync_every:
+                self.resync()
+            m = n - done
+            if self.resync_every:
+                m = min(m, self.resync_every - self._since_sync)
+            if (self.graph is not None and trace is None and
+                    m >= self.steps_per_replay):
+                self.graph.replay()
+                m = self.steps_per_replay
+            else:
+                tr = None if trace is None else trace[done:done + m]
+                self._enqueue(m, tr)
+            done += m
+            self._since_sync += m
+        self.steps_done += n
+        return self
+
+    def energies(self):
+        """conv * potential of the current state of every chain [B]."""
+        return self.state['energy'][:, 0] * self.pot.conv
+
+    def acceptance(self):
+        return (self.state['accepted'].double() /
+                max(self.steps_done, 1)).cpu().numpy()
+
+    def positions(self):
+        return self.x
