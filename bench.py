@@ -464,7 +464,36 @@ def run_delayed_acceptance(torch, iters=20):
                      'proposals_per_s': (ch.proposed - p0) / dt,
                      'acceptance': acc / max(ch.proposed - p0, 1),
                      'exact_evals_per_accepted': (ch.exact_evals - e0) / max(acc, 1)}
+    out['exact_incremental_mh'] = run_incremental_mh(torch, pot, start)
     return out
+
+
+def run_incremental_mh(torch, pot, start, n_steps=8192):
+    """Exact single-atom Metropolis with O(N K) energy changes
+    (pyiid_mh_steps), 64 proposals per chain per CUDA-graph replay, a full
+    re-synchronisation every 4096 steps included in the timing."""
+    from pyiid_gb300.sampling import SingleAtomMC
+    mc = SingleAtomMC(pot, start.reshape(-1, 3), temperature=300, sigma=0.1,
+                      seed=6, graph=True, steps_per_replay=64)
+    mc.step(256)
+    torch.cuda.synchronize()
+    a0 = int(mc.state['accepted'].sum().item())
+    ev0, ev1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+    t = time.perf_counter()
+    ev0.record()
+    mc.step(n_steps)
+    ev1.record()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    acc = int(mc.state['accepted'].sum().item()) - a0
+    props = n_steps * pot.n_configs
+    return {'accepted_steps_per_s': acc / dt,
+            'proposals_per_s': props / dt,
+            'acceptance': acc / props,
+            'us_per_step_all_chains': 1e6 * dt / n_steps,
+            'device_us_per_step': 1e3 * ev0.elapsed_time(ev1) / n_steps,
+            'exact_evals_per_accepted': props / max(acc, 1),
+            'pair_terms_per_proposal': 2 * 999 * pot.n_bins}
 
 
 # ------------------------------------------------------------- CPU arm

@@ -31,6 +31,7 @@
 #ifndef PYIID_GB300_H
 #define PYIID_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -206,35 +207,43 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
 /* ------------------------------------------------------------------------ *
  * Single-atom Metropolis moves with O(N K) exact energy changes.
  *
- * Each chain (configuration) keeps its raw Debye sums
- *   S_k = sum_{a>b} f_a(Q_k) f_b(Q_k) sin(Q_k r_ab) / r_ab   (PDF grid, FP64)
- * on the device.  A step proposes, for every chain, one atom and a Gaussian
- * displacement, computes the exact change of S from the N-1 pair terms of
- * that atom, the proposed F, G(r) and potential V', and accepts with
- * probability min(1, exp(-conv (V' - V) / kT)).  This is the exact energy
- * difference the reference's single-move samplers obtain by re-evaluating
- * the whole configuration (sim/gcmc.py:13-114 add_atom / del_atom call
- * get_potential_energy on a copy; hmc.py:95-209 the same for HMC moves),
- * at O(N K) instead of O(N^2 K) per proposal.
+ * A step proposes, for every chain (configuration), one atom and a Gaussian
+ * displacement, computes the exact change of the Debye sums
+ *   S_k = sum_{a>b} f_a(Q_k) f_b(Q_k) sin(Q_k r_ab) / r_ab   (PDF grid)
+ * from the N-1 pair terms of that atom, the proposed F and potential V', and
+ * accepts with probability min(1, exp(-conv (V' - V) / kT)).  This is the
+ * exact energy difference the reference's Monte Carlo moves obtain by
+ * re-evaluating the whole configuration (sim/gcmc.py:13-114 add_atom /
+ * del_atom call get_potential_energy on a copy; sim/hmc.py:66-92 mh_accept),
+ * at O(N K) instead of O(N^2 K) per proposal.  The potential is formed
+ * without G(r): with the transform G = T^T F, u = F.(T gobs) and
+ * q = F^T (T T^T) F give G.gobs and G.G; the chain state keeps S, F, u and q,
+ * and a proposal F' = F + dF updates u by dF.(T gobs) and q by
+ * dF^T (T T^T) (F + F'), so that it costs K^2, not K R.
  *
- * pyiid_mh_init: full exact evaluation of every chain (the states' S and
- * potential); call it to start and whenever positions were changed by
- * anything else (it also bounds the FP64 drift of the running sums).
- *   positions : device float  [total][3]
- *   species, offsets, scatter, grids, gobs, potential: as
- *               pyiid_batch_potential_grad (scatter on the PDF grid)
- *   sraw      : device double [n_configs][n_bins]  (out: S_k, 0 below qmin)
- *   energy    : device double [n_configs][2]       (out: V, scale)
+ * state (device double [pyiid_mh_state_size(n_configs, n_bins)]):
+ *   v [n_bins] (T gobs), gobs.gobs, 0, S [2][n_configs][n_bins],
+ *   (u, q) [n_configs], F [2][n_configs][n_bins] as float32, then
+ *   cur [n_configs] as int32: chain c's state is S[cur[c]][c], F[cur[c]][c]
+ *   (the other buffer holds the last proposal).
+ *
+ * pyiid_mh_init: full exact evaluation of every chain into state and
+ * energy (device double [n_configs][2]: V, scale); call it to start, when
+ * gobs changes, and whenever positions were changed by anything else (it
+ * also bounds the drift of the running sums).  Arguments as
+ * pyiid_batch_potential_grad (scatter on the PDF grid).  The first call for a
+ * grid builds T T^T on the device (n_bins^2 doubles, kept with T); at most
+ * 6400 bins above qmin.
  *
  * pyiid_mh_steps: n_steps Metropolis steps of every chain, enqueued without
- * host synchronisation (4 kernels per step; capturable in a CUDA graph once
- * a first call has sized the context's buffers).
+ * host synchronisation (3 kernels per step; capturable in a CUDA graph after
+ * a first call with n_steps = 0 has sized the context's buffers).
  *   positions : device float [total][3], updated in place
  *   conv, kT  : energy = conv * V; kT > 0 in the same unit
  *   sigma     : displacement standard deviation per coordinate
  *   seed      : generator key.  Proposal t of chain c depends only on
  *               (seed, c, t): Philox4x32-10 counters (t, c, 0/1)
- *   sraw, energy : the state from pyiid_mh_init (updated)
+ *   state, energy : from pyiid_mh_init (updated)
  *   counter   : device uint64 [n_configs], proposals made so far per chain
  *               (start at 0; advanced by one per step)
  *   accepted  : device int64  [n_configs], incremented on acceptance
@@ -243,20 +252,20 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
  *               log u, V', accepted (0/1), V before the step
  * A proposal that makes two atoms coincide, or any NaN potential, is
  * rejected.  Chains with fewer than two atoms never move. */
+size_t pyiid_mh_state_size(int n_configs, int n_bins);
 int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
                   const int32_t *species, const int32_t *offsets,
                   int n_configs, const float *scatter, int n_species,
                   int n_bins, double qstep, double rstep, const double *rgrid,
                   int n_r, double qmin, const double *gobs, int potential,
-                  double *sraw, double *energy);
+                  double *state, double *energy);
 int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
                    const int32_t *offsets, int n_configs, const float *scatter,
                    int n_species, int n_bins, double qstep, double rstep,
-                   const double *rgrid, int n_r, double qmin,
-                   const double *gobs, int potential, double conv, double kT,
-                   float sigma, uint64_t seed, int n_steps, double *sraw,
-                   double *energy, uint64_t *counter, int64_t *accepted,
-                   double *trace);
+                   const double *rgrid, int n_r, double qmin, int potential,
+                   double conv, double kT, float sigma, uint64_t seed,
+                   int n_steps, double *state, double *energy,
+                   uint64_t *counter, int64_t *accepted, double *trace);
 
 /* F(Q) without device allocation.
  *

@@ -48,12 +48,13 @@ _SIGNATURES = {
     'pyiid_batch_potential_grad': (_c_int, [
         _vp, _vp, _i32p, _i32p, _c_int, _f32p, _c_int, _c_int, _c_dbl,
         _c_dbl, _f64p, _c_int, _c_dbl, _vp, _c_int, _vp, _vp, _vp, _vp]),
+    'pyiid_mh_state_size': (ctypes.c_size_t, [_c_int, _c_int]),
     'pyiid_mh_init': (_c_int, [
         _vp, _vp, _i32p, _i32p, _c_int, _f32p, _c_int, _c_int, _c_dbl,
         _c_dbl, _f64p, _c_int, _c_dbl, _vp, _c_int, _vp, _vp]),
     'pyiid_mh_steps': (_c_int, [
         _vp, _vp, _i32p, _i32p, _c_int, _f32p, _c_int, _c_int, _c_dbl,
-        _c_dbl, _f64p, _c_int, _c_dbl, _vp, _c_int, _c_dbl, _c_dbl,
+        _c_dbl, _f64p, _c_int, _c_dbl, _c_int, _c_dbl, _c_dbl,
         ctypes.c_float, ctypes.c_uint64, _c_int, _vp, _vp, _vp, _vp, _vp]),
     'pyiid_fq_noalloc': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
                                   _c_int, _c_dbl, _c_int, _vp]),

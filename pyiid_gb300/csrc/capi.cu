@@ -154,7 +154,16 @@ struct TMatrix {
   uint64_t key = 0;
   int n_bins = 0, n_r = 0, kmin = 0;
   float *d_T = nullptr;
+  // Gram matrix T T^T (single-atom moves), built on first use
+  double *d_M64 = nullptr;
+  float *d_M32 = nullptr;
 };
+
+void free_tmatrix(TMatrix *M) {
+  cudaFree(M->d_T);
+  cudaFree(M->d_M64);
+  cudaFree(M->d_M32);
+}
 
 struct NaTable {
   uint64_t key = 0;
@@ -517,7 +526,7 @@ int get_tmatrix(pyiid_ctx *ctx, int n_bins, double qstep, double rstep,
   TRY(upload(ctx, &M->d_T, T));
   ctx->tmats.insert(ctx->tmats.begin(), std::move(M));
   while (ctx->tmats.size() > 4) {
-    cudaFree(ctx->tmats.back()->d_T);
+    free_tmatrix(ctx->tmats.back().get());
     ctx->tmats.pop_back();
   }
   *out = ctx->tmats[0].get();
@@ -547,6 +556,9 @@ int set_attrs(pyiid_ctx *ctx) {
   CUDA_TRY(ctx, cudaFuncSetAttribute(adjoint_kernel<kAdjRS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      160 * 1024));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(move_gram_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     200 * 1024));
   ctx->attrs_set = true;
   return PYIID_OK;
 }
@@ -673,7 +685,7 @@ int pyiid_destroy(pyiid_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (auto &kv : ctx->bufs) cudaFree(kv.second.p);
   for (auto &L : ctx->layouts) free_layout(L.get());
-  for (auto &T : ctx->tmats) cudaFree(T->d_T);
+  for (auto &T : ctx->tmats) free_tmatrix(T.get());
   for (auto &N : ctx->nas) cudaFree(N->d_na);
   delete ctx;
   return PYIID_OK;
@@ -963,12 +975,30 @@ static int mh_prepare(pyiid_ctx *ctx, const int32_t *species,
   return PYIID_OK;
 }
 
+// Gram matrix of a transform (built once per T on the context stream).
+static int get_gram(pyiid_ctx *ctx, TMatrix *T) {
+  if (T->d_M64) return PYIID_OK;
+  const size_t kk = (size_t)T->n_bins * T->n_bins;
+  CUDA_TRY(ctx, cudaMalloc(&T->d_M64, kk * sizeof(double)));
+  CUDA_TRY(ctx, cudaMalloc(&T->d_M32, kk * sizeof(float)));
+  dim3 g((T->n_bins + 31) / 32, (T->n_bins + 31) / 32);
+  gram_matrix_kernel<<<g, dim3(32, 8), 0, ctx->stream>>>(
+      T->d_T, T->n_bins, T->n_r, T->d_M64, T->d_M32);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+size_t pyiid_mh_state_size(int n_configs, int n_bins) {
+  if (n_configs < 0 || n_bins < 0) return 0;
+  return mh_state_doubles(n_configs, n_bins);
+}
+
 int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
                   const int32_t *species, const int32_t *offsets,
                   int n_configs, const float *scatter, int n_species,
                   int n_bins, double qstep, double rstep, const double *rgrid,
                   int n_r, double qmin, const double *gobs, int potential,
-                  double *sraw, double *energy) {
+                  double *state, double *energy) {
   Layout *L;
   float *d_ftab;
   double *d_na;
@@ -976,20 +1006,22 @@ int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
   TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
                  qstep, rstep, rgrid, n_r, qmin, potential, &L, &d_ftab, &d_na,
                  &T));
-  void *p;
-  TRY(ensure(ctx, "mh_fq", (size_t)n_configs * n_bins * sizeof(float), &p));
-  float *d_fq = static_cast<float *>(p);
-  TRY(ensure(ctx, "mh_gcalc", (size_t)n_configs * n_r * sizeof(double), &p));
-  double *d_gc = static_cast<double *>(p);
-  TRY(run_fq(ctx, L, positions, d_ftab, d_na, n_bins, qstep, T->kmin, d_fq,
-             sraw));
-  dim3 gp((n_r + 255) / 256, n_configs);
-  pdf_kernel<<<gp, 256, n_bins * sizeof(float), ctx->stream>>>(
-      d_fq, T->d_T, n_bins, n_r, T->kmin, d_gc);
+  if (n_bins - T->kmin > 6400)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "single-atom moves support at most 6400 bins above qmin");
+  TRY(get_gram(ctx, T));
+  const MhState st = mh_state(state, n_configs, n_bins);
+  CUDA_TRY(ctx, cudaMemsetAsync(state, 0,
+                                mh_state_doubles(n_configs, n_bins) *
+                                    sizeof(double),
+                                ctx->stream));
+  TRY(run_fq(ctx, L, positions, d_ftab, d_na, n_bins, qstep, T->kmin, st.F,
+             st.S));
+  mh_gobs_kernel<<<n_bins + 1, 256, 0, ctx->stream>>>(T->d_T, gobs, n_bins,
+                                                      n_r, st);
   LAUNCH_CHECK(ctx);
-  potential_kernel<<<n_configs, 256, 0, ctx->stream>>>(gobs, d_gc, n_r,
-                                                       potential, energy,
-                                                       nullptr);
+  mh_init_kernel<<<n_configs, 256, 0, ctx->stream>>>(
+      T->d_M64, st, n_configs, n_bins, potential, energy);
   LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }
@@ -997,11 +1029,10 @@ int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
 int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
                    const int32_t *offsets, int n_configs, const float *scatter,
                    int n_species, int n_bins, double qstep, double rstep,
-                   const double *rgrid, int n_r, double qmin,
-                   const double *gobs, int potential, double conv, double kT,
-                   float sigma, uint64_t seed, int n_steps, double *sraw,
-                   double *energy, uint64_t *counter, int64_t *accepted,
-                   double *trace) {
+                   const double *rgrid, int n_r, double qmin, int potential,
+                   double conv, double kT, float sigma, uint64_t seed,
+                   int n_steps, double *state, double *energy,
+                   uint64_t *counter, int64_t *accepted, double *trace) {
   if (!(kT > 0) || !std::isfinite(kT))
     return fail(ctx, PYIID_ERR_INVALID_ARG, "kT must be a positive number");
   if (!std::isfinite(conv))
@@ -1016,53 +1047,61 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
   TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
                  qstep, rstep, rgrid, n_r, qmin, potential, &L, &d_ftab, &d_na,
                  &T));
-  const int n_mi = (int)L->mitems.size();
+  if (!T->d_M64)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "pyiid_mh_init must be called first for this grid");
   const int kmin = T->kmin;
+  const int nkk = n_bins - kmin;
+  if (nkk < 1 || nkk > 6400)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "single-atom moves need 1 to 6400 bins above qmin");
+  const size_t gram_smem = (size_t)kGramCH * nkk * sizeof(float);
+  const int n_mi = (int)L->mitems.size();
   const int kb0 = kmin & ~1;
+  const MhState st = mh_state(state, n_configs, n_bins);
+  const int n_cg = (n_configs + kGramCH - 1) / kGramCH;
   void *p;
-  TRY(ensure(ctx, "mh_fq", (size_t)n_configs * n_bins * sizeof(float), &p));
-  float *d_fq = static_cast<float *>(p);
-  TRY(ensure(ctx, "mh_gcalc", (size_t)n_configs * n_r * sizeof(double), &p));
-  double *d_gc = static_cast<double *>(p);
-  TRY(ensure(ctx, "mh_ds", (size_t)n_configs * n_bins * sizeof(double), &p));
-  double *d_ds = static_cast<double *>(p);
   TRY(ensure(ctx, "mh_prop", (size_t)n_configs * sizeof(MoveProposal), &p));
   MoveProposal *d_prop = static_cast<MoveProposal *>(p);
   TRY(ensure(ctx, "mh_partial",
-             (size_t)std::max(n_mi, 1) * n_bins * sizeof(double), &p));
-  double *d_part = static_cast<double *>(p);
+             (size_t)std::max(n_mi, 1) * n_bins * sizeof(float), &p));
+  float *d_part = static_cast<float *>(p);
+  TRY(ensure(ctx, "mh_done", (size_t)(n_configs + n_cg) * sizeof(int), &p));
+  int *d_done = static_cast<int *>(p);
+  const int n_rb = (nkk + kGramRB - 1) / kGramRB;
+  TRY(ensure(ctx, "mh_gpart", (size_t)n_rb * n_configs * 2 * sizeof(double),
+             &p));
+  double *d_gpart = static_cast<double *>(p);
+  if (n_steps == 0) return PYIID_OK;
+  CUDA_TRY(ctx, cudaMemsetAsync(d_done, 0,
+                                (size_t)(n_configs + n_cg) * sizeof(int),
+                                ctx->stream));
   // chunks of kMoveL bins; at most 16 chunks per CTA (>= 16 atom groups)
   const int chunks_total = std::max(1, (n_bins - kb0 + kMoveL - 1) / kMoveL);
   const int n_cb = (chunks_total + 15) / 16;
   const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
   const int n_groups = kBlock / n_chunks;
   const size_t smem = 4 * kMoveTiles * kTile * sizeof(float4) +
-                      (size_t)n_groups * n_chunks * kMoveL * sizeof(float);
+                      (size_t)kMoveL * (kBlock + 1) * sizeof(float);
   float dq_hi, dq_lo;
   split_double(qstep, dq_hi, dq_lo);
   const uint32_t seed_lo = (uint32_t)seed, seed_hi = (uint32_t)(seed >> 32);
+  const double beta = conv / kT;
+  dim3 gg(n_rb, n_cg);
   for (int step = 0; step < n_steps; ++step) {
     if (n_mi > 0) {
       dim3 g1(n_mi, n_cb);
       move_delta_kernel<<<g1, kBlock, smem, ctx->stream>>>(
           positions, L->d_perm, L->d_tiles, L->d_mitems, L->d_mitem_begin,
-          L->d_offsets, reinterpret_cast<const unsigned long long *>(counter),
-          seed_lo, seed_hi, sigma, dq_hi, dq_lo, kb0, n_chunks, n_groups,
-          n_bins, d_prop, d_part);
+          L->d_offsets, L->d_species,
+          reinterpret_cast<const unsigned long long *>(counter), seed_lo,
+          seed_hi, sigma, dq_hi, dq_lo, kb0, kmin, n_chunks, n_groups, n_bins,
+          d_ftab, d_na, st, n_configs, d_prop, d_part, d_done);
       LAUNCH_CHECK(ctx);
     }
-    dim3 g2((n_bins + 127) / 128, n_configs);
-    move_fq_kernel<<<g2, 128, 0, ctx->stream>>>(
-        d_part, L->d_mitems, L->d_mitem_begin, L->d_offsets, L->d_species,
-        d_prop, d_ftab, d_na, sraw, n_bins, kmin, d_fq, d_ds);
-    LAUNCH_CHECK(ctx);
-    dim3 gp((n_r + 255) / 256, n_configs);
-    pdf_kernel<<<gp, 256, n_bins * sizeof(float), ctx->stream>>>(
-        d_fq, T->d_T, n_bins, n_r, kmin, d_gc);
-    LAUNCH_CHECK(ctx);
-    mh_accept_kernel<<<n_configs, 256, 0, ctx->stream>>>(
-        positions, L->d_offsets, d_prop, gobs, d_gc, n_r, potential, conv, kT,
-        d_ds, sraw, n_bins, energy,
+    move_gram_kernel<<<gg, 256, gram_smem, ctx->stream>>>(
+        T->d_M32, L->d_offsets, d_prop, st, n_configs, n_bins, kmin,
+        potential, beta, d_gpart, d_done + n_configs, positions, energy,
         reinterpret_cast<unsigned long long *>(counter),
         reinterpret_cast<long long *>(accepted),
         trace ? trace + (size_t)step * n_configs * 8 : nullptr);

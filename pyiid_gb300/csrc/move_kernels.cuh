@@ -4,16 +4,30 @@
 // Moving atom a from x to x' changes only the N-1 pair terms that involve a:
 //   S'_k = S_k + f_sa(Q_k) sum_{j != a} f_sj(Q_k) [w(|x' - x_j|) - w(|x - x_j|)],
 //   w(r) = sin(Q_k r) / r,
-// so a proposal costs 2 (N-1) K sinusoid terms instead of N(N-1)/2 K.  The
-// raw Debye sums S_k of every chain are kept on the device in FP64; a step is
-//   move_delta_kernel  (pair terms of the moved atom, old and new position)
-//   move_fq_kernel     (F'_k = 2 nan_to_num(float(S_k + dS_k) / float(na_k)))
-//   pdf_kernel         (G'(r) = sum_k F'_k T[k][r])
-//   mh_accept_kernel   (potential of G', Metropolis test, state update)
+// so a proposal costs 2 (N-1) K sinusoid terms instead of N(N-1)/2 K.
+//
+// The potential needs G only through three scalars.  With G = T^T F (the
+// transform of the reference as a K x R matrix T), v = T gobs and the Gram
+// matrix M = T T^T (K x K, symmetric):
+//   G.gobs = F.v = u,   G.G = F^T M F = q,   |gobs - s G|^2 = gobs.gobs - 2 s u + s^2 q.
+// Each chain keeps S (FP64), F (the float F the reference transforms), u and
+// q on the device; a proposal F' = F + dF gives
+//   u' = u + dF.v,   q' = q + dF^T M (F + F'),
+// which costs K^2 instead of K R per chain and is accurate because only the
+// small increments carry FP32 rounding.  S and F are double-buffered per
+// chain: a step writes the proposal's S' and F' into the chain's spare
+// buffer and an acceptance flips the chain's buffer index.  A step is
+//   move_delta_kernel  pair terms of the moved atom (old and new position);
+//                      the last CTA of each chain forms dS, S' and F'
+//   move_gram_kernel   dF.v and dF^T M (F + F') for 8 chains per CTA; the
+//                      last CTA of each 8 chains sums them, evaluates the
+//                      potential and applies the Metropolis test
 // with no host round trip, so any number of steps can be enqueued at once or
 // captured in a CUDA graph.  Proposals come from a counter-based generator
 // (Philox4x32-10) keyed by the caller's seed and counted per chain, so a run
 // is reproducible and independent of how steps are batched into calls.
+// FP64 is used only where values persist or are summed across threads: FP64
+// throughput on this part is a small fraction of FP32.
 #pragma once
 
 #include "debye_kernels.cuh"
@@ -84,16 +98,56 @@ __device__ __forceinline__ MoveProposal make_proposal(uint32_t seed_lo,
   return p;
 }
 
+// Chain state inside the caller's state buffer (doubles):
+//   v [K], goo, 0, S [2][B][K], (u, q) [B], F [2][B][K] as floats,
+//   cur [B] as int32 (which of the two S / F buffers is the chain's state).
+struct MhState {
+  double *v, *goo, *S, *uq;
+  float *F;
+  int *cur;
+};
+
+__host__ __device__ inline size_t mh_state_doubles(int n_chains, int n_bins) {
+  const size_t bk = (size_t)n_chains * n_bins;
+  return (size_t)n_bins + 2 + 2 * bk + 2 * (size_t)n_chains + bk +
+         ((size_t)n_chains + 1) / 2;
+}
+
+__host__ __device__ inline MhState mh_state(double *base, int n_chains,
+                                            int n_bins) {
+  const size_t bk = (size_t)n_chains * n_bins;
+  MhState st;
+  st.v = base;
+  st.goo = base + n_bins;
+  st.S = base + n_bins + 2;
+  st.uq = st.S + 2 * bk;
+  st.F = reinterpret_cast<float *>(st.uq + 2 * (size_t)n_chains);
+  st.cur = reinterpret_cast<int *>(st.uq + 2 * (size_t)n_chains + bk);
+  return st;
+}
+
+// Row of chain b in buffer `which` of a [2][B][K] array.
+__device__ __forceinline__ size_t mh_row(int which, int b, int n_chains,
+                                         int n_bins) {
+  return ((size_t)which * n_chains + b) * n_bins;
+}
+
 // Pair terms of the moved atom.  One CTA per work item (chain, species,
 // tiles [t0, t1) of that species: consecutive sorted atoms) and bin block;
 // thread (chunk c, group g) accumulates bins [kbase, kbase + L) of
 //   sum_j w(|x' - x_j|) - w(|x - x_j|)
 // over the atoms j = g, g + n_groups, ... of the item, with the packed
 // even/odd recurrence of pair_math.cuh for both sinusoids.  The groups are
-// reduced through shared memory in FP64 and the CTA writes one partial row.
-// The moved atom itself contributes nothing (its records are zero).
+// reduced through shared memory and the CTA writes one partial row, already
+// weighted by its species' form factor (FP32: a partial is a difference of a
+// few hundred terms, far below S itself).  The moved atom itself contributes
+// nothing (its records are zero).  The last CTA of a chain to finish
+// (counted in done[chain], which it resets) then writes, for k >= kmin, into
+// the chain's spare buffer
+//   S'_k = S_k + f_sa(Q_k) sum_{items of the chain} partial[item][k]
+//   F'_k = 2 nan_to_num(float(S'_k) / float(na_k)).
 // Dynamic shared memory: 4 * kMoveTiles * 32 float4 records +
-// n_groups * n_chunks * L floats.
+// L * (blockDim + 1) floats.
 __global__ void __launch_bounds__(kBlock)
     move_delta_kernel(const float *__restrict__ pos,
                       const int *__restrict__ perm,
@@ -101,12 +155,16 @@ __global__ void __launch_bounds__(kBlock)
                       const int4 *__restrict__ mitems,
                       const int *__restrict__ mitem_begin,
                       const int *__restrict__ offsets,
+                      const int *__restrict__ species,
                       const unsigned long long *__restrict__ counter,
                       uint32_t seed_lo, uint32_t seed_hi, float sigma,
-                      float dq_hi, float dq_lo, int kb0, int n_chunks,
-                      int n_groups, int n_bins,
+                      float dq_hi, float dq_lo, int kb0, int kmin,
+                      int n_chunks, int n_groups, int n_bins,
+                      const float *__restrict__ ftab,
+                      const double *__restrict__ na,
+                      MhState st, int n_chains,
                       MoveProposal *__restrict__ prop_out,
-                      double *__restrict__ partial) {
+                      float *__restrict__ partial, int *__restrict__ done) {
   constexpr int L = kMoveL;
   constexpr int M = L / 2;
   constexpr int NJ = kMoveTiles * kTile;
@@ -115,9 +173,10 @@ __global__ void __launch_bounds__(kBlock)
   float4 *oB = oA + NJ;
   float4 *nA = oB + NJ;
   float4 *nB = nA + NJ;
-  float *red = reinterpret_cast<float *>(nB + NJ);
+  float *red = reinterpret_cast<float *>(nB + NJ);  // [j][thread], padded
+  const int rs = blockDim.x + 1;
   __shared__ float sx[6];
-  __shared__ int s_atom;
+  __shared__ int s_atom, s_last;
 
   const int4 it = mitems[blockIdx.x];  // (chain, species, t0, t1)
   const int chain = it.x;
@@ -144,22 +203,24 @@ __global__ void __launch_bounds__(kBlock)
   const int4 tl = tiles[it.w - 1];
   const int nj = tl.x + tl.y - s0;
   const int a = s_atom;
-  for (int q = tid; q < nj; q += blockDim.x) {
+  // records: w < nj the old position, nj <= w < 2 nj the new one
+  for (int w = tid; w < 2 * nj; w += blockDim.x) {
+    const bool nw = w >= nj;
+    const int q = nw ? w - nj : w;
     const int o = perm[s0 + q];
+    float4 *rA = nw ? nA : oA;
+    float4 *rB = nw ? nB : oB;
     if (o == a) {
-      oA[q] = nA[q] = make_float4(0.f, 0.f, 0.f, 1.f);
-      oB[q] = nB[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      rA[q] = make_float4(0.f, 0.f, 0.f, 1.f);
+      rB[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
       const float xj = pos[3 * o], yj = pos[3 * o + 1], zj = pos[3 * o + 2];
+      const float *xs = nw ? sx + 3 : sx;
       float dx, dy, dz;
-      const PairPhase2 po =
-          pair_phase2(sx[0], sx[1], sx[2], xj, yj, zj, dq_hi, dq_lo, dx, dy, dz);
-      oA[q] = make_float4(po.th_hi, po.th_lo, po.kappa, po.sigma2);
-      oB[q] = make_float4(po.ch * po.inv_r, po.sh * po.inv_r, po.inv_r, 0.f);
-      const PairPhase2 pn =
-          pair_phase2(sx[3], sx[4], sx[5], xj, yj, zj, dq_hi, dq_lo, dx, dy, dz);
-      nA[q] = make_float4(pn.th_hi, pn.th_lo, pn.kappa, pn.sigma2);
-      nB[q] = make_float4(pn.ch * pn.inv_r, pn.sh * pn.inv_r, pn.inv_r, 0.f);
+      const PairPhase2 p =
+          pair_phase2(xs[0], xs[1], xs[2], xj, yj, zj, dq_hi, dq_lo, dx, dy, dz);
+      rA[q] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
+      rB[q] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
     }
   }
   __syncthreads();
@@ -185,15 +246,14 @@ __global__ void __launch_bounds__(kBlock)
       float2 to = __fmul2_rn(f2(rb.z), s);
       float2 wo = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
       const float2 kpo = f2(ra.z), kmo = f2(-ra.z), sgo = f2(-ra.w);
+      // the difference of the two terms is formed first, so that it is
+      // exactly zero when the atom does not move
 #pragma unroll
       for (int m = 0; m < M; ++m) {
-        if (m & 1) {
-          acc[m] = __ffma2_rn(tn, sgn, acc[m]);
-          acc[m] = __ffma2_rn(to, sgo, acc[m]);
-        } else {
-          acc[m] = __fadd2_rn(acc[m], tn);
-          acc[m] = __ffma2_rn(to, f2(-1.f), acc[m]);
-        }
+        if (m & 1)
+          acc[m] = __fadd2_rn(acc[m], __ffma2_rn(to, sgo, __fmul2_rn(tn, sgn)));
+        else
+          acc[m] = __fadd2_rn(acc[m], __ffma2_rn(to, f2(-1.f), tn));
         if (m + 1 < M) {
           wn = __ffma2_rn(kmn, tn, wn);
           tn = __ffma2_rn(kpn, wn, tn);
@@ -202,118 +262,339 @@ __global__ void __launch_bounds__(kBlock)
         }
       }
     }
-    const int nk = n_chunks * L;
+  }
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-      red[g * nk + c * L + 2 * m] = acc[m].x;
-      red[g * nk + c * L + 2 * m + 1] = acc[m].y;
-    }
+  for (int m = 0; m < M; ++m) {
+    red[(2 * m) * rs + tid] = acc[m].x;
+    red[(2 * m + 1) * rs + tid] = acc[m].y;
   }
   __syncthreads();
   const int nk = n_chunks * L;
   const int kfirst = kb0 + blockIdx.y * nk;
-  double *out = partial + (size_t)blockIdx.x * n_bins;
+  float *out = partial + (size_t)blockIdx.x * n_bins;
+  const float *fs = ftab + (size_t)it.y * n_bins;
   for (int i = tid; i < nk; i += blockDim.x) {
     const int k = kfirst + i;
     if (k >= n_bins) continue;
-    double s = 0.0;
-    for (int gg = 0; gg < n_groups; ++gg) s += (double)red[gg * nk + i];
-    out[k] = s;
+    const int cc = i / L, j = i - cc * L;
+    float sum = 0.f;
+    for (int gg = 0; gg < n_groups; ++gg) sum += red[j * rs + gg * n_chunks + cc];
+    out[k] = fs[k] * sum;
+  }
+
+  // the last CTA of the chain forms dS and F'
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    const int total = (mitem_begin[chain + 1] - mitem_begin[chain]) * gridDim.y;
+    s_last = (atomicAdd(done + chain, 1) == total - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  if (tid == 0) done[chain] = 0;
+  const int sa = species[a];
+  const int i0 = mitem_begin[chain], i1 = mitem_begin[chain + 1];
+  const int cb = st.cur[chain];
+  const double *Sc = st.S + mh_row(cb, chain, n_chains, n_bins);
+  double *Sn = st.S + mh_row(1 - cb, chain, n_chains, n_bins);
+  float *Fn = st.F + mh_row(1 - cb, chain, n_chains, n_bins);
+  const double *nab = na + (size_t)chain * n_bins;
+  for (int k = kmin + tid; k < n_bins; k += blockDim.x) {
+    float d = 0.f;
+#pragma unroll 4
+    for (int i = i0; i < i1; ++i) d += __ldcg(partial + (size_t)i * n_bins + k);
+    const double sn = Sc[k] + (double)(ftab[sa * n_bins + k] * d);
+    Sn[k] = sn;
+    Fn[k] = fq_value(sn, nab[k]);
   }
 }
 
-// Proposed F' of every chain:
-//   dS_k = f_sa(Q_k) sum_{items of the chain} f_s(item)(Q_k) partial[item][k]
-//   F'_k = 2 nan_to_num(float(S_k + dS_k) / float(na_k))  for k >= kmin, else 0.
-// grid (ceil(n_bins / 128), n_chains)
-__global__ void move_fq_kernel(const double *__restrict__ partial,
-                               const int4 *__restrict__ mitems,
-                               const int *__restrict__ mitem_begin,
-                               const int *__restrict__ offsets,
-                               const int *__restrict__ species,
-                               const MoveProposal *__restrict__ prop,
-                               const float *__restrict__ ftab,
-                               const double *__restrict__ na,
-                               const double *__restrict__ sraw, int n_bins,
-                               int kmin, float *__restrict__ fq_prop,
-                               double *__restrict__ ds_out) {
-  const int b = blockIdx.y;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_bins) return;
-  const int base = offsets[b];
-  const int n = offsets[b + 1] - base;
-  double ds = 0.0;
-  float f = 0.f;
-  if (n >= 2 && k >= kmin) {
-    const int sa = species[base + prop[b].atom];
-    double d = 0.0;
-    for (int i = mitem_begin[b]; i < mitem_begin[b + 1]; ++i)
-      d += (double)ftab[mitems[i].y * n_bins + k] *
-           partial[(size_t)i * n_bins + k];
-    ds = (double)ftab[sa * n_bins + k] * d;
-    const size_t bk = (size_t)b * n_bins + k;
-    f = fq_value(sraw[bk] + ds, na[bk]);
-  }
-  fq_prop[(size_t)b * n_bins + k] = f;
-  ds_out[(size_t)b * n_bins + k] = ds;
+
+constexpr int kGramCH = 8;  // chains per CTA of move_gram_kernel
+constexpr int kGramRB = 8;  // rows of M per CTA (one per warp)
+
+// Potential from the Gram scalars (u = G.gobs, q = G.G, goo = gobs.gobs):
+// the reference's Rw / chi^2 with its scale rules, a = u / q;
+// a <= 0 -> Rw = 1 and chi^2 with scale 1; NaN stays NaN.
+__device__ __forceinline__ void potential_from_gram(double u, double q,
+                                                    double goo, int potential,
+                                                    double &value,
+                                                    double &scale) {
+  const double a = u / q;
+  const double s = (a <= 0.0) ? 1.0 : a;
+  double ee = goo - 2.0 * s * u + s * s * q;
+  if (ee < 0.0) ee = 0.0;
+  if (potential == 0)
+    value = (a <= 0.0) ? 1.0 : sqrt(ee / goo);
+  else
+    value = ee;
+  scale = s;
 }
 
-// Metropolis test and state update, one CTA per chain: the potential of the
-// proposed G'(r), accept when log u < -conv (V' - V) / kT (never for a NaN
-// potential), then on acceptance move the atom, add dS to S and store V'.
-// The chain's proposal counter advances either way.  Chains with fewer than
-// two atoms have no pair terms and never move.
+// dF.v and dF^T M (F + F') for 8 chains and 8 rows of M per CTA (one row k
+// per warp; each lane sums M[k][l] (F + F')_l over its columns for the 8
+// chains, scales by dF_k, and one recursive-halving shuffle per warp leaves
+// the 8 chain sums in lanes 0, 4, ..., 28): gpart[rb][b] = (du, dq).
+// The last CTA of the 8 chains (counted in done[blockIdx.y], which it
+// resets) sums the row blocks in a fixed order, one warp per chain:
+//   u' = u + du,  q' = q + dq,  potential V' from (u', q', goo);
+// accept when log u < -beta (V' - V), beta = conv / kT (never for a NaN
+// potential); on acceptance the atom moves, the chain's buffer index flips
+// and (u, q) = (u', q'), energy = (V', scale).  The chain's proposal
+// counter advances either way; chains with fewer than two atoms never move.
 // trace (optional) [n_chains][8]: atom, x', y', z', log u, V', accepted, V.
-__global__ void mh_accept_kernel(
-    float *__restrict__ pos, const int *__restrict__ offsets,
-    const MoveProposal *__restrict__ prop, const double *__restrict__ gobs,
-    const double *__restrict__ gcalc, int n_r, int potential, double conv,
-    double kT, const double *__restrict__ ds, double *__restrict__ sraw,
-    int n_bins, double *__restrict__ energy,
-    unsigned long long *__restrict__ counter,
-    long long *__restrict__ accepted, double *__restrict__ trace) {
-  __shared__ double scratch[32 * 3];
-  const int b = blockIdx.x;
-  const int base = offsets[b];
-  const int n = offsets[b + 1] - base;
-  if (n < 2) {
-    if (threadIdx.x == 0) {
-      counter[b] += 1ull;
-      if (trace)
-        for (int i = 0; i < 8; ++i) trace[(size_t)b * 8 + i] = 0.0;
+// grid (ceil((n_bins - kmin) / 8), ceil(n_chains / 8)), 256 threads,
+// dynamic shared memory 8 * (n_bins - kmin) floats.
+__global__ void __launch_bounds__(256)
+    move_gram_kernel(const float *__restrict__ M32,
+                     const int *__restrict__ offsets,
+                     const MoveProposal *__restrict__ prop, MhState st,
+                     int n_chains, int n_bins, int kmin, int potential,
+                     double beta, double *__restrict__ gpart,
+                     int *__restrict__ done, float *__restrict__ pos,
+                     double *__restrict__ energy,
+                     unsigned long long *__restrict__ counter,
+                     long long *__restrict__ accepted,
+                     double *__restrict__ trace) {
+  extern __shared__ float4 sum4[];
+  float *ssum = reinterpret_cast<float *>(sum4);  // [l][8]: F + F'
+  __shared__ float dfr[kGramRB][kGramCH];         // dF of this CTA's rows
+  __shared__ double red[8][kGramCH][2];
+  __shared__ int s_moves[kGramCH], s_cur[kGramCH], s_last;
+  const int nkk = n_bins - kmin;
+  const int b0 = blockIdx.y * kGramCH;
+  const int row0 = blockIdx.x * kGramRB;
+  if (threadIdx.x < kGramCH) {
+    const int b = b0 + threadIdx.x;
+    const bool mv = (b < n_chains) && (offsets[b + 1] - offsets[b] >= 2);
+    s_moves[threadIdx.x] = mv;
+    s_cur[threadIdx.x] = mv ? st.cur[b] : 0;
+  }
+  __syncthreads();
+#pragma unroll 4
+  for (int idx = threadIdx.x; idx < kGramCH * nkk; idx += blockDim.x) {
+    const int l = idx >> 3, c = idx & 7;
+    float fc = 0.f, fp = 0.f;
+    if (s_moves[c]) {
+      const int cb = s_cur[c];
+      const size_t k = (size_t)kmin + l;
+      fc = st.F[mh_row(cb, b0 + c, n_chains, n_bins) + k];
+      fp = st.F[mh_row(1 - cb, b0 + c, n_chains, n_bins) + k];
     }
+    ssum[idx] = fc + fp;
+    if (l >= row0 && l < row0 + kGramRB) dfr[l - row0][c] = fp - fc;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the chain whose sum this lane holds after the halving (lanes 4c' ...)
+  const int hc = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+  const int row = row0 + warp;
+  float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  double du = 0.0;
+  if (row < nkk) {
+    const float *mrow = M32 + (size_t)(kmin + row) * n_bins + kmin;
+#pragma unroll 4
+    for (int l = lane; l < nkk; l += 32) {
+      const float m = mrow[l];
+      const float4 f0 = sum4[2 * l], f1 = sum4[2 * l + 1];
+      v[0] = fmaf(m, f0.x, v[0]);
+      v[1] = fmaf(m, f0.y, v[1]);
+      v[2] = fmaf(m, f0.z, v[2]);
+      v[3] = fmaf(m, f0.w, v[3]);
+      v[4] = fmaf(m, f1.x, v[4]);
+      v[5] = fmaf(m, f1.y, v[5]);
+      v[6] = fmaf(m, f1.z, v[6]);
+      v[7] = fmaf(m, f1.w, v[7]);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] *= dfr[warp][c];
+    if (lane < kGramCH) du = (double)dfr[warp][lane] * st.v[kmin + row];
+  }
+  // recursive halving: 8 sums over 32 lanes in 4 + 2 + 1 + 1 + 1 shuffles
+  {
+    const bool up = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float give = up ? v[i] : v[i + 4];
+      const float keep = up ? v[i + 4] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+    }
+  }
+  {
+    const bool up = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const float give = up ? v[i] : v[i + 2];
+      const float keep = up ? v[i + 2] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+    }
+  }
+  {
+    const bool up = lane & 4;
+    const float give = up ? v[0] : v[1];
+    const float keep = up ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, give, 4);
+  }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  if ((lane & 3) == 0) red[warp][hc][1] = (double)v[0];
+  if (lane < kGramCH) red[warp][lane][0] = du;
+  __syncthreads();
+  if (threadIdx.x < kGramCH * 2) {
+    const int c = threadIdx.x >> 1, j = threadIdx.x & 1;
+    const int b = b0 + c;
+    if (b < n_chains) {
+      double sum = 0.0;
+      for (int w = 0; w < 8; ++w) sum += red[w][c][j];
+      gpart[((size_t)blockIdx.x * n_chains + b) * 2 + j] = sum;
+    }
+  }
+
+  // the last CTA of these chains: potential and Metropolis test
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0)
+    s_last = (atomicAdd(done + blockIdx.y, 1) == (int)gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  if (threadIdx.x == 0) done[blockIdx.y] = 0;
+  const int b = b0 + warp;  // one warp per chain
+  if (b >= n_chains) return;
+  double su = 0.0, sq = 0.0;
+  for (int rb = lane; rb < (int)gridDim.x; rb += 32) {
+    const double *g = gpart + ((size_t)rb * n_chains + b) * 2;
+    su += __ldcg(g);
+    sq += __ldcg(g + 1);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    su += __shfl_xor_sync(0xffffffffu, su, o);
+    sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  }
+  if (lane != 0) return;
+  double *tr = trace ? trace + (size_t)b * 8 : nullptr;
+  if (!s_moves[warp]) {
+    counter[b] += 1ull;
+    if (tr)
+      for (int i = 0; i < 8; ++i) tr[i] = 0.0;
     return;
   }
-  const PotentialValue pv = potential_value(gobs, gcalc + (size_t)b * n_r,
-                                            n_r, potential, scratch);
   const MoveProposal p = prop[b];
+  const double u1 = st.uq[2 * b] + su;
+  const double q1 = st.uq[2 * b + 1] + sq;
+  double value, scale;
+  potential_from_gram(u1, q1, *st.goo, potential, value, scale);
   const double e0 = energy[2 * b];
-  const bool acc = p.logu < -conv * (pv.value - e0) / kT;
-  if (acc)
-    for (int k = threadIdx.x; k < n_bins; k += blockDim.x)
-      sraw[(size_t)b * n_bins + k] += ds[(size_t)b * n_bins + k];
+  const bool acc = p.logu < -beta * (value - e0);
+  const int at = offsets[b] + p.atom;
+  float xn[3];
+  for (int i = 0; i < 3; ++i) xn[i] = __fadd_rn(pos[3 * at + i], p.d[i]);
+  if (acc) {
+    for (int i = 0; i < 3; ++i) pos[3 * at + i] = xn[i];
+    st.cur[b] = 1 - s_cur[warp];
+    st.uq[2 * b] = u1;
+    st.uq[2 * b + 1] = q1;
+    energy[2 * b] = value;
+    energy[2 * b + 1] = scale;
+    accepted[b] += 1;
+  }
+  if (tr) {
+    tr[0] = (double)p.atom;
+    tr[1] = xn[0];
+    tr[2] = xn[1];
+    tr[3] = xn[2];
+    tr[4] = p.logu;
+    tr[5] = value;
+    tr[6] = acc ? 1.0 : 0.0;
+    tr[7] = e0;
+  }
+  counter[b] += 1ull;
+}
+
+// ---------------------------------------------------------- state set-up
+// M64[k][l] = sum_i T[k][i] T[l][i] in FP64 (exact products of the float T),
+// 32 x 32 tiles, 32 x 8 threads with 4 rows each; M32 = float(M64).
+__global__ void gram_matrix_kernel(const float *__restrict__ T, int n_bins,
+                                   int n_r, double *__restrict__ M64,
+                                   float *__restrict__ M32) {
+  __shared__ float ta[32][33], tb[32][33];
+  const int k0 = blockIdx.y * 32, l0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i0 = 0; i0 < n_r; i0 += 32) {
+    for (int r = ty; r < 32; r += 8) {
+      const int i = i0 + tx;
+      ta[r][tx] = (k0 + r < n_bins && i < n_r) ? T[(size_t)(k0 + r) * n_r + i] : 0.f;
+      tb[r][tx] = (l0 + r < n_bins && i < n_r) ? T[(size_t)(l0 + r) * n_r + i] : 0.f;
+    }
+    __syncthreads();
+    for (int ii = 0; ii < 32; ++ii) {
+      const double bv = (double)tb[tx][ii];
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        acc[m] = fma((double)ta[ty + 8 * m][ii], bv, acc[m]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int k = k0 + ty + 8 * m, l = l0 + tx;
+    if (k < n_bins && l < n_bins) {
+      M64[(size_t)k * n_bins + l] = acc[m];
+      M32[(size_t)k * n_bins + l] = (float)acc[m];
+    }
+  }
+}
+
+// v[k] = sum_i T[k][i] gobs[i] (block k < n_bins) and goo = gobs.gobs
+// (block n_bins), FP64.
+__global__ void mh_gobs_kernel(const float *__restrict__ T,
+                               const double *__restrict__ gobs, int n_bins,
+                               int n_r, MhState st) {
+  __shared__ double scratch[32];
+  const int k = blockIdx.x;
+  double a[1] = {0.0};
+  if (k < n_bins) {
+    for (int i = threadIdx.x; i < n_r; i += blockDim.x)
+      a[0] += (double)T[(size_t)k * n_r + i] * gobs[i];
+  } else {
+    for (int i = threadIdx.x; i < n_r; i += blockDim.x) a[0] += gobs[i] * gobs[i];
+  }
+  block_sum<1>(a, scratch);
   if (threadIdx.x == 0) {
-    const int a = base + p.atom;
-    float xn[3];
-    for (int i = 0; i < 3; ++i) xn[i] = __fadd_rn(pos[3 * a + i], p.d[i]);
-    if (acc) {
-      for (int i = 0; i < 3; ++i) pos[3 * a + i] = xn[i];
-      energy[2 * b] = pv.value;
-      energy[2 * b + 1] = pv.scale;
-      accepted[b] += 1;
+    if (k < n_bins)
+      st.v[k] = a[0];
+    else {
+      *st.goo = a[0];
+      st.goo[1] = 0.0;
     }
-    if (trace) {
-      double *t = trace + (size_t)b * 8;
-      t[0] = (double)p.atom;
-      t[1] = xn[0];
-      t[2] = xn[1];
-      t[3] = xn[2];
-      t[4] = p.logu;
-      t[5] = pv.value;
-      t[6] = acc ? 1.0 : 0.0;
-      t[7] = e0;
-    }
-    counter[b] += 1ull;
+  }
+}
+
+// Per chain (one CTA): u = v.F, q = F^T M64 F (FP64) of buffer 0, cur = 0,
+// and the potential of the state into energy.
+__global__ void mh_init_kernel(const double *__restrict__ M64, MhState st,
+                               int n_chains, int n_bins, int potential,
+                               double *__restrict__ energy) {
+  __shared__ double scratch[32 * 2];
+  const int b = blockIdx.x;
+  const float *F = st.F + mh_row(0, b, n_chains, n_bins);
+  double a2[2] = {0.0, 0.0};
+  for (int k = threadIdx.x; k < n_bins; k += blockDim.x) {
+    const double *mr = M64 + (size_t)k * n_bins;
+    double yk = 0.0;
+    for (int l = 0; l < n_bins; ++l) yk = fma(mr[l], (double)F[l], yk);
+    a2[0] += st.v[k] * (double)F[k];
+    a2[1] += yk * (double)F[k];
+  }
+  block_sum<2>(a2, scratch);
+  if (threadIdx.x == 0) {
+    st.cur[b] = 0;
+    st.uq[2 * b] = a2[0];
+    st.uq[2 * b + 1] = a2[1];
+    double value, scale;
+    potential_from_gram(a2[0], a2[1], *st.goo, potential, value, scale);
+    energy[2 * b] = value;
+    energy[2 * b + 1] = scale;
   }
 }
 

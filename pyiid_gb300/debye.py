@@ -11,7 +11,8 @@ import torch
 from ._native import context, POTENTIALS, NativeError
 
 __all__ = ['fq', 'batch_fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
-           'batch_potential_grad', 'as_positions', 'mh_init', 'mh_steps']
+           'batch_potential_grad', 'as_positions', 'mh_init', 'mh_steps',
+           'mh_state_size', 'mh_views']
 
 _f32p = None
 
@@ -219,11 +220,36 @@ def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
     return out
 
 
+def mh_state_size(n_configs, n_bins):
+    """Doubles of the single-atom Metropolis chain state."""
+    from ._native import load
+    return int(load().pyiid_mh_state_size(int(n_configs), int(n_bins)))
+
+
+def mh_views(state):
+    """Views of the chain state buffer (layout of pyiid_mh_state_size):
+    v [K], goo, S2 / F2 [2, B, K] (both buffers), uq [B, 2], cur [B] (int32),
+    and S / F [B, K]: each chain's current buffer (gathered copies)."""
+    buf, b, k = state['buf'], state['n_configs'], state['n_bins']
+    bk = b * k
+    o = k + 2
+    s2 = buf[o:o + 2 * bk].view(2, b, k)
+    uq = buf[o + 2 * bk:o + 2 * bk + 2 * b].view(b, 2)
+    f_off = o + 2 * bk + 2 * b
+    f2 = buf[f_off:f_off + bk].view(torch.float32).view(2, b, k)
+    cur = buf[f_off + bk:].view(torch.int32)[:b]
+    idx = cur.long()
+    ar = torch.arange(b, device=buf.device)
+    return {'v': buf[:k], 'goo': buf[k], 'S2': s2, 'F2': f2, 'uq': uq,
+            'cur': cur, 'S': s2[idx, ar], 'F': f2[idx, ar]}
+
+
 def mh_init(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
             gobs, kind='rw', state=None):
     """Full exact evaluation that starts (or re-synchronises) single-atom
-    Metropolis chains: fills state['sraw'] [B, K] f64 (raw Debye sums on the
-    PDF grid) and state['energy'] [B, 2] f64 (potential, scale)."""
+    Metropolis chains.  Returns (and fills) the state dict: 'buf' (the
+    device chain state), 'energy' [B, 2] f64 (potential, scale),
+    'n_configs', 'n_bins'."""
     import ctypes
     pos = as_positions(positions)
     sp = _np(species, np.int32)
@@ -231,36 +257,38 @@ def mh_init(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
     tab = _np(scatter, np.float32)
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
+    k = tab.shape[1]
     dev = pos.device
     go = gobs.to(device=dev, dtype=torch.float64).contiguous()
     if state is None:
         state = {}
-    if state.get('sraw') is None:
-        state['sraw'] = torch.empty((b, tab.shape[1]), dtype=torch.float64,
-                                    device=dev)
+    if state.get('buf') is None or state.get('n_configs') != b or \
+            state.get('n_bins') != k:
+        state['buf'] = torch.zeros(mh_state_size(b, k), dtype=torch.float64,
+                                   device=dev)
+        state['n_configs'], state['n_bins'] = b, k
     if state.get('energy') is None:
         state['energy'] = torch.empty((b, 2), dtype=torch.float64, device=dev)
     ctx = context(dev.index)
     ctx.call('pyiid_mh_init', ctypes.c_void_p(pos.data_ptr()),
              _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
-             _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
+             _ptr(tab, ctypes.c_float), tab.shape[0], k,
              float(qstep), float(rstep), _ptr(rg, ctypes.c_double), len(rg),
              float(qmin), ctypes.c_void_p(go.data_ptr()), POTENTIALS[kind],
-             ctypes.c_void_p(state['sraw'].data_ptr()),
+             ctypes.c_void_p(state['buf'].data_ptr()),
              ctypes.c_void_p(state['energy'].data_ptr()))
     return state
 
 
 def mh_steps(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
-             gobs, state, n_steps, conv, kT, sigma, seed, kind='rw',
-             trace=None):
+             state, n_steps, conv, kT, sigma, seed, kind='rw', trace=None):
     """Enqueue n_steps single-atom Metropolis steps of every chain.
 
-    positions [sum N, 3] f32 CUDA tensor, updated in place.  ``state`` holds
-    'sraw' and 'energy' (from mh_init), 'counter' (uint64 proposals per
-    chain, as int64 tensor) and 'accepted' (int64).  ``trace`` may be a
-    float64 CUDA tensor [n_steps, B, 8] receiving every proposal (atom,
-    x', y', z', log u, V', accepted, V)."""
+    positions [sum N, 3] f32 CUDA tensor, updated in place.  ``state`` is
+    the dict of mh_init; 'counter' (proposals per chain) and 'accepted'
+    (int64 tensors) are added if missing.  ``trace`` may be a float64 CUDA
+    tensor [n_steps, B, 8] receiving every proposal (atom, x', y', z',
+    log u, V', accepted, V)."""
     import ctypes
     pos = positions
     if not (isinstance(pos, torch.Tensor) and pos.is_cuda and
@@ -273,7 +301,8 @@ def mh_steps(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
     dev = pos.device
-    go = gobs.to(device=dev, dtype=torch.float64).contiguous()
+    if state.get('n_configs') != b or state.get('n_bins') != tab.shape[1]:
+        raise NativeError('state does not match the batch (call mh_init)')
     for key in ('counter', 'accepted'):
         if state.get(key) is None:
             state[key] = torch.zeros(b, dtype=torch.int64, device=dev)
@@ -286,10 +315,9 @@ def mh_steps(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
              _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
              _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
              float(qstep), float(rstep), _ptr(rg, ctypes.c_double), len(rg),
-             float(qmin), ctypes.c_void_p(go.data_ptr()), POTENTIALS[kind],
-             float(conv), float(kT), float(sigma),
-             int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_steps),
-             ctypes.c_void_p(state['sraw'].data_ptr()),
+             float(qmin), POTENTIALS[kind], float(conv), float(kT),
+             float(sigma), int(seed) & 0xFFFFFFFFFFFFFFFF, int(n_steps),
+             ctypes.c_void_p(state['buf'].data_ptr()),
              ctypes.c_void_p(state['energy'].data_ptr()),
              ctypes.c_void_p(state['counter'].data_ptr()),
              ctypes.c_void_p(state['accepted'].data_ptr()),

@@ -14,8 +14,8 @@
   captured once in a CUDA graph and replayed.
 * :class:`SingleAtomMC` -- single-atom Metropolis chains whose exact energy
   change costs O(N K) per proposal (``pyiid_mh_steps``): the raw Debye sums
-  of every chain stay on the device and only the moved atom's pair terms
-  are recomputed.
+  and the Gram form of the potential of every chain stay on the device and
+  only the moved atom's pair terms are recomputed.
 
 Units are ASE's: Angstrom, eV, amu; time unit Angstrom * sqrt(amu / eV).
 The form factors of this API are species-correct (f evaluated at the PDF
@@ -291,9 +291,9 @@ class SingleAtomMC:
     def _enqueue(self, n, trace=None):
         p = self.pot
         debye.mh_steps(self.x, p.species, p.offsets, p.table, p.qstep,
-                       p.exp['rstep'], p.rgrid, p.exp['qmin'], p.gobs,
-                       self.state, n, p.conv, self.kT, self.sigma, self.seed,
-                       kind=p.kind, trace=trace)
+                       p.exp['rstep'], p.rgrid, p.exp['qmin'], self.state, n,
+                       p.conv, self.kT, self.sigma, self.seed, kind=p.kind,
+                       trace=trace)
 
     def _capture(self):
         self.graph = torch.cuda.CUDAGraph()
@@ -341,3 +341,7 @@ class SingleAtomMC:
 
     def positions(self):
         return self.x
+
+    def sums(self):
+        """Running raw Debye sums S [B, K] (FP64, PDF grid)."""
+        return debye.mh_views(self.state)['S']

@@ -94,7 +94,7 @@ def test_trace_matches_oracle_step_by_step():
     e = mc.state['energy'][:, 0].cpu().numpy()
     for c in (0, 1, 4):
         assert abs(e[c] - v[c]) <= 1e-5 * v[c]
-    sr = mc.state['sraw'].cpu().numpy()
+    sr = mc.sums().cpu().numpy()
     kmin = int(np.ceil(EXP['qmin'] / pot.qstep))
     for c in (0, 1, 4):
         o0, o1 = pot.offsets[c], pot.offsets[c + 1]
@@ -115,13 +115,18 @@ def test_zero_displacement_is_always_accepted_and_exact():
     pot, x0, exp, gobs = make_potential([50, 33], alloy=True, seed=3)
     mc = SingleAtomMC(pot, x0, temperature=300, sigma=0.0, seed=1,
                       resync_every=None)
+    from pyiid_gb300 import debye
     e0 = mc.state['energy'].clone()
-    s0 = mc.state['sraw'].clone()
-    mc.step(20)
-    assert np.all(mc.state['accepted'].cpu().numpy() == 20)
+    v0 = {k: debye.mh_views(mc.state)[k].clone() for k in ('S', 'F', 'uq')}
+    mc.step(21)
+    assert np.all(mc.state['accepted'].cpu().numpy() == 21)
     assert np.array_equal(mc.positions().cpu().numpy(), x0)
     assert bool((mc.state['energy'] == e0).all())
-    assert bool((mc.state['sraw'] == s0).all())
+    v1 = debye.mh_views(mc.state)
+    for k, t in v0.items():
+        assert bool((v1[k] == t).all()), k
+    # an odd number of acceptances leaves the chains on the second buffer
+    assert bool((v1['cur'] == 1).all())
 
 
 def test_graph_replay_equals_eager():
@@ -154,8 +159,12 @@ def test_running_sums_do_not_drift():
     fresh = debye.mh_init(mc.x, pot.species, pot.offsets, pot.table,
                           pot.qstep, pot.exp['rstep'], pot.rgrid,
                           pot.exp['qmin'], pot.gobs, state={})
-    s_run = mc.state['sraw'].cpu().numpy()
-    s_new = fresh['sraw'].cpu().numpy()
+    s_run = mc.sums().cpu().numpy()
+    s_new = debye.mh_views(fresh)['S'].cpu().numpy()
+    for key in ('F', 'uq'):
+        run = debye.mh_views(mc.state)[key].cpu().numpy()
+        new = debye.mh_views(fresh)[key].cpu().numpy()
+        assert np.abs(run - new).max() <= 1e-6 * np.abs(new).max(), key
     err = np.abs(s_run - s_new).max() / np.abs(s_new).max()
     assert err < 1e-6, err
     e_run = mc.state['energy'][:, 0].cpu().numpy()
@@ -211,12 +220,33 @@ def test_invalid_arguments_raise():
     st = debye.mh_init(x, pot.species, pot.offsets, pot.table, pot.qstep,
                        pot.exp['rstep'], pot.rgrid, pot.exp['qmin'], pot.gobs)
     args = (x, pot.species, pot.offsets, pot.table, pot.qstep,
-            pot.exp['rstep'], pot.rgrid, pot.exp['qmin'], pot.gobs, st, 1)
+            pot.exp['rstep'], pot.rgrid, pot.exp['qmin'], st, 1)
     with pytest.raises(NativeError, match='kT'):
         debye.mh_steps(*args, conv=1.0, kT=0.0, sigma=0.1, seed=0)
     with pytest.raises(NativeError, match='sigma'):
         debye.mh_steps(*args, conv=1.0, kT=1.0, sigma=-1.0, seed=0)
     with pytest.raises(NativeError, match='n_steps'):
         debye.mh_steps(x, pot.species, pot.offsets, pot.table, pot.qstep,
-                       pot.exp['rstep'], pot.rgrid, pot.exp['qmin'], pot.gobs,
-                       st, -1, conv=1.0, kT=1.0, sigma=0.1, seed=0)
+                       pot.exp['rstep'], pot.rgrid, pot.exp['qmin'], st, -1,
+                       conv=1.0, kT=1.0, sigma=0.1, seed=0)
+
+
+def test_gram_form_equals_transform_path():
+    """The potential of mh_init (Gram form, no G(r)) equals the fused
+    F -> G -> potential path of pyiid_batch_potential_grad."""
+    import torch
+    from pyiid_gb300 import debye
+    for kind in ('rw', 'chi_sq'):
+        pot, x0, exp, gobs = make_potential([40, 33, 57], alloy=True, seed=4)
+        pot.kind = kind
+        x = torch.as_tensor(x0, device='cuda')
+        st = debye.mh_init(x, pot.species, pot.offsets, pot.table, pot.qstep,
+                           pot.exp['rstep'], pot.rgrid, pot.exp['qmin'],
+                           pot.gobs, kind=kind)
+        e_ref, _ = pot.evaluate(x, want_grad=False)
+        e_ref = e_ref.cpu().numpy() / pot.conv
+        e = st['energy'][:, 0].cpu().numpy()
+        assert np.allclose(e, e_ref, rtol=1e-6, atol=0), (kind, e, e_ref)
+        sc = st['energy'][:, 1].cpu().numpy()
+        sc_ref = pot.buffers()['energy'][:, 1].cpu().numpy()
+        assert np.allclose(sc, sc_ref, rtol=1e-6, atol=0)
