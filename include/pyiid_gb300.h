@@ -233,7 +233,7 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
  * also bounds the drift of the running sums).  Arguments as
  * pyiid_batch_potential_grad (scatter on the PDF grid).  The first call for a
  * grid builds T T^T on the device (n_bins^2 doubles, kept with T); at most
- * 6400 bins above qmin.
+ * 3200 bins.
  *
  * pyiid_mh_steps: n_steps Metropolis steps of every chain, enqueued without
  * host synchronisation (3 kernels per step; capturable in a CUDA graph after

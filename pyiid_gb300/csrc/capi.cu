@@ -558,7 +558,7 @@ int set_attrs(pyiid_ctx *ctx) {
                                      160 * 1024));
   CUDA_TRY(ctx, cudaFuncSetAttribute(move_gram_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     200 * 1024));
+                                     2 * kGramCH * 3200 * (int)sizeof(float)));
   ctx->attrs_set = true;
   return PYIID_OK;
 }
@@ -1006,9 +1006,9 @@ int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
   TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
                  qstep, rstep, rgrid, n_r, qmin, potential, &L, &d_ftab, &d_na,
                  &T));
-  if (n_bins - T->kmin > 6400)
+  if (n_bins > 3200)
     return fail(ctx, PYIID_ERR_INVALID_ARG,
-                "single-atom moves support at most 6400 bins above qmin");
+                "single-atom moves support at most 3200 bins");
   TRY(get_gram(ctx, T));
   const MhState st = mh_state(state, n_configs, n_bins);
   CUDA_TRY(ctx, cudaMemsetAsync(state, 0,
@@ -1052,10 +1052,12 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
                 "pyiid_mh_init must be called first for this grid");
   const int kmin = T->kmin;
   const int nkk = n_bins - kmin;
-  if (nkk < 1 || nkk > 6400)
+  if (nkk < 1 || n_bins > 3200)
     return fail(ctx, PYIID_ERR_INVALID_ARG,
-                "single-atom moves need 1 to 6400 bins above qmin");
-  const size_t gram_smem = (size_t)kGramCH * nkk * sizeof(float);
+                "single-atom moves need 1 to 3200 bins (and at least one "
+                "above qmin)");
+  const int kp = (n_bins + 3) & ~3;  // row stride of the F + F', dF rows
+  const size_t gram_smem = 2 * (size_t)kGramCH * kp * sizeof(float);
   const int n_mi = (int)L->mitems.size();
   const int kb0 = kmin & ~1;
   const MhState st = mh_state(state, n_configs, n_bins);
@@ -1072,9 +1074,16 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
   TRY(ensure(ctx, "mh_gpart", (size_t)n_rb * n_configs * 2 * sizeof(double),
              &p));
   double *d_gpart = static_cast<double *>(p);
+  // F + F' and dF rows; rows of chains without pair terms stay zero
+  TRY(ensure(ctx, "mh_fsd", 2 * (size_t)n_configs * kp * sizeof(float), &p));
+  float *d_fsum = static_cast<float *>(p);
+  float *d_fdif = d_fsum + (size_t)n_configs * kp;
   if (n_steps == 0) return PYIID_OK;
   CUDA_TRY(ctx, cudaMemsetAsync(d_done, 0,
                                 (size_t)(n_configs + n_cg) * sizeof(int),
+                                ctx->stream));
+  CUDA_TRY(ctx, cudaMemsetAsync(d_fsum, 0,
+                                2 * (size_t)n_configs * kp * sizeof(float),
                                 ctx->stream));
   // chunks of kMoveL bins; at most 16 chunks per CTA (>= 16 atom groups)
   const int chunks_total = std::max(1, (n_bins - kb0 + kMoveL - 1) / kMoveL);
@@ -1096,11 +1105,13 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
           L->d_offsets, L->d_species,
           reinterpret_cast<const unsigned long long *>(counter), seed_lo,
           seed_hi, sigma, dq_hi, dq_lo, kb0, kmin, n_chunks, n_groups, n_bins,
-          d_ftab, d_na, st, n_configs, d_prop, d_part, d_done);
+          d_ftab, d_na, st, n_configs, kp, d_prop, d_part, d_done, d_fsum,
+          d_fdif);
       LAUNCH_CHECK(ctx);
     }
     move_gram_kernel<<<gg, 256, gram_smem, ctx->stream>>>(
-        T->d_M32, L->d_offsets, d_prop, st, n_configs, n_bins, kmin,
+        T->d_M32, d_fsum, d_fdif, kp, L->d_offsets, d_prop, st, n_configs,
+        n_bins, kmin,
         potential, beta, d_gpart, d_done + n_configs, positions, energy,
         reinterpret_cast<unsigned long long *>(counter),
         reinterpret_cast<long long *>(accepted),

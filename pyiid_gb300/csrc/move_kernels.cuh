@@ -145,7 +145,9 @@ __device__ __forceinline__ size_t mh_row(int which, int b, int n_chains,
 // (counted in done[chain], which it resets) then writes, for k >= kmin, into
 // the chain's spare buffer
 //   S'_k = S_k + f_sa(Q_k) sum_{items of the chain} partial[item][k]
-//   F'_k = 2 nan_to_num(float(S'_k) / float(na_k)).
+//   F'_k = 2 nan_to_num(float(S'_k) / float(na_k)),
+// and F_k + F'_k, F'_k - F_k into rows of stride kp (a multiple of 4) of
+// fsum and fdif.
 // Dynamic shared memory: 4 * kMoveTiles * 32 float4 records +
 // L * (blockDim + 1) floats.
 __global__ void __launch_bounds__(kBlock)
@@ -162,9 +164,10 @@ __global__ void __launch_bounds__(kBlock)
                       int n_chunks, int n_groups, int n_bins,
                       const float *__restrict__ ftab,
                       const double *__restrict__ na,
-                      MhState st, int n_chains,
+                      MhState st, int n_chains, int kp,
                       MoveProposal *__restrict__ prop_out,
-                      float *__restrict__ partial, int *__restrict__ done) {
+                      float *__restrict__ partial, int *__restrict__ done,
+                      float *__restrict__ fsum, float *__restrict__ fdif) {
   constexpr int L = kMoveL;
   constexpr int M = L / 2;
   constexpr int NJ = kMoveTiles * kTile;
@@ -296,16 +299,23 @@ __global__ void __launch_bounds__(kBlock)
   const int i0 = mitem_begin[chain], i1 = mitem_begin[chain + 1];
   const int cb = st.cur[chain];
   const double *Sc = st.S + mh_row(cb, chain, n_chains, n_bins);
+  const float *Fc = st.F + mh_row(cb, chain, n_chains, n_bins);
   double *Sn = st.S + mh_row(1 - cb, chain, n_chains, n_bins);
   float *Fn = st.F + mh_row(1 - cb, chain, n_chains, n_bins);
   const double *nab = na + (size_t)chain * n_bins;
+  float *fs_row = fsum + (size_t)chain * kp;
+  float *fd_row = fdif + (size_t)chain * kp;
   for (int k = kmin + tid; k < n_bins; k += blockDim.x) {
     float d = 0.f;
 #pragma unroll 4
     for (int i = i0; i < i1; ++i) d += __ldcg(partial + (size_t)i * n_bins + k);
     const double sn = Sc[k] + (double)(ftab[sa * n_bins + k] * d);
+    const float fn = fq_value(sn, nab[k]);
+    const float fc = Fc[k];
     Sn[k] = sn;
-    Fn[k] = fq_value(sn, nab[k]);
+    Fn[k] = fn;
+    fs_row[k] = fc + fn;
+    fd_row[k] = fn - fc;
   }
 }
 
@@ -335,6 +345,7 @@ __device__ __forceinline__ void potential_from_gram(double u, double q,
 // per warp; each lane sums M[k][l] (F + F')_l over its columns for the 8
 // chains, scales by dF_k, and one recursive-halving shuffle per warp leaves
 // the 8 chain sums in lanes 0, 4, ..., 28): gpart[rb][b] = (du, dq).
+// F + F' and dF come as rows of stride kp (zero where never written).
 // The last CTA of the 8 chains (counted in done[blockIdx.y], which it
 // resets) sums the row blocks in a fixed order, one warp per chain:
 //   u' = u + du,  q' = q + dq,  potential V' from (u', q', goo);
@@ -344,9 +355,13 @@ __device__ __forceinline__ void potential_from_gram(double u, double q,
 // counter advances either way; chains with fewer than two atoms never move.
 // trace (optional) [n_chains][8]: atom, x', y', z', log u, V', accepted, V.
 // grid (ceil((n_bins - kmin) / 8), ceil(n_chains / 8)), 256 threads,
-// dynamic shared memory 8 * (n_bins - kmin) floats.
+// dynamic shared memory 2 * 8 * kp floats.
+constexpr int kGramNL = 12;  // column loads in flight per lane and row
+
 __global__ void __launch_bounds__(256)
     move_gram_kernel(const float *__restrict__ M32,
+                     const float *__restrict__ fsum,
+                     const float *__restrict__ fdif, int kp,
                      const int *__restrict__ offsets,
                      const MoveProposal *__restrict__ prop, MhState st,
                      int n_chains, int n_bins, int kmin, int potential,
@@ -356,59 +371,69 @@ __global__ void __launch_bounds__(256)
                      unsigned long long *__restrict__ counter,
                      long long *__restrict__ accepted,
                      double *__restrict__ trace) {
-  extern __shared__ float4 sum4[];
-  float *ssum = reinterpret_cast<float *>(sum4);  // [l][8]: F + F'
-  __shared__ float dfr[kGramRB][kGramCH];         // dF of this CTA's rows
+  extern __shared__ float4 sm4[];
+  float *ssum = reinterpret_cast<float *>(sm4);  // [l][8]: F + F'
+  float *sdif = ssum + 8 * kp;                   // [l][8]: dF
   __shared__ double red[8][kGramCH][2];
-  __shared__ int s_moves[kGramCH], s_cur[kGramCH], s_last;
+  __shared__ int s_last;
   const int nkk = n_bins - kmin;
   const int b0 = blockIdx.y * kGramCH;
-  const int row0 = blockIdx.x * kGramRB;
-  if (threadIdx.x < kGramCH) {
-    const int b = b0 + threadIdx.x;
-    const bool mv = (b < n_chains) && (offsets[b + 1] - offsets[b] >= 2);
-    s_moves[threadIdx.x] = mv;
-    s_cur[threadIdx.x] = mv ? st.cur[b] : 0;
-  }
-  __syncthreads();
-#pragma unroll 4
-  for (int idx = threadIdx.x; idx < kGramCH * nkk; idx += blockDim.x) {
-    const int l = idx >> 3, c = idx & 7;
-    float fc = 0.f, fp = 0.f;
-    if (s_moves[c]) {
-      const int cb = s_cur[c];
-      const size_t k = (size_t)kmin + l;
-      fc = st.F[mh_row(cb, b0 + c, n_chains, n_bins) + k];
-      fp = st.F[mh_row(1 - cb, b0 + c, n_chains, n_bins) + k];
-    }
-    ssum[idx] = fc + fp;
-    if (l >= row0 && l < row0 + kGramRB) dfr[l - row0][c] = fp - fc;
-  }
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = blockIdx.x * kGramRB + warp;
+  // loads of the epilogue, issued first
+  const double vk = (row < nkk && lane < kGramCH) ? st.v[kmin + row] : 0.0;
+  const int kp4 = kp >> 2;
+#pragma unroll 3
+  for (int idx = threadIdx.x; idx < kGramCH * kp4; idx += blockDim.x) {
+    const int c = idx & 7, j = idx >> 3;
+    const int b = b0 + c;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
+    if (b < n_chains) {
+      a = reinterpret_cast<const float4 *>(fsum + (size_t)b * kp)[j];
+      d = reinterpret_cast<const float4 *>(fdif + (size_t)b * kp)[j];
+    }
+    const float av[4] = {a.x, a.y, a.z, a.w}, dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int k = 4 * j + i;
+      if (k >= kmin && k < n_bins) {  // shared row k - kmin
+        ssum[(k - kmin) * 8 + c] = av[i];
+        sdif[(k - kmin) * 8 + c] = dv[i];
+      }
+    }
+  }
+  __syncthreads();
   // the chain whose sum this lane holds after the halving (lanes 4c' ...)
   const int hc = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
-  const int row = row0 + warp;
   float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   double du = 0.0;
   if (row < nkk) {
     const float *mrow = M32 + (size_t)(kmin + row) * n_bins + kmin;
-#pragma unroll 4
-    for (int l = lane; l < nkk; l += 32) {
-      const float m = mrow[l];
-      const float4 f0 = sum4[2 * l], f1 = sum4[2 * l + 1];
-      v[0] = fmaf(m, f0.x, v[0]);
-      v[1] = fmaf(m, f0.y, v[1]);
-      v[2] = fmaf(m, f0.z, v[2]);
-      v[3] = fmaf(m, f0.w, v[3]);
-      v[4] = fmaf(m, f1.x, v[4]);
-      v[5] = fmaf(m, f1.y, v[5]);
-      v[6] = fmaf(m, f1.z, v[6]);
-      v[7] = fmaf(m, f1.w, v[7]);
+    for (int base = 0; base < nkk; base += 32 * kGramNL) {
+      float m[kGramNL];
+#pragma unroll
+      for (int i = 0; i < kGramNL; ++i) {
+        const int l = base + lane + 32 * i;
+        m[i] = l < nkk ? mrow[l] : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < kGramNL; ++i) {
+        const int l = base + lane + 32 * i;
+        if (l >= nkk) break;
+        const float4 f0 = sm4[2 * l], f1 = sm4[2 * l + 1];
+        v[0] = fmaf(m[i], f0.x, v[0]);
+        v[1] = fmaf(m[i], f0.y, v[1]);
+        v[2] = fmaf(m[i], f0.z, v[2]);
+        v[3] = fmaf(m[i], f0.w, v[3]);
+        v[4] = fmaf(m[i], f1.x, v[4]);
+        v[5] = fmaf(m[i], f1.y, v[5]);
+        v[6] = fmaf(m[i], f1.z, v[6]);
+        v[7] = fmaf(m[i], f1.w, v[7]);
+      }
     }
 #pragma unroll
-    for (int c = 0; c < 8; ++c) v[c] *= dfr[warp][c];
-    if (lane < kGramCH) du = (double)dfr[warp][lane] * st.v[kmin + row];
+    for (int c = 0; c < 8; ++c) v[c] *= sdif[row * 8 + c];
+    if (lane < kGramCH) du = (double)sdif[row * 8 + lane] * vk;
   }
   // recursive halving: 8 sums over 32 lanes in 4 + 2 + 1 + 1 + 1 shuffles
   {
@@ -460,6 +485,20 @@ __global__ void __launch_bounds__(256)
   if (threadIdx.x == 0) done[blockIdx.y] = 0;
   const int b = b0 + warp;  // one warp per chain
   if (b >= n_chains) return;
+  // per-chain values, loaded by lane 0 before the reduction
+  int o0 = 0, o1 = 0, cb = 0;
+  double u0 = 0.0, q0 = 0.0, e0 = 0.0, goo = 0.0;
+  MoveProposal p;
+  if (lane == 0) {
+    o0 = offsets[b];
+    o1 = offsets[b + 1];
+    cb = st.cur[b];
+    u0 = st.uq[2 * b];
+    q0 = st.uq[2 * b + 1];
+    e0 = energy[2 * b];
+    goo = *st.goo;
+    p = prop[b];
+  }
   double su = 0.0, sq = 0.0;
   for (int rb = lane; rb < (int)gridDim.x; rb += 32) {
     const double *g = gpart + ((size_t)rb * n_chains + b) * 2;
@@ -472,25 +511,23 @@ __global__ void __launch_bounds__(256)
   }
   if (lane != 0) return;
   double *tr = trace ? trace + (size_t)b * 8 : nullptr;
-  if (!s_moves[warp]) {
+  if (o1 - o0 < 2) {
     counter[b] += 1ull;
     if (tr)
       for (int i = 0; i < 8; ++i) tr[i] = 0.0;
     return;
   }
-  const MoveProposal p = prop[b];
-  const double u1 = st.uq[2 * b] + su;
-  const double q1 = st.uq[2 * b + 1] + sq;
-  double value, scale;
-  potential_from_gram(u1, q1, *st.goo, potential, value, scale);
-  const double e0 = energy[2 * b];
-  const bool acc = p.logu < -beta * (value - e0);
-  const int at = offsets[b] + p.atom;
+  const int at = o0 + p.atom;
   float xn[3];
   for (int i = 0; i < 3; ++i) xn[i] = __fadd_rn(pos[3 * at + i], p.d[i]);
+  const double u1 = u0 + su;
+  const double q1 = q0 + sq;
+  double value, scale;
+  potential_from_gram(u1, q1, goo, potential, value, scale);
+  const bool acc = p.logu < -beta * (value - e0);
   if (acc) {
     for (int i = 0; i < 3; ++i) pos[3 * at + i] = xn[i];
-    st.cur[b] = 1 - s_cur[warp];
+    st.cur[b] = 1 - cb;
     st.uq[2 * b] = u1;
     st.uq[2 * b + 1] = q1;
     energy[2 * b] = value;
