@@ -468,11 +468,32 @@ def run_delayed_acceptance(torch, iters=20):
     return out
 
 
-def run_incremental_mh(torch, pot, start, n_steps=8192):
+def setup_au1000_chains(torch, n_chains=64):
+    """The 64-chain single-atom workload: 1,000-atom fcc Au (a = 4.08 A),
+    gobs = G(r) of the undisplaced particle, chains started from seeded
+    0.05 A displacements, E = 100 Rw on the default PDF grid."""
+    from pyiid_gb300 import structures, debye
+    from pyiid_gb300.sampling import PDFPotential, experiment_grids
+    from pyiid_gb300.scatter_factors import species_tables
+    exp, qb, nb, rg = experiment_grids(None)
+    ref = structures.fcc_nearest(4.08, 1000).astype(np.float32)
+    sp, tab, _ = species_tables([79] * 1000, qb, nb)
+    gobs = debye.pdf(debye.fq(ref, sp, tab, qb), qb, exp['rstep'], rg,
+                     exp['qmin']).cpu().numpy()
+    start = np.stack([structures.displaced(ref, 0.05, 4 + c)
+                      for c in range(n_chains)])
+    pot = PDFPotential([79] * 1000, gobs, None, conv=100.0,
+                       n_configs=n_chains)
+    return pot, start
+
+
+def run_incremental_mh(torch, pot=None, start=None, n_steps=8192):
     """Exact single-atom Metropolis with O(N K) energy changes
     (pyiid_mh_steps), 64 proposals per chain per CUDA-graph replay, a full
     re-synchronisation every 4096 steps included in the timing."""
     from pyiid_gb300.sampling import SingleAtomMC
+    if pot is None:
+        pot, start = setup_au1000_chains(torch)
     mc = SingleAtomMC(pot, start.reshape(-1, 3), temperature=300, sigma=0.1,
                       seed=6, graph=True, steps_per_replay=64)
     mc.step(256)
@@ -561,6 +582,16 @@ def run_reference(args, rank, world):
     }
 
 
+WORKLOADS = {
+    'batched_fq_256_alloys': lambda torch, **kw: run_batched(torch, **kw),
+    'hmc_64_chains_au1000': lambda torch, **kw: run_hmc(torch, **kw),
+    'delayed_acceptance_au1000':
+        lambda torch, **kw: run_delayed_acceptance(torch, **kw),
+    'exact_incremental_mh':
+        lambda torch, **kw: run_incremental_mh(torch, **kw),
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -577,7 +608,21 @@ def main():
                     help='skip the batched and HMC secondary workloads')
     ap.add_argument('--no-tune', action='store_true',
                     help='use the default launch shapes (no autotuning)')
+    ap.add_argument('--only-workload', default=None,
+                    choices=sorted(WORKLOADS),
+                    help='run one secondary workload alone and print its '
+                         'result (for profiling)')
+    ap.add_argument('--workload-steps', type=int, default=None,
+                    help='steps of --only-workload exact_incremental_mh')
     args = ap.parse_args()
+    if args.only_workload:
+        import torch
+        fn = WORKLOADS[args.only_workload]
+        kw = {}
+        if args.workload_steps and args.only_workload == 'exact_incremental_mh':
+            kw['n_steps'] = args.workload_steps
+        print(json.dumps({args.only_workload: fn(torch, **kw)}))
+        return
     rank, world, local = dist_env()
     if args.impl == 'reference':
         line = run_reference(args, rank, world)

@@ -217,13 +217,16 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
  * del_atom call get_potential_energy on a copy; sim/hmc.py:66-92 mh_accept),
  * at O(N K) instead of O(N^2 K) per proposal.  The potential is formed
  * without G(r): with the transform G = T^T F, u = F.(T gobs) and
- * q = F^T (T T^T) F give G.gobs and G.G; the chain state keeps S, F, u and q,
- * and a proposal F' = F + dF updates u by dF.(T gobs) and q by
- * dF^T (T T^T) (F + F'), so that it costs K^2, not K R.
+ * q = F^T (T T^T) F give G.gobs and G.G, and ee = gobs.gobs - u^2 / q is
+ * |gobs - s G|^2 at the optimal scale; the chain state keeps S, F, u, q and
+ * ee, and a proposal F' = F + dF changes them by du = dF.(T gobs),
+ * dq = dF^T (T T^T) (F + F') and ee' - ee = -[(2 u du + du^2) q - u^2 dq] /
+ * (q (q + dq)), so that it costs K^2, not K R, and the acceptance test runs
+ * in FP32 on increments.
  *
  * state (device double [pyiid_mh_state_size(n_configs, n_bins)]):
- *   v [n_bins] (T gobs), gobs.gobs, 0, S [2][n_configs][n_bins],
- *   (u, q) [n_configs], F [2][n_configs][n_bins] as float32, then
+ *   v [n_bins] (T gobs), gobs.gobs, 1 / gobs.gobs, S [2][n_configs][n_bins],
+ *   (u, q, ee, 0) [n_configs], F [2][n_configs][n_bins] as float32, then
  *   cur [n_configs] as int32: chain c's state is S[cur[c]][c], F[cur[c]][c]
  *   (the other buffer holds the last proposal).
  *

@@ -59,7 +59,8 @@ def _unit_float(x):
 
 def proposal(seed, chain, step, n_atoms, sigma):
     """(atom, displacement float32 [3], log u) of proposal ``step`` of
-    ``chain`` (counters (step lo, step hi, chain, 0/1), key = seed)."""
+    ``chain`` (counters (step lo, step hi, chain, 0/1), key = seed); log u
+    is the float32 log of the float uniform of word 1 of the second block."""
     key = (seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
     slo, shi = step & 0xFFFFFFFF, (step >> 32) & 0xFFFFFFFF
     r0 = philox4x32_10([slo, shi, chain, 0], key)
@@ -73,8 +74,7 @@ def proposal(seed, chain, step, n_atoms, sigma):
     d = np.array([ra * np.cos(np.pi * np.float64(ang)),
                   ra * np.sin(np.pi * np.float64(ang)),
                   rb * np.cos(np.pi * np.float64(ang2))]) * np.float64(sigma)
-    m = ((int(r1[1]) << 32) | int(r1[2])) >> 11
-    logu = np.log((m + 0.5) * 2.0 ** -53)
+    logu = float(np.log(_unit_float(r1[1])))
     return atom, d, logu
 
 

@@ -1071,9 +1071,9 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
   TRY(ensure(ctx, "mh_done", (size_t)(n_configs + n_cg) * sizeof(int), &p));
   int *d_done = static_cast<int *>(p);
   const int n_rb = (nkk + kGramRB - 1) / kGramRB;
-  TRY(ensure(ctx, "mh_gpart", (size_t)n_rb * n_configs * 2 * sizeof(double),
+  TRY(ensure(ctx, "mh_gpart", (size_t)n_rb * n_configs * 2 * sizeof(float),
              &p));
-  double *d_gpart = static_cast<double *>(p);
+  float *d_gpart = static_cast<float *>(p);
   // F + F' and dF rows; rows of chains without pair terms stay zero
   TRY(ensure(ctx, "mh_fsd", 2 * (size_t)n_configs * kp * sizeof(float), &p));
   float *d_fsum = static_cast<float *>(p);

@@ -10,11 +10,13 @@
 // transform of the reference as a K x R matrix T), v = T gobs and the Gram
 // matrix M = T T^T (K x K, symmetric):
 //   G.gobs = F.v = u,   G.G = F^T M F = q,   |gobs - s G|^2 = gobs.gobs - 2 s u + s^2 q.
-// Each chain keeps S (FP64), F (the float F the reference transforms), u and
-// q on the device; a proposal F' = F + dF gives
-//   u' = u + dF.v,   q' = q + dF^T M (F + F'),
-// which costs K^2 instead of K R per chain and is accurate because only the
-// small increments carry FP32 rounding.  S and F are double-buffered per
+// Each chain keeps S (FP64), F (the float F the reference transforms), u, q
+// and ee = |gobs - s G|^2 at the optimal scale s = u / q; a proposal
+// F' = F + dF gives
+//   du = dF.v,   dq = dF^T M (F + F'),
+//   ee' - ee = -[(2 u du + du^2) q - u^2 dq] / (q (q + dq)),
+// which costs K^2 instead of K R per chain and is accurate in FP32 because
+// only small increments are formed (no cancellation of totals).  S and F are double-buffered per
 // chain: a step writes the proposal's S' and F' into the chain's spare
 // buffer and an acceptance flips the chain's buffer index.  A step is
 //   move_delta_kernel  pair terms of the moved atom (old and new position);
@@ -26,8 +28,10 @@
 // captured in a CUDA graph.  Proposals come from a counter-based generator
 // (Philox4x32-10) keyed by the caller's seed and counted per chain, so a run
 // is reproducible and independent of how steps are batched into calls.
-// FP64 is used only where values persist or are summed across threads: FP64
-// throughput on this part is a small fraction of FP32.
+// FP64 is used only for the persistent sums: on this part an FP64 FMA has a
+// latency of about 64 cycles (FP32: under 5), a division about 430 and a
+// square root about 670, and the FP64 pipe is shared by all warps of an SM,
+// so nothing on a step's critical path computes in FP64.
 #pragma once
 
 #include "debye_kernels.cuh"
@@ -72,7 +76,8 @@ __device__ __forceinline__ float unit_float(uint32_t x) {
 //   counter words (step lo, step hi, chain, 0/1), key (seed lo, seed hi);
 //   atom  = floor(r0.x * n / 2^32)
 //   d     = sigma * (n0, n1, n2), Box-Muller on (r0.y, r0.z) and (r0.w, r1.x)
-//   log u = log((53-bit integer of r1.y, r1.z + 1/2) / 2^53)
+//   log u = logf(u), u the float in (0, 1) of r1.y (FP32: a Metropolis test
+//           needs no finer u, and FP64 log costs about a microsecond here)
 __device__ __forceinline__ MoveProposal make_proposal(uint32_t seed_lo,
                                                       uint32_t seed_hi,
                                                       unsigned long long step,
@@ -93,14 +98,14 @@ __device__ __forceinline__ MoveProposal make_proposal(uint32_t seed_lo,
   const float rb = sqrtf(-2.0f * logf(unit_float(r0.w)));
   sincospif(2.0f * unit_float(r1.x), &s, &c);
   p.d[2] = sigma * (rb * c);
-  const uint64_t m = ((((uint64_t)r1.y) << 32) | r1.z) >> 11;
-  p.logu = log(((double)m + 0.5) * 1.1102230246251565e-16);  // 2^-53
+  p.logu = (double)logf(unit_float(r1.y));
   return p;
 }
 
 // Chain state inside the caller's state buffer (doubles):
-//   v [K], goo, 0, S [2][B][K], (u, q) [B], F [2][B][K] as floats,
-//   cur [B] as int32 (which of the two S / F buffers is the chain's state).
+//   v [K], goo, 1/goo, S [2][B][K], (u, q, ee, 0) [B], F [2][B][K] as
+//   floats, cur [B] as int32 (which of the two S / F buffers is the chain's
+//   state).
 struct MhState {
   double *v, *goo, *S, *uq;
   float *F;
@@ -109,7 +114,7 @@ struct MhState {
 
 __host__ __device__ inline size_t mh_state_doubles(int n_chains, int n_bins) {
   const size_t bk = (size_t)n_chains * n_bins;
-  return (size_t)n_bins + 2 + 2 * bk + 2 * (size_t)n_chains + bk +
+  return (size_t)n_bins + 2 + 2 * bk + 4 * (size_t)n_chains + bk +
          ((size_t)n_chains + 1) / 2;
 }
 
@@ -121,8 +126,8 @@ __host__ __device__ inline MhState mh_state(double *base, int n_chains,
   st.goo = base + n_bins;
   st.S = base + n_bins + 2;
   st.uq = st.S + 2 * bk;
-  st.F = reinterpret_cast<float *>(st.uq + 2 * (size_t)n_chains);
-  st.cur = reinterpret_cast<int *>(st.uq + 2 * (size_t)n_chains + bk);
+  st.F = reinterpret_cast<float *>(st.uq + 4 * (size_t)n_chains);
+  st.cur = reinterpret_cast<int *>(st.uq + 4 * (size_t)n_chains + bk);
   return st;
 }
 
@@ -171,6 +176,7 @@ __global__ void __launch_bounds__(kBlock)
   constexpr int L = kMoveL;
   constexpr int M = L / 2;
   constexpr int NJ = kMoveTiles * kTile;
+  static_assert(2 * NJ <= kBlock, "one record per thread");
   extern __shared__ float4 smem[];
   float4 *oA = smem;
   float4 *oB = oA + NJ;
@@ -184,6 +190,20 @@ __global__ void __launch_bounds__(kBlock)
   const int4 it = mitems[blockIdx.x];  // (chain, species, t0, t1)
   const int chain = it.x;
   const int tid = threadIdx.x;
+  const int s0 = tiles[it.z].x;
+  const int4 tl = tiles[it.w - 1];
+  const int nj = tl.x + tl.y - s0;
+  // the record atom of this thread (loaded while thread 0 forms the proposal)
+  const bool has_rec = tid < 2 * nj;
+  const int q_rec = tid < nj ? tid : tid - nj;
+  int o_rec = -1;
+  float xr = 0.f, yr = 0.f, zr = 0.f;
+  if (has_rec) {
+    o_rec = perm[s0 + q_rec];
+    xr = pos[3 * o_rec];
+    yr = pos[3 * o_rec + 1];
+    zr = pos[3 * o_rec + 2];
+  }
   if (tid == 0) {
     const int base = offsets[chain];
     const int n = offsets[chain + 1] - base;
@@ -202,28 +222,23 @@ __global__ void __launch_bounds__(kBlock)
     sx[5] = __fadd_rn(z, p.d[2]);
   }
   __syncthreads();
-  const int s0 = tiles[it.z].x;
-  const int4 tl = tiles[it.w - 1];
-  const int nj = tl.x + tl.y - s0;
   const int a = s_atom;
-  // records: w < nj the old position, nj <= w < 2 nj the new one
-  for (int w = tid; w < 2 * nj; w += blockDim.x) {
-    const bool nw = w >= nj;
-    const int q = nw ? w - nj : w;
-    const int o = perm[s0 + q];
+  // records: thread w < nj the old position, nj <= w < 2 nj the new one
+  // (2 nj <= blockDim.x: at most kMoveTiles * 32 atoms per item)
+  if (has_rec) {
+    const bool nw = tid >= nj;
     float4 *rA = nw ? nA : oA;
     float4 *rB = nw ? nB : oB;
-    if (o == a) {
-      rA[q] = make_float4(0.f, 0.f, 0.f, 1.f);
-      rB[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (o_rec == a) {
+      rA[q_rec] = make_float4(0.f, 0.f, 0.f, 1.f);
+      rB[q_rec] = make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
-      const float xj = pos[3 * o], yj = pos[3 * o + 1], zj = pos[3 * o + 2];
       const float *xs = nw ? sx + 3 : sx;
       float dx, dy, dz;
       const PairPhase2 p =
-          pair_phase2(xs[0], xs[1], xs[2], xj, yj, zj, dq_hi, dq_lo, dx, dy, dz);
-      rA[q] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
-      rB[q] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
+          pair_phase2(xs[0], xs[1], xs[2], xr, yr, zr, dq_hi, dq_lo, dx, dy, dz);
+      rA[q_rec] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
+      rB[q_rec] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
     }
   }
   __syncthreads();
@@ -323,35 +338,44 @@ __global__ void __launch_bounds__(kBlock)
 constexpr int kGramCH = 8;  // chains per CTA of move_gram_kernel
 constexpr int kGramRB = 8;  // rows of M per CTA (one per warp)
 
-// Potential from the Gram scalars (u = G.gobs, q = G.G, goo = gobs.gobs):
-// the reference's Rw / chi^2 with its scale rules, a = u / q;
-// a <= 0 -> Rw = 1 and chi^2 with scale 1; NaN stays NaN.
-__device__ __forceinline__ void potential_from_gram(double u, double q,
-                                                    double goo, int potential,
-                                                    double &value,
-                                                    double &scale) {
-  const double a = u / q;
-  const double s = (a <= 0.0) ? 1.0 : a;
-  double ee = goo - 2.0 * s * u + s * s * q;
-  if (ee < 0.0) ee = 0.0;
-  if (potential == 0)
-    value = (a <= 0.0) ? 1.0 : sqrt(ee / goo);
-  else
-    value = ee;
-  scale = s;
+// Potential of a state from its Gram scalars u = G.gobs, q = G.G and
+// ee = goo - u^2 / q (|gobs - s G|^2 at the optimal scale s = u / q):
+//   u / q > 0:  Rw = sqrt(ee / goo), chi^2 = ee, scale u / q;
+//   otherwise the reference's rules: Rw = 1, chi^2 = goo - 2 u + q (scale 1);
+//   NaN stays NaN.
+// The values are formed in FP32 from the FP64 state (the same expressions at
+// initialisation and in the step, so that an unchanged state keeps bitwise
+// the same potential).
+__device__ __forceinline__ void gram_value(double u, double q, double ee,
+                                           double goo, float inv_goo,
+                                           int potential, double &value,
+                                           double &scale) {
+  const float uf = (float)u, qf = (float)q;
+  if (uf > 0.f && qf > 0.f) {
+    const float ef = fmaxf((float)ee, 0.f);
+    value = (potential == 0) ? (double)sqrtf(ef * inv_goo) : (double)ef;
+    scale = (double)(uf / qf);
+  } else if (uf != uf || qf != qf || (qf == 0.f && uf == 0.f)) {
+    value = scale = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+  } else {
+    value = (potential == 0) ? 1.0 : goo - 2.0 * u + q;
+    scale = 1.0;
+  }
 }
 
 // dF.v and dF^T M (F + F') for 8 chains and 8 rows of M per CTA (one row k
 // per warp; each lane sums M[k][l] (F + F')_l over its columns for the 8
 // chains, scales by dF_k, and one recursive-halving shuffle per warp leaves
-// the 8 chain sums in lanes 0, 4, ..., 28): gpart[rb][b] = (du, dq).
+// the 8 chain sums in lanes 0, 4, ..., 28): gpart[rb][b] = (du, dq)
+// (FP32: these are small increments).
 // F + F' and dF come as rows of stride kp (zero where never written).
 // The last CTA of the 8 chains (counted in done[blockIdx.y], which it
-// resets) sums the row blocks in a fixed order, one warp per chain:
-//   u' = u + du,  q' = q + dq,  potential V' from (u', q', goo);
-// accept when log u < -beta (V' - V), beta = conv / kT (never for a NaN
+// resets) sums the row blocks in a fixed order, one warp per chain, and
+// forms ee' - ee from the increments (FP32; the FP64 expressions of the
+// reference's rules when a scale is not positive), V' and V' - V; it
+// accepts when log u < -beta (V' - V), beta = conv / kT (never for a NaN
 // potential); on acceptance the atom moves, the chain's buffer index flips
-// and (u, q) = (u', q'), energy = (V', scale).  The chain's proposal
+// and (u, q, ee) and energy = (V', scale) are updated.  The chain's proposal
 // counter advances either way; chains with fewer than two atoms never move.
 // trace (optional) [n_chains][8]: atom, x', y', z', log u, V', accepted, V.
 // grid (ceil((n_bins - kmin) / 8), ceil(n_chains / 8)), 256 threads,
@@ -365,7 +389,7 @@ __global__ void __launch_bounds__(256)
                      const int *__restrict__ offsets,
                      const MoveProposal *__restrict__ prop, MhState st,
                      int n_chains, int n_bins, int kmin, int potential,
-                     double beta, double *__restrict__ gpart,
+                     double beta, float *__restrict__ gpart,
                      int *__restrict__ done, float *__restrict__ pos,
                      double *__restrict__ energy,
                      unsigned long long *__restrict__ counter,
@@ -374,14 +398,14 @@ __global__ void __launch_bounds__(256)
   extern __shared__ float4 sm4[];
   float *ssum = reinterpret_cast<float *>(sm4);  // [l][8]: F + F'
   float *sdif = ssum + 8 * kp;                   // [l][8]: dF
-  __shared__ double red[8][kGramCH][2];
+  __shared__ float red[8][kGramCH][2];
   __shared__ int s_last;
   const int nkk = n_bins - kmin;
   const int b0 = blockIdx.y * kGramCH;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int row = blockIdx.x * kGramRB + warp;
   // loads of the epilogue, issued first
-  const double vk = (row < nkk && lane < kGramCH) ? st.v[kmin + row] : 0.0;
+  const float vk = (row < nkk && lane < kGramCH) ? (float)st.v[kmin + row] : 0.f;
   const int kp4 = kp >> 2;
 #pragma unroll 3
   for (int idx = threadIdx.x; idx < kGramCH * kp4; idx += blockDim.x) {
@@ -406,7 +430,7 @@ __global__ void __launch_bounds__(256)
   // the chain whose sum this lane holds after the halving (lanes 4c' ...)
   const int hc = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
   float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  double du = 0.0;
+  float du = 0.f;
   if (row < nkk) {
     const float *mrow = M32 + (size_t)(kmin + row) * n_bins + kmin;
     for (int base = 0; base < nkk; base += 32 * kGramNL) {
@@ -433,7 +457,7 @@ __global__ void __launch_bounds__(256)
     }
 #pragma unroll
     for (int c = 0; c < 8; ++c) v[c] *= sdif[row * 8 + c];
-    if (lane < kGramCH) du = (double)sdif[row * 8 + lane] * vk;
+    if (lane < kGramCH) du = sdif[row * 8 + lane] * vk;
   }
   // recursive halving: 8 sums over 32 lanes in 4 + 2 + 1 + 1 + 1 shuffles
   {
@@ -462,14 +486,14 @@ __global__ void __launch_bounds__(256)
   }
   v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
   v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-  if ((lane & 3) == 0) red[warp][hc][1] = (double)v[0];
+  if ((lane & 3) == 0) red[warp][hc][1] = v[0];
   if (lane < kGramCH) red[warp][lane][0] = du;
   __syncthreads();
   if (threadIdx.x < kGramCH * 2) {
     const int c = threadIdx.x >> 1, j = threadIdx.x & 1;
     const int b = b0 + c;
     if (b < n_chains) {
-      double sum = 0.0;
+      float sum = 0.f;
       for (int w = 0; w < 8; ++w) sum += red[w][c][j];
       gpart[((size_t)blockIdx.x * n_chains + b) * 2 + j] = sum;
     }
@@ -487,23 +511,27 @@ __global__ void __launch_bounds__(256)
   if (b >= n_chains) return;
   // per-chain values, loaded by lane 0 before the reduction
   int o0 = 0, o1 = 0, cb = 0;
-  double u0 = 0.0, q0 = 0.0, e0 = 0.0, goo = 0.0;
+  double u0 = 0.0, q0 = 0.0, ee0 = 0.0, e0 = 0.0, goo = 0.0;
+  float inv_goo = 0.f;
   MoveProposal p;
   if (lane == 0) {
     o0 = offsets[b];
     o1 = offsets[b + 1];
     cb = st.cur[b];
-    u0 = st.uq[2 * b];
-    q0 = st.uq[2 * b + 1];
+    u0 = st.uq[4 * b];
+    q0 = st.uq[4 * b + 1];
+    ee0 = st.uq[4 * b + 2];
     e0 = energy[2 * b];
-    goo = *st.goo;
+    goo = st.goo[0];
+    inv_goo = (float)st.goo[1];
     p = prop[b];
   }
-  double su = 0.0, sq = 0.0;
+  float su = 0.f, sq = 0.f;
   for (int rb = lane; rb < (int)gridDim.x; rb += 32) {
-    const double *g = gpart + ((size_t)rb * n_chains + b) * 2;
-    su += __ldcg(g);
-    sq += __ldcg(g + 1);
+    const float2 g = __ldcg(reinterpret_cast<const float2 *>(gpart) +
+                            (size_t)rb * n_chains + b);
+    su += g.x;
+    sq += g.y;
   }
   for (int o = 16; o > 0; o >>= 1) {
     su += __shfl_xor_sync(0xffffffffu, su, o);
@@ -520,16 +548,45 @@ __global__ void __launch_bounds__(256)
   const int at = o0 + p.atom;
   float xn[3];
   for (int i = 0; i < 3; ++i) xn[i] = __fadd_rn(pos[3 * at + i], p.d[i]);
-  const double u1 = u0 + su;
-  const double q1 = q0 + sq;
-  double value, scale;
-  potential_from_gram(u1, q1, goo, potential, value, scale);
-  const bool acc = p.logu < -beta * (value - e0);
+  const float uf = (float)u0, qf = (float)q0;
+  const float u1f = uf + su, q1f = qf + sq;
+  double value, scale, u1, q1, ee1;
+  float dv;  // V' - V for the test
+  if (uf > 0.f && qf > 0.f && u1f > 0.f && q1f > 0.f) {
+    // increments only: ee' - ee = -[(2 u du + du^2) q - u^2 dq] / (q q')
+    const float dee = -(fmaf(2.f * uf, su, su * su) * qf - uf * uf * sq) /
+                      (qf * q1f);
+    const float ef = fmaxf((float)ee0 + dee, 0.f);
+    const float ve = (float)e0;
+    if (potential == 0) {
+      const float v1 = sqrtf(ef * inv_goo);
+      const float den = v1 + ve;
+      dv = den > 0.f ? dee * inv_goo / den : 0.f;
+      value = (double)v1;
+    } else {
+      dv = dee;
+      value = (double)ef;
+    }
+    scale = (double)(u1f / q1f);
+    u1 = u0 + (double)su;
+    q1 = q0 + (double)sq;
+    ee1 = ee0 + (double)dee;
+  } else {
+    // a non-positive or undefined scale on either side: the reference's
+    // rules in FP64 (rare)
+    u1 = u0 + (double)su;
+    q1 = q0 + (double)sq;
+    ee1 = goo - u1 * u1 / q1;
+    gram_value(u1, q1, ee1, goo, inv_goo, potential, value, scale);
+    dv = (float)(value - e0);
+  }
+  const bool acc = (float)p.logu < -(float)beta * dv;
   if (acc) {
     for (int i = 0; i < 3; ++i) pos[3 * at + i] = xn[i];
     st.cur[b] = 1 - cb;
-    st.uq[2 * b] = u1;
-    st.uq[2 * b + 1] = q1;
+    st.uq[4 * b] = u1;
+    st.uq[4 * b + 1] = q1;
+    st.uq[4 * b + 2] = ee1;
     energy[2 * b] = value;
     energy[2 * b + 1] = scale;
     accepted[b] += 1;
@@ -601,14 +658,14 @@ __global__ void mh_gobs_kernel(const float *__restrict__ T,
     if (k < n_bins)
       st.v[k] = a[0];
     else {
-      *st.goo = a[0];
-      st.goo[1] = 0.0;
+      st.goo[0] = a[0];
+      st.goo[1] = 1.0 / a[0];
     }
   }
 }
 
-// Per chain (one CTA): u = v.F, q = F^T M64 F (FP64) of buffer 0, cur = 0,
-// and the potential of the state into energy.
+// Per chain (one CTA): u = v.F, q = F^T M64 F, ee = goo - u^2 / q (FP64) of
+// buffer 0, cur = 0, and the potential of the state into energy.
 __global__ void mh_init_kernel(const double *__restrict__ M64, MhState st,
                                int n_chains, int n_bins, int potential,
                                double *__restrict__ energy) {
@@ -625,11 +682,15 @@ __global__ void mh_init_kernel(const double *__restrict__ M64, MhState st,
   }
   block_sum<2>(a2, scratch);
   if (threadIdx.x == 0) {
+    const double u = a2[0], q = a2[1], goo = st.goo[0];
+    const double ee = goo - u * u / q;
     st.cur[b] = 0;
-    st.uq[2 * b] = a2[0];
-    st.uq[2 * b + 1] = a2[1];
+    st.uq[4 * b] = u;
+    st.uq[4 * b + 1] = q;
+    st.uq[4 * b + 2] = ee;
+    st.uq[4 * b + 3] = 0.0;
     double value, scale;
-    potential_from_gram(a2[0], a2[1], *st.goo, potential, value, scale);
+    gram_value(u, q, ee, goo, (float)st.goo[1], potential, value, scale);
     energy[2 * b] = value;
     energy[2 * b + 1] = scale;
   }

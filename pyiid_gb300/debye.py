@@ -228,19 +228,20 @@ def mh_state_size(n_configs, n_bins):
 
 def mh_views(state):
     """Views of the chain state buffer (layout of pyiid_mh_state_size):
-    v [K], goo, S2 / F2 [2, B, K] (both buffers), uq [B, 2], cur [B] (int32),
-    and S / F [B, K]: each chain's current buffer (gathered copies)."""
+    v [K], goo, S2 / F2 [2, B, K] (both buffers), uqe [B, 4] (u = G.gobs,
+    q = G.G, ee = |gobs - s G|^2, 0), cur [B] (int32), and S / F [B, K]:
+    each chain's current buffer (gathered copies)."""
     buf, b, k = state['buf'], state['n_configs'], state['n_bins']
     bk = b * k
     o = k + 2
     s2 = buf[o:o + 2 * bk].view(2, b, k)
-    uq = buf[o + 2 * bk:o + 2 * bk + 2 * b].view(b, 2)
-    f_off = o + 2 * bk + 2 * b
+    uqe = buf[o + 2 * bk:o + 2 * bk + 4 * b].view(b, 4)
+    f_off = o + 2 * bk + 4 * b
     f2 = buf[f_off:f_off + bk].view(torch.float32).view(2, b, k)
     cur = buf[f_off + bk:].view(torch.int32)[:b]
     idx = cur.long()
     ar = torch.arange(b, device=buf.device)
-    return {'v': buf[:k], 'goo': buf[k], 'S2': s2, 'F2': f2, 'uq': uq,
+    return {'v': buf[:k], 'goo': buf[k], 'S2': s2, 'F2': f2, 'uqe': uqe,
             'cur': cur, 'S': s2[idx, ar], 'F': f2[idx, ar]}
 
 
