@@ -281,7 +281,7 @@ def run_gpu(args, rank, world, local):
             'bound': 'fp32',
             'kernel': ('gradfq2_kernel' if (tuned is None or
                                             tuned['grad_fq']['pairs_per_thread']
-                                            == 0) else 'gradfq_kernel'),
+                                            <= 0) else 'gradfq_kernel'),
             'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
             'frac': achieved / peak if peak else None,
             'peak_source': 'measured live: cuBLAS SGEMM 8192^3 (TF32 off)',

@@ -348,7 +348,8 @@ int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy, float *g_w1,
  *           (the gradient of pyiid_batch_potential_grad: variant 0 evaluates
  *           each unordered pair once, variant 1 twice).
  *   params (pyiid_variant_info): {bins per thread, pairs per thread, threads
- *   per CTA}. */
+ *   per CTA}; pairs per thread <= 0 marks the packed (FP32x2) even/odd
+ *   kernels (0: one pair per thread at a time, -2: two interleaved). */
 enum { PYIID_KERNEL_FQ = 0, PYIID_KERNEL_GRAD_FQ = 1, PYIID_KERNEL_ADJOINT = 2 };
 int pyiid_variant_count(int kernel);
 int pyiid_variant_info(int kernel, int variant, int *params, int n_params);

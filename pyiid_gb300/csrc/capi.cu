@@ -62,10 +62,15 @@ struct GradEntry {
   GradKernel k;
 };
 
-// NP == 0 marks the packed (FP32x2) even/odd kernels
+// NP <= 0 marks the packed (FP32x2) even/odd kernels: 0 one pair per
+// thread at a time, -2 two pairs interleaved
 const FqEntry kFqTable[] = {
     {{32, 0}, fq_pair2_kernel<32>},   {{48, 0}, fq_pair2_kernel<48>},
     {{64, 0}, fq_pair2_kernel<64>},   {{24, 0}, fq_pair2_kernel<24>},
+    {{32, -2}, fq_pair2_kernel<32, 2>},
+    {{48, -2}, fq_pair2_kernel<48, 2>},
+    {{24, -2}, fq_pair2_kernel<24, 2>},
+    {{16, -2}, fq_pair2_kernel<16, 2>},
     {{32, 1}, fq_pair_kernel<32, 1>}, {{32, 2}, fq_pair_kernel<32, 2>},
     {{16, 1}, fq_pair_kernel<16, 1>}, {{16, 2}, fq_pair_kernel<16, 2>},
     {{24, 1}, fq_pair_kernel<24, 1>}, {{24, 2}, fq_pair_kernel<24, 2>},

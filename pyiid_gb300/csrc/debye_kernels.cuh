@@ -414,7 +414,10 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
 // of pair_math.cuh: one packed instruction advances bins k and k+1.
 // F(Q) per two bins and pair: FFMA2 + FFMA2 (recurrence) + FADD2/FFMA2.
 // Records: a = (th_hi, th_lo, kappa, sigma2), b = (ch/r, sh/r, 1/r, 0).
-template <int L>
+// NP = 2: each thread advances two pairs together (independent recurrence
+// chains for the FMA pipe; the two-FMA dependency of one chain is what
+// limits NP = 1); a missing second pair has zero records.
+template <int L, int NP = 1>
 __global__ void __launch_bounds__(kBlock, 2)
     fq_pair2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                     const int4 *__restrict__ tiles,
@@ -474,20 +477,34 @@ __global__ void __launch_bounds__(kBlock, 2)
       float2 acc[M];
 #pragma unroll
       for (int m = 0; m < M; ++m) acc[m] = f2(0.f);
-      for (int q = g; q < np; q += n_groups) {
-        const float4 ra = recA[q];
-        const float4 rb = recB[q];
-        float2 s, co;
-        seed_sincos2(kf, ra.x, ra.y, s, co);
-        float2 t = __fmul2_rn(f2(rb.z), s);
-        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
-        const float2 kp = f2(ra.z), km = f2(-ra.z), sg = f2(ra.w);
+      for (int q = g; q < np; q += NP * n_groups) {
+        float2 t[NP], w[NP], kp[NP], km[NP], sg[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const int qq = q + p * n_groups;
+          const bool ok = qq < np;
+          const float4 ra = recA[ok ? qq : q];
+          const float4 rb = ok ? recB[qq] : make_float4(0.f, 0.f, 0.f, 0.f);
+          float2 s, co;
+          seed_sincos2(kf, ra.x, ra.y, s, co);
+          t[p] = __fmul2_rn(f2(rb.z), s);
+          w[p] = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+          kp[p] = f2(ra.z);
+          km[p] = f2(-ra.z);
+          sg[p] = f2(ra.w);
+        }
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-          acc[m] = (m & 1) ? __ffma2_rn(t, sg, acc[m]) : __fadd2_rn(acc[m], t);
+#pragma unroll
+          for (int p = 0; p < NP; ++p)
+            acc[m] = (m & 1) ? __ffma2_rn(t[p], sg[p], acc[m])
+                             : __fadd2_rn(acc[m], t[p]);
           if (m + 1 < M) {
-            w = __ffma2_rn(km, t, w);
-            t = __ffma2_rn(kp, w, t);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+              w[p] = __ffma2_rn(km[p], t[p], w[p]);
+              t[p] = __ffma2_rn(kp[p], w[p], t[p]);
+            }
           }
         }
       }
