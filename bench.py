@@ -248,7 +248,8 @@ def run_gpu(args, rank, world, local):
     if rank == 0 and not args.no_workloads:
         for name, fn in (('batched_fq_256_alloys', run_batched),
                          ('hmc_64_chains_au1000', run_hmc),
-                         ('delayed_acceptance_au1000', run_delayed_acceptance)):
+                         ('delayed_acceptance_au1000', run_delayed_acceptance),
+                         ('gcmc_au500', run_gcmc)):
             try:
                 workloads[name] = fn(torch)
             except Exception as e:  # noqa: BLE001 -- reported, not fatal
@@ -582,6 +583,49 @@ def run_reference(args, rank, world):
     }
 
 
+def run_gcmc(torch, steps=200):
+    """Grand-canonical Monte Carlo (insert / remove moves, the reference's
+    rule) on a 500-atom fcc Au particle against the G(r) of a 600-atom one,
+    E = 100 Rw, 1000 K, mu = 0: the O(N K) device engine against the
+    reference algorithm (full energy of every trial configuration through
+    Calc1D on the same GPU), same seeds, same number of steps."""
+    from pyiid_gb300 import structures
+    from pyiid_gb300.atoms import Atoms
+    from pyiid_gb300.calc.calc_1d import Calc1D
+    from pyiid_gb300.experiments.elasticscatter import ElasticScatter
+    from pyiid_gb300.sim.gcmc import GrandCanonicalEnsemble
+    s = ElasticScatter(exp_dict=None)
+    target = s.get_pdf(Atoms(numbers=[79] * 600,
+                             positions=structures.fcc_nearest(4.08, 600)))
+    out = {'workload': 'GCMC, 500-atom fcc Au, Au mu = 0, 1000 K, '
+                       'E = 100 Rw, insertions in a 12 A cube'}
+    for name, inc in (('incremental_engine', True),
+                      ('reference_algorithm', False)):
+        atoms = Atoms(numbers=[79] * 500,
+                      positions=structures.fcc_nearest(4.08, 500))
+        atoms.set_cell(np.eye(3) * 12.0)
+        atoms.set_calculator(Calc1D(target_data=target,
+                                    exp_function=s.get_pdf,
+                                    exp_grad_function=s.get_grad_pdf,
+                                    conv=100.))
+        np.random.seed(11)
+        gc = GrandCanonicalEnsemble(atoms, {'Au': 0.0}, temperature=1000,
+                                    seed=11, incremental=inc)
+        n = steps if inc else max(steps // 10, 10)
+        gc.step()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(n):
+            gc.step()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        m = gc.metadata
+        out[name] = {'moves_per_s': n / dt, 'steps_timed': n,
+                     'accepted': m['accepted_additions'] + m['accepted_removals'],
+                     'atoms_at_end': len(gc.traj[-1])}
+    return out
+
+
 WORKLOADS = {
     'batched_fq_256_alloys': lambda torch, **kw: run_batched(torch, **kw),
     'hmc_64_chains_au1000': lambda torch, **kw: run_hmc(torch, **kw),
@@ -589,6 +633,7 @@ WORKLOADS = {
         lambda torch, **kw: run_delayed_acceptance(torch, **kw),
     'exact_incremental_mh':
         lambda torch, **kw: run_incremental_mh(torch, **kw),
+    'gcmc_au500': lambda torch, **kw: run_gcmc(torch, **kw),
 }
 
 

@@ -270,6 +270,45 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
                    int n_steps, double *state, double *energy,
                    uint64_t *counter, int64_t *accepted, double *trace);
 
+/* Host-chosen moves with O(N K) exact energies (grand-canonical and other
+ * Monte Carlo schemes whose proposals and acceptance live on the host, as in
+ * the reference's sim/gcmc.py:13-114 add_atom / del_atom).
+ *
+ * pyiid_mc_propose: one proposal per chain, evaluated exactly without
+ * changing the state; returns when eval is ready.
+ *   mode        : host int32 [n_configs]: PYIID_MOVE_DISPLACE (atom moves to
+ *                 xyz), PYIID_MOVE_INSERT (a new atom of species
+ *                 new_species at xyz; the configuration must have >= 1
+ *                 atom), PYIID_MOVE_REMOVE (atom deleted; >= 2 atoms)
+ *   atom        : host int32 [n_configs], index within the configuration
+ *   xyz         : host float [n_configs][3]
+ *   new_species : host int32 [n_configs]
+ *   state       : from pyiid_mh_init for the current configurations
+ *   eval        : device double [n_configs][8]: V' (potential of the
+ *                 proposed configuration), its scale, u', q', ee' (the Gram
+ *                 scalars), V of the current state (0 if not tracked), 0, 0
+ * Arguments otherwise as pyiid_mh_steps.  The normalisation na of an
+ * inserted or removed atom's configuration is the one the layout of the
+ * new configuration gives.
+ *
+ * pyiid_mc_accept: for chains with accept[c] != 0 the evaluated proposal
+ * becomes the state (host int32 accept [n_configs]; eval from the last
+ * pyiid_mc_propose; energy as pyiid_mh_init's).  The caller then applies the
+ * move to its positions / species / offsets (for insertion and removal the
+ * next call sees the new configuration sizes).  Returns when done. */
+enum { PYIID_MOVE_DISPLACE = 0, PYIID_MOVE_INSERT = 1, PYIID_MOVE_REMOVE = 2 };
+int pyiid_mc_propose(pyiid_ctx *ctx, const float *positions,
+                     const int32_t *species, const int32_t *offsets,
+                     int n_configs, const float *scatter, int n_species,
+                     int n_bins, double qstep, double rstep,
+                     const double *rgrid, int n_r, double qmin, int potential,
+                     const int32_t *mode, const int32_t *atom,
+                     const float *xyz, const int32_t *new_species,
+                     double *state, double *eval);
+int pyiid_mc_accept(pyiid_ctx *ctx, const int32_t *accept, int n_configs,
+                    int n_bins, const double *eval, double *state,
+                    double *energy);
+
 /* F(Q) without device allocation.
  *
  * Same arguments, result and error behaviour as pyiid_fq, for callers that

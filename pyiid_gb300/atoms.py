@@ -243,6 +243,13 @@ class Atoms:
     def append(self, atom):
         self += atom
 
+    def get_cell(self):
+        return self.cell.copy()
+
+    def set_cell(self, cell):
+        c = np.asarray(cell, dtype=float)
+        self.cell = np.diag(c) if c.ndim == 1 else c.reshape(3, 3).copy()
+
     # --------------------------------------------------------- calculator
     def set_calculator(self, calc=None):
         self.calc = calc

@@ -439,6 +439,27 @@ int get_ftab(pyiid_ctx *ctx, const float *scatter, int n_species, int n_bins,
 
 // na[c][k] = N_c * (sum_sp pairs_sp f_sa f_sb) / P_c  (NaN when P_c == 0,
 // as numpy's mean of an empty array).
+// na_k of one configuration from its species counts:
+//   n * (sum_{sa >= sb} pairs(sa, sb) f_sa f_sb) / P,  P = n (n - 1) / 2
+// (NaN when P == 0).  The species-pair order is the layouts'.
+void na_row(const int *count, int n_species, const float *scatter,
+            int n_bins, double *row) {
+  double n = 0;
+  for (int sa = 0; sa < n_species; ++sa) n += count[sa];
+  const double P = n * (n - 1) / 2;
+  for (int k = 0; k < n_bins; ++k) {
+    double s = 0.0;
+    for (int sa = 0; sa < n_species; ++sa)
+      for (int sb = 0; sb <= sa; ++sb) {
+        const double na = count[sa], nb = count[sb];
+        const double pc = (sa == sb) ? na * (na - 1) / 2 : na * nb;
+        s += pc * (double)scatter[(size_t)sa * n_bins + k] *
+             (double)scatter[(size_t)sb * n_bins + k];
+      }
+    row[k] = (P > 0) ? n * s / P : NAN;
+  }
+}
+
 int get_na(pyiid_ctx *ctx, const Layout *L, const float *scatter, int n_bins,
            double **out) {
   uint64_t key = mix(L->key, ctx->ftab_key);
@@ -449,19 +470,13 @@ int get_na(pyiid_ctx *ctx, const Layout *L, const float *scatter, int n_bins,
       return PYIID_OK;
     }
   std::vector<double> na((size_t)L->n_configs * n_bins);
+  std::vector<int> count(L->n_species);
   for (int c = 0; c < L->n_configs; ++c) {
-    const double n = L->natoms[c];
-    const double P = n * (n - 1) / 2;
-    for (int k = 0; k < n_bins; ++k) {
-      double s = 0.0;
-      for (int sp = 0; sp < L->n_spairs; ++sp) {
-        const int2 ss = L->spair_species[sp];
-        s += L->pair_counts[(size_t)c * L->n_spairs + sp] *
-             (double)scatter[(size_t)ss.x * n_bins + k] *
-             (double)scatter[(size_t)ss.y * n_bins + k];
-      }
-      na[(size_t)c * n_bins + k] = (P > 0) ? n * s / P : NAN;
-    }
+    std::fill(count.begin(), count.end(), 0);
+    for (int t = L->cfg_tiles[c].x; t < L->cfg_tiles[c].y; ++t)
+      count[L->tiles[t].w] += L->tiles[t].y;
+    na_row(count.data(), L->n_species, scatter, n_bins,
+           na.data() + (size_t)c * n_bins);
   }
   auto T = std::make_unique<NaTable>();
   T->key = key;
@@ -1031,6 +1046,117 @@ int pyiid_mh_init(pyiid_ctx *ctx, const float *positions,
   return PYIID_OK;
 }
 
+// Buffers and launch shapes of one single-atom step (sized before any launch,
+// so that calls after the first are capturable).
+struct MhStep {
+  Layout *L = nullptr;
+  TMatrix *T = nullptr;
+  float *ftab = nullptr;
+  double *na = nullptr;
+  MhState st;
+  MoveProposal *prop = nullptr;
+  float *part = nullptr, *gpart = nullptr, *fsum = nullptr, *fdif = nullptr;
+  int *done = nullptr;
+  int n_configs = 0, n_bins = 0, kmin = 0, kb0 = 0, kp = 0, n_mi = 0;
+  int n_cg = 0, n_rb = 0, n_cb = 0, n_chunks = 0, n_groups = 0;
+  size_t smem = 0, gram_smem = 0;
+  float dq_hi = 0.f, dq_lo = 0.f;
+};
+
+static int mh_step_setup(pyiid_ctx *ctx, const int32_t *species,
+                         const int32_t *offsets, int n_configs,
+                         const float *scatter, int n_species, int n_bins,
+                         double qstep, double rstep, const double *rgrid,
+                         int n_r, double qmin, int potential, double *state,
+                         MhStep *S) {
+  TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
+                 qstep, rstep, rgrid, n_r, qmin, potential, &S->L, &S->ftab,
+                 &S->na, &S->T));
+  if (!S->T->d_M64)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "pyiid_mh_init must be called first for this grid");
+  S->n_configs = n_configs;
+  S->n_bins = n_bins;
+  S->kmin = S->T->kmin;
+  const int nkk = n_bins - S->kmin;
+  if (nkk < 1 || n_bins > 3200)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "single-atom moves need 1 to 3200 bins (and at least one "
+                "above qmin)");
+  S->kp = (n_bins + 3) & ~3;  // row stride of the F + F', dF rows
+  S->gram_smem = 2 * (size_t)kGramCH * S->kp * sizeof(float);
+  S->n_mi = (int)S->L->mitems.size();
+  S->kb0 = S->kmin & ~1;
+  S->st = mh_state(state, n_configs, n_bins);
+  S->n_cg = (n_configs + kGramCH - 1) / kGramCH;
+  S->n_rb = (nkk + kGramRB - 1) / kGramRB;
+  void *p;
+  TRY(ensure(ctx, "mh_prop", (size_t)n_configs * sizeof(MoveProposal), &p));
+  S->prop = static_cast<MoveProposal *>(p);
+  TRY(ensure(ctx, "mh_partial",
+             (size_t)std::max(S->n_mi, 1) * n_bins * sizeof(float), &p));
+  S->part = static_cast<float *>(p);
+  TRY(ensure(ctx, "mh_done", (size_t)(n_configs + S->n_cg) * sizeof(int),
+             &p));
+  S->done = static_cast<int *>(p);
+  TRY(ensure(ctx, "mh_gpart",
+             (size_t)S->n_rb * n_configs * 2 * sizeof(float), &p));
+  S->gpart = static_cast<float *>(p);
+  // F + F' and dF rows; rows of chains without pair terms stay zero
+  TRY(ensure(ctx, "mh_fsd", 2 * (size_t)n_configs * S->kp * sizeof(float),
+             &p));
+  S->fsum = static_cast<float *>(p);
+  S->fdif = S->fsum + (size_t)n_configs * S->kp;
+  // chunks of kMoveL bins; at most 16 chunks per CTA (>= 16 atom groups)
+  const int chunks_total =
+      std::max(1, (n_bins - S->kb0 + kMoveL - 1) / kMoveL);
+  S->n_cb = (chunks_total + 15) / 16;
+  S->n_chunks = (chunks_total + S->n_cb - 1) / S->n_cb;
+  S->n_groups = kBlock / S->n_chunks;
+  S->smem = 4 * kMoveTiles * kTile * sizeof(float4) +
+            (size_t)kMoveL * (kBlock + 1) * sizeof(float);
+  split_double(qstep, S->dq_hi, S->dq_lo);
+  return PYIID_OK;
+}
+
+// Counters and spare rows start at zero for each call.
+static int mh_step_reset(pyiid_ctx *ctx, const MhStep &S) {
+  CUDA_TRY(ctx, cudaMemsetAsync(S.done, 0,
+                                (size_t)(S.n_configs + S.n_cg) * sizeof(int),
+                                ctx->stream));
+  CUDA_TRY(ctx, cudaMemsetAsync(S.fsum, 0,
+                                2 * (size_t)S.n_configs * S.kp * sizeof(float),
+                                ctx->stream));
+  return PYIID_OK;
+}
+
+static int mh_step_launch(pyiid_ctx *ctx, const MhStep &S, float *positions,
+                          uint64_t *counter, uint64_t seed, float sigma,
+                          HostMoves hm, int potential, double beta,
+                          double *energy, int64_t *accepted, double *trace,
+                          double *eval_out) {
+  if (S.n_mi > 0) {
+    dim3 g1(S.n_mi, S.n_cb);
+    move_delta_kernel<<<g1, kBlock, S.smem, ctx->stream>>>(
+        positions, S.L->d_perm, S.L->d_tiles, S.L->d_mitems,
+        S.L->d_mitem_begin, S.L->d_offsets, S.L->d_species,
+        reinterpret_cast<const unsigned long long *>(counter), (uint32_t)seed,
+        (uint32_t)(seed >> 32), sigma, S.dq_hi, S.dq_lo, S.kb0, S.kmin,
+        S.n_chunks, S.n_groups, S.n_bins, S.ftab, S.na, S.st, S.n_configs,
+        S.kp, hm, S.prop, S.part, S.done, S.fsum, S.fdif);
+    LAUNCH_CHECK(ctx);
+  }
+  dim3 gg(S.n_rb, S.n_cg);
+  move_gram_kernel<<<gg, 256, S.gram_smem, ctx->stream>>>(
+      S.T->d_M32, S.fsum, S.fdif, S.kp, S.L->d_offsets, S.prop, S.st,
+      S.n_configs, S.n_bins, S.kmin, potential, beta, S.gpart,
+      S.done + S.n_configs, positions, energy,
+      reinterpret_cast<unsigned long long *>(counter),
+      reinterpret_cast<long long *>(accepted), trace, eval_out);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
 int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
                    const int32_t *offsets, int n_configs, const float *scatter,
                    int n_species, int n_bins, double qstep, double rstep,
@@ -1045,84 +1171,106 @@ int pyiid_mh_steps(pyiid_ctx *ctx, float *positions, const int32_t *species,
   if (!(sigma >= 0) || !std::isfinite(sigma))
     return fail(ctx, PYIID_ERR_INVALID_ARG, "sigma must be >= 0");
   if (n_steps < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_steps < 0");
-  Layout *L;
-  float *d_ftab;
-  double *d_na;
-  TMatrix *T;
-  TRY(mh_prepare(ctx, species, offsets, n_configs, scatter, n_species, n_bins,
-                 qstep, rstep, rgrid, n_r, qmin, potential, &L, &d_ftab, &d_na,
-                 &T));
-  if (!T->d_M64)
-    return fail(ctx, PYIID_ERR_INVALID_ARG,
-                "pyiid_mh_init must be called first for this grid");
-  const int kmin = T->kmin;
-  const int nkk = n_bins - kmin;
-  if (nkk < 1 || n_bins > 3200)
-    return fail(ctx, PYIID_ERR_INVALID_ARG,
-                "single-atom moves need 1 to 3200 bins (and at least one "
-                "above qmin)");
-  const int kp = (n_bins + 3) & ~3;  // row stride of the F + F', dF rows
-  const size_t gram_smem = 2 * (size_t)kGramCH * kp * sizeof(float);
-  const int n_mi = (int)L->mitems.size();
-  const int kb0 = kmin & ~1;
-  const MhState st = mh_state(state, n_configs, n_bins);
-  const int n_cg = (n_configs + kGramCH - 1) / kGramCH;
-  void *p;
-  TRY(ensure(ctx, "mh_prop", (size_t)n_configs * sizeof(MoveProposal), &p));
-  MoveProposal *d_prop = static_cast<MoveProposal *>(p);
-  TRY(ensure(ctx, "mh_partial",
-             (size_t)std::max(n_mi, 1) * n_bins * sizeof(float), &p));
-  float *d_part = static_cast<float *>(p);
-  TRY(ensure(ctx, "mh_done", (size_t)(n_configs + n_cg) * sizeof(int), &p));
-  int *d_done = static_cast<int *>(p);
-  const int n_rb = (nkk + kGramRB - 1) / kGramRB;
-  TRY(ensure(ctx, "mh_gpart", (size_t)n_rb * n_configs * 2 * sizeof(float),
-             &p));
-  float *d_gpart = static_cast<float *>(p);
-  // F + F' and dF rows; rows of chains without pair terms stay zero
-  TRY(ensure(ctx, "mh_fsd", 2 * (size_t)n_configs * kp * sizeof(float), &p));
-  float *d_fsum = static_cast<float *>(p);
-  float *d_fdif = d_fsum + (size_t)n_configs * kp;
+  MhStep S;
+  TRY(mh_step_setup(ctx, species, offsets, n_configs, scatter, n_species,
+                    n_bins, qstep, rstep, rgrid, n_r, qmin, potential, state,
+                    &S));
   if (n_steps == 0) return PYIID_OK;
-  CUDA_TRY(ctx, cudaMemsetAsync(d_done, 0,
-                                (size_t)(n_configs + n_cg) * sizeof(int),
-                                ctx->stream));
-  CUDA_TRY(ctx, cudaMemsetAsync(d_fsum, 0,
-                                2 * (size_t)n_configs * kp * sizeof(float),
-                                ctx->stream));
-  // chunks of kMoveL bins; at most 16 chunks per CTA (>= 16 atom groups)
-  const int chunks_total = std::max(1, (n_bins - kb0 + kMoveL - 1) / kMoveL);
-  const int n_cb = (chunks_total + 15) / 16;
-  const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
-  const int n_groups = kBlock / n_chunks;
-  const size_t smem = 4 * kMoveTiles * kTile * sizeof(float4) +
-                      (size_t)kMoveL * (kBlock + 1) * sizeof(float);
-  float dq_hi, dq_lo;
-  split_double(qstep, dq_hi, dq_lo);
-  const uint32_t seed_lo = (uint32_t)seed, seed_hi = (uint32_t)(seed >> 32);
+  TRY(mh_step_reset(ctx, S));
   const double beta = conv / kT;
-  dim3 gg(n_rb, n_cg);
-  for (int step = 0; step < n_steps; ++step) {
-    if (n_mi > 0) {
-      dim3 g1(n_mi, n_cb);
-      move_delta_kernel<<<g1, kBlock, smem, ctx->stream>>>(
-          positions, L->d_perm, L->d_tiles, L->d_mitems, L->d_mitem_begin,
-          L->d_offsets, L->d_species,
-          reinterpret_cast<const unsigned long long *>(counter), seed_lo,
-          seed_hi, sigma, dq_hi, dq_lo, kb0, kmin, n_chunks, n_groups, n_bins,
-          d_ftab, d_na, st, n_configs, kp, d_prop, d_part, d_done, d_fsum,
-          d_fdif);
-      LAUNCH_CHECK(ctx);
-    }
-    move_gram_kernel<<<gg, 256, gram_smem, ctx->stream>>>(
-        T->d_M32, d_fsum, d_fdif, kp, L->d_offsets, d_prop, st, n_configs,
-        n_bins, kmin,
-        potential, beta, d_gpart, d_done + n_configs, positions, energy,
-        reinterpret_cast<unsigned long long *>(counter),
-        reinterpret_cast<long long *>(accepted),
-        trace ? trace + (size_t)step * n_configs * 8 : nullptr);
-    LAUNCH_CHECK(ctx);
+  for (int step = 0; step < n_steps; ++step)
+    TRY(mh_step_launch(ctx, S, positions, counter, seed, sigma, HostMoves{},
+                       potential, beta, energy, accepted,
+                       trace ? trace + (size_t)step * n_configs * 8 : nullptr,
+                       nullptr));
+  return PYIID_OK;
+}
+
+int pyiid_mc_propose(pyiid_ctx *ctx, const float *positions,
+                     const int32_t *species, const int32_t *offsets,
+                     int n_configs, const float *scatter, int n_species,
+                     int n_bins, double qstep, double rstep,
+                     const double *rgrid, int n_r, double qmin, int potential,
+                     const int32_t *mode, const int32_t *atom,
+                     const float *xyz, const int32_t *new_species,
+                     double *state, double *eval) {
+  MhStep S;
+  TRY(mh_step_setup(ctx, species, offsets, n_configs, scatter, n_species,
+                    n_bins, qstep, rstep, rgrid, n_r, qmin, potential, state,
+                    &S));
+  std::vector<int4> hp(n_configs);
+  std::vector<float4> hx(n_configs);
+  std::vector<double> na((size_t)n_configs * n_bins);
+  std::vector<int> count(n_species);
+  for (int c = 0; c < n_configs; ++c) {
+    const int o0 = offsets[c], n = offsets[c + 1] - offsets[c];
+    const int m = mode[c];
+    if (m != kMoveDisplace && m != kMoveInsert && m != kMoveRemove)
+      return fail(ctx, PYIID_ERR_INVALID_ARG, "mode[%d] = %d is unknown", c, m);
+    if (m == kMoveInsert && n < 1)
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "insertion into configuration %d needs at least one atom", c);
+    if (m == kMoveInsert &&
+        (new_species[c] < 0 || new_species[c] >= n_species))
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "new_species[%d] = %d outside [0, %d)", c, new_species[c],
+                  n_species);
+    if (m != kMoveInsert && (atom[c] < 0 || atom[c] >= n))
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "atom[%d] = %d outside configuration %d (%d atoms)", c,
+                  atom[c], c, n);
+    if (m == kMoveRemove && n < 2)
+      return fail(ctx, PYIID_ERR_INVALID_ARG,
+                  "removal from configuration %d needs at least two atoms", c);
+    hp[c] = make_int4(m, m == kMoveInsert ? 0 : atom[c],
+                      m == kMoveInsert ? new_species[c] : 0, 0);
+    hx[c] = make_float4(m == kMoveRemove ? 0.f : xyz[3 * c],
+                        m == kMoveRemove ? 0.f : xyz[3 * c + 1],
+                        m == kMoveRemove ? 0.f : xyz[3 * c + 2], 0.f);
+    std::fill(count.begin(), count.end(), 0);
+    for (int i = o0; i < o0 + n; ++i) count[species[i]]++;
+    if (m == kMoveInsert) count[new_species[c]]++;
+    if (m == kMoveRemove) count[species[o0 + atom[c]]]--;
+    na_row(count.data(), n_species, scatter, n_bins,
+           na.data() + (size_t)c * n_bins);
   }
+  void *p;
+  TRY(ensure(ctx, "mc_prop", (size_t)n_configs * sizeof(int4), &p));
+  int4 *d_hp = static_cast<int4 *>(p);
+  TRY(ensure(ctx, "mc_xyz", (size_t)n_configs * sizeof(float4), &p));
+  float4 *d_hx = static_cast<float4 *>(p);
+  TRY(ensure(ctx, "mc_na", na.size() * sizeof(double), &p));
+  double *d_na = static_cast<double *>(p);
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_hp, hp.data(), hp.size() * sizeof(int4),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_hx, hx.data(), hx.size() * sizeof(float4),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_na, na.data(), na.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  TRY(mh_step_reset(ctx, S));
+  HostMoves hm{d_hp, d_hx, d_na};
+  TRY(mh_step_launch(ctx, S, const_cast<float *>(positions), nullptr, 0, 0.f,
+                     hm, potential, 1.0, nullptr, nullptr, nullptr, eval));
+  // the host arrays above are read by the copies: wait before returning
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return PYIID_OK;
+}
+
+int pyiid_mc_accept(pyiid_ctx *ctx, const int32_t *accept, int n_configs,
+                    int n_bins, const double *eval, double *state,
+                    double *energy) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_configs < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_configs < 1");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  void *p;
+  TRY(ensure(ctx, "mc_accept", (size_t)n_configs * sizeof(int), &p));
+  int *d_acc = static_cast<int *>(p);
+  CUDA_TRY(ctx, cudaMemcpyAsync(d_acc, accept, (size_t)n_configs * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  mh_commit_kernel<<<(n_configs + 127) / 128, 128, 0, ctx->stream>>>(
+      d_acc, eval, mh_state(state, n_configs, n_bins), energy, n_configs);
+  LAUNCH_CHECK(ctx);
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return PYIID_OK;
 }
 

@@ -137,6 +137,16 @@ __device__ __forceinline__ size_t mh_row(int which, int b, int n_chains,
   return ((size_t)which * n_chains + b) * n_bins;
 }
 
+// Moves with host-chosen proposals (one per chain): mode, atom index within
+// the configuration, species of an inserted atom; its position in xyz; na of
+// the configuration after the move (insertion and removal change it).
+enum { kMoveDisplace = 0, kMoveInsert = 1, kMoveRemove = 2 };
+struct HostMoves {
+  const int4 *prop;    // (mode, atom, new species, 0) per chain, or NULL
+  const float4 *xyz;   // new position (displace, insert)
+  const double *na;    // [n_chains][n_bins] after the move, or NULL
+};
+
 // Pair terms of the moved atom.  One CTA per work item (chain, species,
 // tiles [t0, t1) of that species: consecutive sorted atoms) and bin block;
 // thread (chunk c, group g) accumulates bins [kbase, kbase + L) of
@@ -146,7 +156,9 @@ __device__ __forceinline__ size_t mh_row(int which, int b, int n_chains,
 // reduced through shared memory and the CTA writes one partial row, already
 // weighted by its species' form factor (FP32: a partial is a difference of a
 // few hundred terms, far below S itself).  The moved atom itself contributes
-// nothing (its records are zero).  The last CTA of a chain to finish
+// nothing (its records are zero); with host moves an inserted atom has no
+// old terms and a removed one no new terms (zero records), so the rows hold
+// +new or -old.  The last CTA of a chain to finish
 // (counted in done[chain], which it resets) then writes, for k >= kmin, into
 // the chain's spare buffer
 //   S'_k = S_k + f_sa(Q_k) sum_{items of the chain} partial[item][k]
@@ -169,7 +181,7 @@ __global__ void __launch_bounds__(kBlock)
                       int n_chunks, int n_groups, int n_bins,
                       const float *__restrict__ ftab,
                       const double *__restrict__ na,
-                      MhState st, int n_chains, int kp,
+                      MhState st, int n_chains, int kp, HostMoves hm,
                       MoveProposal *__restrict__ prop_out,
                       float *__restrict__ partial, int *__restrict__ done,
                       float *__restrict__ fsum, float *__restrict__ fdif) {
@@ -185,7 +197,7 @@ __global__ void __launch_bounds__(kBlock)
   float *red = reinterpret_cast<float *>(nB + NJ);  // [j][thread], padded
   const int rs = blockDim.x + 1;
   __shared__ float sx[6];
-  __shared__ int s_atom, s_last;
+  __shared__ int s_atom, s_last, s_mode, s_sa;
 
   const int4 it = mitems[blockIdx.x];  // (chain, species, t0, t1)
   const int chain = it.x;
@@ -207,29 +219,47 @@ __global__ void __launch_bounds__(kBlock)
   if (tid == 0) {
     const int base = offsets[chain];
     const int n = offsets[chain + 1] - base;
-    const MoveProposal p =
-        make_proposal(seed_lo, seed_hi, counter[chain], chain, n, sigma);
-    if (blockIdx.y == 0 && (int)blockIdx.x == mitem_begin[chain])
-      prop_out[chain] = p;
-    const int a = base + p.atom;  // items exist only for n >= 1
-    s_atom = a;
-    const float x = pos[3 * a], y = pos[3 * a + 1], z = pos[3 * a + 2];
-    sx[0] = x;
-    sx[1] = y;
-    sx[2] = z;
-    sx[3] = __fadd_rn(x, p.d[0]);
-    sx[4] = __fadd_rn(y, p.d[1]);
-    sx[5] = __fadd_rn(z, p.d[2]);
+    if (hm.prop) {
+      const int4 h = hm.prop[chain];
+      const float4 xyz = hm.xyz[chain];
+      const int a = (h.x == kMoveInsert) ? -1 : base + h.y;
+      s_mode = h.x;
+      s_atom = a;
+      s_sa = (h.x == kMoveInsert) ? h.z : species[a];
+      sx[0] = a >= 0 ? pos[3 * a] : 0.f;
+      sx[1] = a >= 0 ? pos[3 * a + 1] : 0.f;
+      sx[2] = a >= 0 ? pos[3 * a + 2] : 0.f;
+      sx[3] = xyz.x;
+      sx[4] = xyz.y;
+      sx[5] = xyz.z;
+    } else {
+      const MoveProposal p =
+          make_proposal(seed_lo, seed_hi, counter[chain], chain, n, sigma);
+      if (blockIdx.y == 0 && (int)blockIdx.x == mitem_begin[chain])
+        prop_out[chain] = p;
+      const int a = base + p.atom;  // items exist only for n >= 1
+      s_mode = kMoveDisplace;
+      s_atom = a;
+      s_sa = species[a];
+      const float x = pos[3 * a], y = pos[3 * a + 1], z = pos[3 * a + 2];
+      sx[0] = x;
+      sx[1] = y;
+      sx[2] = z;
+      sx[3] = __fadd_rn(x, p.d[0]);
+      sx[4] = __fadd_rn(y, p.d[1]);
+      sx[5] = __fadd_rn(z, p.d[2]);
+    }
   }
   __syncthreads();
   const int a = s_atom;
+  const int mode = s_mode;
   // records: thread w < nj the old position, nj <= w < 2 nj the new one
   // (2 nj <= blockDim.x: at most kMoveTiles * 32 atoms per item)
   if (has_rec) {
     const bool nw = tid >= nj;
     float4 *rA = nw ? nA : oA;
     float4 *rB = nw ? nB : oB;
-    if (o_rec == a) {
+    if (o_rec == a || mode == (nw ? kMoveRemove : kMoveInsert)) {
       rA[q_rec] = make_float4(0.f, 0.f, 0.f, 1.f);
       rB[q_rec] = make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
@@ -310,14 +340,14 @@ __global__ void __launch_bounds__(kBlock)
   __syncthreads();
   if (!s_last) return;
   if (tid == 0) done[chain] = 0;
-  const int sa = species[a];
+  const int sa = s_sa;
   const int i0 = mitem_begin[chain], i1 = mitem_begin[chain + 1];
   const int cb = st.cur[chain];
   const double *Sc = st.S + mh_row(cb, chain, n_chains, n_bins);
   const float *Fc = st.F + mh_row(cb, chain, n_chains, n_bins);
   double *Sn = st.S + mh_row(1 - cb, chain, n_chains, n_bins);
   float *Fn = st.F + mh_row(1 - cb, chain, n_chains, n_bins);
-  const double *nab = na + (size_t)chain * n_bins;
+  const double *nab = (hm.na ? hm.na : na) + (size_t)chain * n_bins;
   float *fs_row = fsum + (size_t)chain * kp;
   float *fd_row = fdif + (size_t)chain * kp;
   for (int k = kmin + tid; k < n_bins; k += blockDim.x) {
@@ -394,7 +424,8 @@ __global__ void __launch_bounds__(256)
                      double *__restrict__ energy,
                      unsigned long long *__restrict__ counter,
                      long long *__restrict__ accepted,
-                     double *__restrict__ trace) {
+                     double *__restrict__ trace,
+                     double *__restrict__ eval_out) {
   extern __shared__ float4 sm4[];
   float *ssum = reinterpret_cast<float *>(sm4);  // [l][8]: F + F'
   float *sdif = ssum + 8 * kp;                   // [l][8]: dF
@@ -521,7 +552,7 @@ __global__ void __launch_bounds__(256)
     u0 = st.uq[4 * b];
     q0 = st.uq[4 * b + 1];
     ee0 = st.uq[4 * b + 2];
-    e0 = energy[2 * b];
+    e0 = energy ? energy[2 * b] : 0.0;
     goo = st.goo[0];
     inv_goo = (float)st.goo[1];
     p = prop[b];
@@ -539,6 +570,34 @@ __global__ void __launch_bounds__(256)
   }
   if (lane != 0) return;
   double *tr = trace ? trace + (size_t)b * 8 : nullptr;
+  if (eval_out) {
+    // evaluation only (host-chosen moves): the proposal's potential and Gram
+    // scalars, no state change
+    double *ev = eval_out + (size_t)b * 8;
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    double value = nan, scale = nan, u1 = nan, q1 = nan, ee1 = nan;
+    if (o1 - o0 >= 1) {
+      u1 = u0 + (double)su;
+      q1 = q0 + (double)sq;
+      const float uf = (float)u0, qf = (float)q0;
+      const float u1f = uf + su, q1f = qf + sq;
+      if (uf > 0.f && qf > 0.f && u1f > 0.f && q1f > 0.f) {
+        const float dee = -(fmaf(2.f * uf, su, su * su) * qf - uf * uf * sq) /
+                          (qf * q1f);
+        ee1 = ee0 + (double)dee;
+      } else {
+        ee1 = goo - u1 * u1 / q1;
+      }
+      gram_value(u1, q1, ee1, goo, inv_goo, potential, value, scale);
+    }
+    ev[0] = value;
+    ev[1] = scale;
+    ev[2] = u1;
+    ev[3] = q1;
+    ev[4] = ee1;
+    ev[5] = e0;
+    return;
+  }
   if (o1 - o0 < 2) {
     counter[b] += 1ull;
     if (tr)
@@ -602,6 +661,23 @@ __global__ void __launch_bounds__(256)
     tr[7] = e0;
   }
   counter[b] += 1ull;
+}
+
+// Host decision on host-chosen moves: for chains with accept[b] != 0 the
+// proposal evaluated by move_gram_kernel (eval[b] = V', scale, u', q', ee')
+// becomes the state: the buffer index flips, (u, q, ee) and energy are stored.
+__global__ void mh_commit_kernel(const int *__restrict__ accept,
+                                 const double *__restrict__ eval, MhState st,
+                                 double *__restrict__ energy, int n_chains) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_chains || !accept[b]) return;
+  const double *ev = eval + (size_t)b * 8;
+  st.cur[b] = 1 - st.cur[b];
+  st.uq[4 * b] = ev[2];
+  st.uq[4 * b + 1] = ev[3];
+  st.uq[4 * b + 2] = ev[4];
+  energy[2 * b] = ev[0];
+  energy[2 * b + 1] = ev[1];
 }
 
 // ---------------------------------------------------------- state set-up

@@ -12,7 +12,10 @@ from ._native import context, POTENTIALS, NativeError
 
 __all__ = ['fq', 'batch_fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
            'batch_potential_grad', 'as_positions', 'mh_init', 'mh_steps',
-           'mh_state_size', 'mh_views']
+           'mh_state_size', 'mh_views', 'mc_propose', 'mc_accept',
+           'MOVE_DISPLACE', 'MOVE_INSERT', 'MOVE_REMOVE']
+
+MOVE_DISPLACE, MOVE_INSERT, MOVE_REMOVE = 0, 1, 2
 
 _f32p = None
 
@@ -323,4 +326,59 @@ def mh_steps(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
              ctypes.c_void_p(state['counter'].data_ptr()),
              ctypes.c_void_p(state['accepted'].data_ptr()),
              ctypes.c_void_p(trace.data_ptr() if trace is not None else 0))
+    return state
+
+
+def mc_propose(positions, species, offsets, scatter, qstep, rstep, rgrid,
+               qmin, state, mode, atom, xyz, new_species=None, kind='rw'):
+    """Exact potential of one host-chosen move per chain (no state change).
+
+    mode [B] (MOVE_DISPLACE, MOVE_INSERT, MOVE_REMOVE), atom [B] (index
+    within its configuration), xyz [B, 3] (new position), new_species [B]
+    (inserted species id).  Returns the device tensor eval [B, 8]:
+    V', scale, u', q', ee', V (0), 0, 0; the proposal is kept in the state's
+    spare buffers for :func:`mc_accept`."""
+    import ctypes
+    pos = as_positions(positions)
+    sp = _np(species, np.int32)
+    off = _np(offsets, np.int32)
+    tab = _np(scatter, np.float32)
+    rg = _np(rgrid, np.float64)
+    b = len(off) - 1
+    md = _np(mode, np.int32).reshape(b)
+    at = _np(atom, np.int32).reshape(b)
+    xz = _np(xyz, np.float32).reshape(b, 3)
+    ns = _np(np.zeros(b) if new_species is None else new_species,
+             np.int32).reshape(b)
+    if state.get('n_configs') != b or state.get('n_bins') != tab.shape[1]:
+        raise NativeError('state does not match the batch (call mh_init)')
+    if state.get('eval') is None:
+        state['eval'] = torch.empty((b, 8), dtype=torch.float64,
+                                    device=pos.device)
+    ctx = context(pos.device.index)
+    ctx.call('pyiid_mc_propose', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
+             _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
+             float(qstep), float(rstep), _ptr(rg, ctypes.c_double), len(rg),
+             float(qmin), POTENTIALS[kind], _ptr(md, ctypes.c_int32),
+             _ptr(at, ctypes.c_int32), _ptr(xz, ctypes.c_float),
+             _ptr(ns, ctypes.c_int32), ctypes.c_void_p(state['buf'].data_ptr()),
+             ctypes.c_void_p(state['eval'].data_ptr()))
+    return state['eval']
+
+
+def mc_accept(state, accept):
+    """Make the proposals of the last :func:`mc_propose` the state of the
+    chains with accept[c] true (the caller then applies the moves to its
+    positions, species and offsets)."""
+    import ctypes
+    acc = _np(np.asarray(accept, bool).astype(np.int32), np.int32)
+    b = state['n_configs']
+    if acc.size != b:
+        raise NativeError(f'accept has {acc.size} entries, the state {b}')
+    ctx = context(state['buf'].device.index)
+    ctx.call('pyiid_mc_accept', _ptr(acc, ctypes.c_int32), b,
+             state['n_bins'], ctypes.c_void_p(state['eval'].data_ptr()),
+             ctypes.c_void_p(state['buf'].data_ptr()),
+             ctypes.c_void_p(state['energy'].data_ptr()))
     return state
