@@ -309,6 +309,33 @@ int pyiid_mc_accept(pyiid_ctx *ctx, const int32_t *accept, int n_configs,
                     int n_bins, const double *eval, double *state,
                     double *energy);
 
+/* ------------------------------------------------------------------------ *
+ * Spring potentials (pyiid/calc/spring_calc.py), the pair potentials the
+ * reference's samplers combine with the scattering potential (MultiCalc).
+ *   sp_type : PYIID_SPRING_REP (pairs closer than rt, spring_nrg /
+ *             spring_force :99-141), PYIID_SPRING_ATT (pairs farther than
+ *             rt, att_spring_* :252-295), PYIID_SPRING_COM (atoms farther
+ *             than rt from com, com_spring_* :185-217)
+ *   com     : host double [3], the centre of mass (PYIID_SPRING_COM only)
+ * pyiid_spring: energy (device double [1]) = sum over ordered pairs (or
+ *   atoms) of k (r - rt)^2 / 2; forces (device float [n][3], may be NULL)
+ *   are the reference's (half of -dE/dq for the pair springs); atomwise
+ *   (device double, may be NULL) is calculate_atomwise_energy: per atom the
+ *   energy change on its removal for the pair springs ([n]), and the
+ *   reference's scalar for the com spring ([1]).
+ * pyiid_spring_voxels: calculate_voxel_energy (voxel_spring_nrg :145-166 and
+ *   its att/com twins): for each voxel centre ((i+1/2) res, (j+1/2) res,
+ *   (k+1/2) res) the energy change on inserting an atom there; voxels is a
+ *   device double [nx][ny][nz]. */
+enum { PYIID_SPRING_REP = 0, PYIID_SPRING_ATT = 1, PYIID_SPRING_COM = 2 };
+int pyiid_spring(pyiid_ctx *ctx, const float *positions, int n_atoms,
+                 double k, double rt, int sp_type, const double *com,
+                 double *energy, float *forces, double *atomwise);
+int pyiid_spring_voxels(pyiid_ctx *ctx, const float *positions, int n_atoms,
+                        double k, double rt, int sp_type, const double *com,
+                        int nx, int ny, int nz, double resolution,
+                        double *voxels);
+
 /* F(Q) without device allocation.
  *
  * Same arguments, result and error behaviour as pyiid_fq, for callers that

@@ -61,6 +61,11 @@ _SIGNATURES = {
         _c_dbl, _f64p, _c_int, _c_dbl, _c_int, _i32p, _i32p, _f32p, _i32p,
         _vp, _vp]),
     'pyiid_mc_accept': (_c_int, [_vp, _i32p, _c_int, _c_int, _vp, _vp, _vp]),
+    'pyiid_spring': (_c_int, [_vp, _vp, _c_int, _c_dbl, _c_dbl, _c_int,
+                              _f64p, _vp, _vp, _vp]),
+    'pyiid_spring_voxels': (_c_int, [_vp, _vp, _c_int, _c_dbl, _c_dbl,
+                                     _c_int, _f64p, _c_int, _c_int, _c_int,
+                                     _c_dbl, _vp]),
     'pyiid_fq_noalloc': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
                                   _c_int, _c_dbl, _c_int, _vp]),
     'pyiid_rbf_features': (_c_int, [_vp, _vp, _i32p, _c_int, _c_int,

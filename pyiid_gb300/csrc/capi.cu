@@ -25,6 +25,7 @@
 #include "../../include/pyiid_gb300.h"
 #include "debye_kernels.cuh"
 #include "move_kernels.cuh"
+#include "spring_kernels.cuh"
 #include "transform_kernels.cuh"
 
 using namespace pyiid;
@@ -1271,6 +1272,79 @@ int pyiid_mc_accept(pyiid_ctx *ctx, const int32_t *accept, int n_configs,
       d_acc, eval, mh_state(state, n_configs, n_bins), energy, n_configs);
   LAUNCH_CHECK(ctx);
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return PYIID_OK;
+}
+
+// ------------------------------------------------------------------ springs
+static int spring_check(pyiid_ctx *ctx, int n_atoms, double k, double rt,
+                        int sp_type, const double *com) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  if (!std::isfinite(k) || !std::isfinite(rt))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "k and rt must be finite");
+  if (sp_type < PYIID_SPRING_REP || sp_type > PYIID_SPRING_COM)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "unknown spring type %d", sp_type);
+  if (sp_type == PYIID_SPRING_COM && !com)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "the centre-of-mass spring needs com");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  return PYIID_OK;
+}
+
+int pyiid_spring(pyiid_ctx *ctx, const float *positions, int n_atoms,
+                 double k, double rt, int sp_type, const double *com,
+                 double *energy, float *forces, double *atomwise) {
+  TRY(spring_check(ctx, n_atoms, k, rt, sp_type, com));
+  const int nb = std::max(1, (n_atoms + kSpringBlock - 1) / kSpringBlock);
+  void *p;
+  TRY(ensure(ctx, "spring_part", 2 * (size_t)nb * sizeof(double), &p));
+  double *part = static_cast<double *>(p);
+  if (n_atoms == 0) {
+    CUDA_TRY(ctx, cudaMemsetAsync(energy, 0, sizeof(double), ctx->stream));
+    if (atomwise && sp_type == PYIID_SPRING_COM)
+      CUDA_TRY(ctx, cudaMemsetAsync(atomwise, 0, sizeof(double), ctx->stream));
+    return PYIID_OK;
+  }
+  if (sp_type == PYIID_SPRING_COM) {
+    com_spring_kernel<<<nb, kSpringBlock, 0, ctx->stream>>>(
+        positions, n_atoms, (float)k, (float)rt, com[0], com[1], com[2], part,
+        part + nb, forces);
+    LAUNCH_CHECK(ctx);
+    if (atomwise) {
+      sum_partials_kernel<<<1, 256, 0, ctx->stream>>>(part + nb, nb, atomwise);
+      LAUNCH_CHECK(ctx);
+    }
+  } else {
+    spring_pair_kernel<<<nb, kSpringBlock, 0, ctx->stream>>>(
+        positions, n_atoms, (float)k, (float)rt, sp_type, part, forces,
+        atomwise);
+    LAUNCH_CHECK(ctx);
+  }
+  sum_partials_kernel<<<1, 256, 0, ctx->stream>>>(part, nb, energy);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+int pyiid_spring_voxels(pyiid_ctx *ctx, const float *positions, int n_atoms,
+                        double k, double rt, int sp_type, const double *com,
+                        int nx, int ny, int nz, double resolution,
+                        double *voxels) {
+  TRY(spring_check(ctx, n_atoms, k, rt, sp_type, com));
+  if (nx < 0 || ny < 0 || nz < 0)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "negative voxel grid");
+  if (!(resolution > 0) || !std::isfinite(resolution))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "resolution must be > 0");
+  const long long nv = (long long)nx * ny * nz;
+  if (nv == 0) return PYIID_OK;
+  const long long nb = (nv + kSpringBlock - 1) / kSpringBlock;
+  if (nb > INT32_MAX)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "voxel grid too large");
+  const double c0 = com ? com[0] : 0.0, c1 = com ? com[1] : 0.0,
+               c2 = com ? com[2] : 0.0;
+  spring_voxel_kernel<<<(unsigned)nb, kSpringBlock, 0, ctx->stream>>>(
+      positions, n_atoms, (float)k, (float)rt, sp_type, c0, c1, c2, nx, ny, nz,
+      (float)resolution, voxels);
+  LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }
 
