@@ -64,7 +64,8 @@ struct GradEntry {
 };
 
 // NP <= 0 marks the packed (FP32x2) even/odd kernels: 0 one pair per
-// thread at a time, -2 two pairs interleaved
+// thread at a time, -2 two pairs interleaved, -3 (and -4) the per-tile-pair
+// group reduction at 3 (4) CTAs per SM
 const FqEntry kFqTable[] = {
     {{32, 0}, fq_pair2_kernel<32>},   {{48, 0}, fq_pair2_kernel<48>},
     {{64, 0}, fq_pair2_kernel<64>},   {{24, 0}, fq_pair2_kernel<24>},
@@ -76,6 +77,9 @@ const FqEntry kFqTable[] = {
     {{16, 1}, fq_pair_kernel<16, 1>}, {{16, 2}, fq_pair_kernel<16, 2>},
     {{24, 1}, fq_pair_kernel<24, 1>}, {{24, 2}, fq_pair_kernel<24, 2>},
     {{48, 1}, fq_pair_kernel<48, 1>}, {{16, 4}, fq_pair_kernel<16, 4>},
+    {{32, -3}, fq_pair3_kernel<32, 3>}, {{32, -4}, fq_pair3_kernel<32, 4>},
+    {{24, -3}, fq_pair3_kernel<24, 3>}, {{24, -4}, fq_pair3_kernel<24, 4>},
+    {{16, -4}, fq_pair3_kernel<16, 4>},
 };
 // (the last template argument is the minimum resident CTAs per SM, i.e. the
 // register budget: 2 x 256 threads -> 128 registers, 3 x 256 -> 85)
@@ -96,7 +100,13 @@ const GradEntry kGradTable[] = {
 constexpr int kNumFq = sizeof(kFqTable) / sizeof(kFqTable[0]);
 constexpr int kNumGrad = sizeof(kGradTable) / sizeof(kGradTable[0]);
 
-size_t fq_smem(const FqVariant &v) {
+// Dynamic shared memory of an F(Q) launch with n_chunks chunks per CTA
+// (n_chunks < 0: the upper bound over all launches, for the attribute).
+size_t fq_smem(const FqVariant &v, int n_chunks = -1) {
+  if (v.NP <= -3) {  // records / group scratch + FP64 per-bin accumulators
+    const size_t acc = n_chunks < 0 ? 32768 : (size_t)n_chunks * v.L * 8;
+    return 2 * kTile * kTile * sizeof(float4) + acc;
+  }
   return 2 * kTile * kTile * sizeof(float4) +
          2 * (size_t)v.L * kBlock * sizeof(float);
 }
@@ -626,7 +636,7 @@ int run_fq(pyiid_ctx *ctx, const Layout *L, const float *positions,
     TRY(ensure(ctx, "fq_partial", (size_t)n_items * n_bins * sizeof(double), &p));
     partial = static_cast<double *>(p);
     dim3 grid(n_items, n_cb);
-    E.k<<<grid, kBlock, fq_smem(E.v), ctx->stream>>>(
+    E.k<<<grid, kBlock, fq_smem(E.v, n_chunks), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_items, dq_hi, dq_lo, kb0,
         n_chunks, n_groups, n_bins, partial);
     LAUNCH_CHECK(ctx);
@@ -1575,7 +1585,7 @@ extern "C" int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
     const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
     const int n_groups = kBlock / n_chunks;
     dim3 grid(n_items, n_cb);
-    E.k<<<grid, kBlock, fq_smem(E.v), st>>>(positions, d_perm, d_tiles,
+    E.k<<<grid, kBlock, fq_smem(E.v, n_chunks), st>>>(positions, d_perm, d_tiles,
                                             d_items, dq_hi, dq_lo, kb0,
                                             n_chunks, n_groups, n_bins, d_part);
     LAUNCH_CHECK(ctx);

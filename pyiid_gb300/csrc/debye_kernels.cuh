@@ -545,6 +545,114 @@ __global__ void __launch_bounds__(kBlock, 2)
   }
 }
 
+// F(Q) pair sums with the group reduction done per tile pair: after each
+// tile pair the groups' FP32 register sums go through the (then idle)
+// record buffer, are added in a fixed order and accumulated per bin in FP64
+// shared memory.  No per-thread compensated sums are kept, so the kernel
+// fits MINB CTAs per SM (e.g. 4 x 256 threads at <= 64 registers) instead
+// of two.  Dynamic shared memory: 2*32*32 float4 records (>= n_groups *
+// n_chunks * L floats of group scratch) + n_chunks * L doubles.
+template <int L, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB)
+    fq_pair3_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                    const int4 *__restrict__ tiles,
+                    const int4 *__restrict__ items, float dq_hi, float dq_lo,
+                    int kb0, int n_chunks, int n_groups, int n_bins,
+                    double *__restrict__ partial) {
+  static_assert(L % 2 == 0, "L must be even");
+  static_assert(kBlock * L <= 2 * kTile * kTile * 4,
+                "group scratch must fit the record buffer");
+  constexpr int M = L / 2;
+  extern __shared__ float4 smem[];
+  float4 *recA = smem;
+  float4 *recB = smem + kTile * kTile;
+  float *scratch = reinterpret_cast<float *>(smem);
+  double *acc64 = reinterpret_cast<double *>(smem + 2 * kTile * kTile);
+  __shared__ float4 sI[kTile], sJ[kTile];
+
+  const int4 it = items[blockIdx.x];
+  const int4 ti = tiles[it.x];
+  const int tid = threadIdx.x;
+  const int c = tid % n_chunks;
+  const int g = tid / n_chunks;
+  const bool active = g < n_groups;
+  const int kbase = kb0 + (blockIdx.y * n_chunks + c) * L;
+  const float kf = (float)kbase;
+  const int nk = n_chunks * L;
+
+  if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+  for (int i = tid; i < nk; i += blockDim.x) acc64[i] = 0.0;
+
+  for (int tj = it.y; tj < it.z; ++tj) {
+    const int4 tJ = tiles[tj];
+    __syncthreads();
+    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
+    __syncthreads();
+    const bool diag = (tj == it.x);
+    const int np = diag ? ti.y * (ti.y - 1) / 2 : ti.y * tJ.y;
+    for (int q = tid; q < np; q += blockDim.x) {
+      int a, b;
+      if (diag) {
+        tri_index(q, a, b);
+      } else {
+        a = q / tJ.y;
+        b = q - a * tJ.y;
+      }
+      const float4 pa = sI[a];
+      const float4 pb = diag ? sI[b] : sJ[b];
+      float dx, dy, dz;
+      PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
+                                 dq_lo, dx, dy, dz);
+      recA[q] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
+      recB[q] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
+    }
+    __syncthreads();
+    float2 acc[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) acc[m] = f2(0.f);
+    if (active) {
+      for (int q = g; q < np; q += n_groups) {
+        const float4 ra = recA[q];
+        const float4 rb = recB[q];
+        float2 s, co;
+        seed_sincos2(kf, ra.x, ra.y, s, co);
+        float2 t = __fmul2_rn(f2(rb.z), s);
+        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+        const float2 kp = f2(ra.z), km = f2(-ra.z), sg = f2(ra.w);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+          acc[m] = (m & 1) ? __ffma2_rn(t, sg, acc[m]) : __fadd2_rn(acc[m], t);
+          if (m + 1 < M) {
+            w = __ffma2_rn(km, t, w);
+            t = __ffma2_rn(kp, w, t);
+          }
+        }
+      }
+    }
+    __syncthreads();  // records are dead: reuse them as group scratch
+    if (active) {
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+        scratch[g * nk + c * L + 2 * m] = acc[m].x;
+        scratch[g * nk + c * L + 2 * m + 1] = acc[m].y;
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < nk; i += blockDim.x) {
+      float sum = 0.f;
+      for (int gg = 0; gg < n_groups; ++gg) sum += scratch[gg * nk + i];
+      acc64[i] += (double)sum;
+    }
+  }
+  __syncthreads();
+  const int kfirst = kb0 + blockIdx.y * nk;
+  double *out = partial + (size_t)blockIdx.x * n_bins;
+  for (int i = tid; i < nk; i += blockDim.x) {
+    const int k = kfirst + i;
+    if (k < n_bins) out[k] = acc64[i];
+  }
+}
+
 // dF/dx, packed.  Records per (a, b), stored [b][a]:
 //   a = (th_hi, th_lo, kappa, sigma2)
 //   b = (beta ch, beta sh, beta, gamma')   beta = -1/r^3, gamma' = -r dq/(2 ch)
