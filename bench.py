@@ -249,7 +249,8 @@ def run_gpu(args, rank, world, local):
         for name, fn in (('batched_fq_256_alloys', run_batched),
                          ('hmc_64_chains_au1000', run_hmc),
                          ('delayed_acceptance_au1000', run_delayed_acceptance),
-                         ('gcmc_au500', run_gcmc)):
+                         ('gcmc_au500', run_gcmc),
+                         ('nuts_64_chains_au1000', run_nuts)):
             try:
                 workloads[name] = fn(torch)
             except Exception as e:  # noqa: BLE001 -- reported, not fatal
@@ -626,6 +627,57 @@ def run_gcmc(torch, steps=200):
     return out
 
 
+def run_nuts(torch, iters=2):
+    """NUTS (the reference's algorithm) on 64 chains of the 1,000-atom Au
+    particle (300 K, E = 100 Rw, escape depth 6): all chains batched into
+    one exact evaluation per tree leaf, against one chain of the sequential
+    NUTSCanonicalEnsemble (the reference's per-chain loop) on the same GPU."""
+    from pyiid_gb300.atoms import Atoms
+    from pyiid_gb300.calc.calc_1d import Calc1D
+    from pyiid_gb300.experiments.elasticscatter import ElasticScatter
+    from pyiid_gb300.experiments.elasticscatter.gb300_wrap import species_of
+    from pyiid_gb300.nuts_batched import BatchedNUTS
+    from pyiid_gb300.sampling import PDFPotential
+    from pyiid_gb300.sim.nuts_hmc import NUTSCanonicalEnsemble
+    from pyiid_gb300 import structures
+    s = ElasticScatter(exp_dict=None)
+    ref = structures.fcc_nearest(4.08, 1000)
+    target = s.get_pdf(Atoms(numbers=[79] * 1000, positions=ref))
+    starts = np.stack([structures.displaced(ref, 0.05, 4 + c)
+                       for c in range(64)])
+    probe = Atoms(numbers=[79] * 1000, positions=starts[0])
+    s._ensure(probe)
+    tab = species_of(probe, 'PDF')[1]
+    pot = PDFPotential([79] * 1000, target, None, conv=100., n_configs=64,
+                       table=tab)
+    out = {'workload': 'NUTS, 64 chains x 1000-atom fcc Au, 300 K, '
+                       'E = 100 Rw, escape depth 6'}
+    t = time.perf_counter()
+    bn = BatchedNUTS(pot, starts, temperature=300, seeds=range(64),
+                     escape_level=6)
+    ev0 = bn.evaluations
+    t1 = time.perf_counter()
+    bn.step(iters)
+    dt = time.perf_counter() - t1
+    leaves = sum(ch.metadata['samples_total'] for ch in bn.chains)
+    out['batched'] = {'chain_iterations_per_s': 64 * iters / dt,
+                      'leapfrog_steps_per_s': leaves / dt,
+                      'batched_evaluations': bn.evaluations - ev0,
+                      'setup_s': t1 - t}
+    atoms = Atoms(numbers=[79] * 1000, positions=starts[0])
+    atoms.set_calculator(Calc1D(target_data=target, exp_function=s.get_pdf,
+                                exp_grad_function=s.get_grad_pdf, conv=100.))
+    ens = NUTSCanonicalEnsemble(atoms, temperature=300, seed=0,
+                                escape_level=6)
+    t1 = time.perf_counter()
+    ens.run(1)
+    dt = time.perf_counter() - t1
+    out['sequential_one_chain'] = {
+        'chain_iterations_per_s': 1 / dt,
+        'leapfrog_steps_per_s': ens.metadata['samples_total'] / dt}
+    return out
+
+
 WORKLOADS = {
     'batched_fq_256_alloys': lambda torch, **kw: run_batched(torch, **kw),
     'hmc_64_chains_au1000': lambda torch, **kw: run_hmc(torch, **kw),
@@ -634,6 +686,7 @@ WORKLOADS = {
     'exact_incremental_mh':
         lambda torch, **kw: run_incremental_mh(torch, **kw),
     'gcmc_au500': lambda torch, **kw: run_gcmc(torch, **kw),
+    'nuts_64_chains_au1000': lambda torch, **kw: run_nuts(torch, **kw),
 }
 
 

@@ -57,10 +57,12 @@ class PDFPotential:
               has the same atoms; or a list of per-configuration arrays
               (uneven sizes allowed).
     gobs    : observed G(r) on the experiment's r grid.
+    table   : optional form factors [number of distinct elements][n_bins]
+              on the PDF grid (default: the stand-in f(Q) at the grid's Q).
     """
 
     def __init__(self, numbers, gobs, exp_dict=None, potential='rw',
-                 conv=1.0, n_configs=1, device=None):
+                 conv=1.0, n_configs=1, device=None, table=None):
         self.exp, self.qstep, self.n_bins, self.rgrid = experiment_grids(
             exp_dict)
         if isinstance(numbers, (list, tuple)) and len(numbers) and \
@@ -74,9 +76,17 @@ class PDFPotential:
         self.offsets = np.concatenate(
             [[0], np.cumsum([len(n) for n in per_cfg])]).astype(np.int32)
         q = np.arange(self.n_bins) * self.qstep
-        self.table = np.stack([form_factor_array(z, q) for z in self.uniq]
-                              ).astype(np.float32) if len(self.uniq) else \
-            np.zeros((1, self.n_bins), np.float32)
+        if table is not None:
+            # explicit rows [len(unique numbers)][n_bins], e.g. the tables a
+            # GB300 ElasticScatter attached to the atoms
+            self.table = np.ascontiguousarray(table, np.float32)
+            if self.table.shape != (max(len(self.uniq), 1), self.n_bins):
+                raise ValueError(f'table shape {self.table.shape}, expected '
+                                 f'({len(self.uniq)}, {self.n_bins})')
+        else:
+            self.table = np.stack([form_factor_array(z, q) for z in self.uniq]
+                                  ).astype(np.float32) if len(self.uniq) else \
+                np.zeros((1, self.n_bins), np.float32)
         self.masses = np.array([atomic_mass(z) for z in allnum])
         self.device = torch.device('cuda' if device is None else device)
         self.gobs = torch.as_tensor(np.asarray(gobs, np.float64),
