@@ -209,11 +209,9 @@ def run_gpu(args, rank, world, local):
     launches = ctx.launches - launches0
     t_f = [ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)]
     t_g = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
-    ms_step = float(np.sum(t_f) + np.sum(t_g)) / args.steps
-    if pg:
-        t = torch.tensor([ms_step], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_step = float(t.item())
+    from pyiid_gb300.distributed import max_over_ranks
+    ms_step = max_over_ranks(float(np.sum(t_f) + np.sum(t_g)) / args.steps,
+                             device=dev)
     value = world / (ms_step * 1e-3)
 
     # end to end: pinned host positions -> device, F + dF/dx, results -> pinned host
@@ -236,11 +234,7 @@ def run_gpu(args, rank, world, local):
         e.synchronize()
         if i:
             times.append(s.elapsed_time(e))
-    e2e_ms = float(np.mean(times))
-    if pg:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(float(np.mean(times)), device=dev)
     # correctness guard on what was timed: finite, nonzero
     assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
 
