@@ -325,11 +325,21 @@ def batched_workload():
 
 def run_batched(torch, steps=5):
     """Configuration 3: F(Q) of all 256 configurations per step, one graph
-    replay (one pair-sum launch + one finishing launch)."""
-    from pyiid_gb300 import debye
+    replay (one pair-sum launch + one finishing launch), with the F(Q) launch
+    shape tuned on this batch."""
+    from pyiid_gb300 import autotune
+    with autotune.variant_scope():
+        return _run_batched(torch, steps)
+
+
+def _run_batched(torch, steps):
+    from pyiid_gb300 import autotune, debye
     pos, sp, off, tab, sizes = batched_workload()
     p = torch.as_tensor(pos, device='cuda')
     out = torch.empty((len(sizes), 500), dtype=torch.float32, device='cuda')
+    tuned = autotune.tune_call(
+        lambda: debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out),
+        kernels=('fq',), reps=2)
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
@@ -354,14 +364,22 @@ def run_batched(torch, steps=5):
             'atoms': int(sizes.sum()), 'pairs': pairs,
             'ms_per_batch': ms, 'configs_per_s': len(sizes) / (ms * 1e-3),
             'pair_bin_terms_per_s': pairs * 498 / (ms * 1e-3),
+            'fq_variant': tuned['fq']['best'],
             'launch': 'CUDA graph replay: 1 pair-sum + 1 finishing kernel'}
 
 
 def run_hmc(torch, iters=6):
     """Configuration 4: 1,000-atom fcc Au, 64 chains, 10 leapfrog steps,
     dt = 1e-3, T = 300 K, E = 100 * Rw against the undisplaced G(r); one
-    CUDA-graph replay per HMC iteration of all chains."""
-    from pyiid_gb300 import structures
+    CUDA-graph replay per HMC iteration of all chains, with the F(Q) and
+    adjoint launch shapes tuned on the batched evaluation."""
+    from pyiid_gb300 import autotune
+    with autotune.variant_scope():
+        return _run_hmc(torch, iters)
+
+
+def _run_hmc(torch, iters):
+    from pyiid_gb300 import autotune, structures
     from pyiid_gb300.sampling import PDFPotential, BatchedHMC, experiment_grids
     from pyiid_gb300.scatter_factors import species_tables
     from pyiid_gb300 import debye
@@ -372,6 +390,8 @@ def run_hmc(torch, iters=6):
     gobs = debye.pdf(f, qb, exp['rstep'], rg, exp['qmin']).cpu().numpy()
     pot = PDFPotential([79] * 1000, gobs, None, conv=100.0, n_configs=64)
     xs = np.stack([structures.displaced(ref, 0.05, 4 + c) for c in range(64)])
+    x0 = torch.as_tensor(xs.reshape(-1, 3).astype(np.float32), device='cuda')
+    tuned = autotune.tune_call(lambda: pot.evaluate(x0), reps=2)
     hmc = BatchedHMC(pot, xs, temperature=300.0, dt=1e-3, n_steps=10, seed=4,
                      graph=True)
     hmc.step(2)
@@ -400,6 +420,7 @@ def run_hmc(torch, iters=6):
             'acceptance': acc / (iters * 64),
             'ms_per_iteration': 1e3 * s / iters,
             'ms_per_force_eval_64_chains': e0.elapsed_time(e1) / 3,
+            'variants': {k: v['best'] for k, v in tuned.items()},
             'launch': 'CUDA graph replay per HMC iteration (11 batched exact evaluations)'}
 
 
@@ -622,6 +643,12 @@ def run_gcmc(torch, steps=200):
 
 
 def run_nuts(torch, iters=2):
+    from pyiid_gb300 import autotune
+    with autotune.variant_scope():
+        return _run_nuts(torch, iters)
+
+
+def _run_nuts(torch, iters):
     """NUTS (the reference's algorithm) on 64 chains of the 1,000-atom Au
     particle (300 K, E = 100 Rw, escape depth 6): all chains batched into
     one exact evaluation per tree leaf, against one chain of the sequential
@@ -644,6 +671,10 @@ def run_nuts(torch, iters=2):
     tab = species_of(probe, 'PDF')[1]
     pot = PDFPotential([79] * 1000, target, None, conv=100., n_configs=64,
                        table=tab)
+    from pyiid_gb300 import autotune
+    x0 = torch.as_tensor(starts.reshape(-1, 3).astype(np.float32),
+                         device='cuda')
+    autotune.tune_call(lambda: pot.evaluate(x0), reps=2)
     out = {'workload': 'NUTS, 64 chains x 1000-atom fcc Au, 300 K, '
                        'E = 100 Rw, escape depth 6'}
     t = time.perf_counter()

@@ -20,7 +20,8 @@ import torch
 from . import debye
 from ._native import context, load, KERNELS
 
-__all__ = ['variants', 'tune', 'apply_cached', 'cache_path']
+__all__ = ['variants', 'tune', 'tune_call', 'variant_scope', 'apply_cached',
+           'cache_path']
 
 
 def cache_path():
@@ -113,6 +114,44 @@ def tune(positions, species, scatter, qbin, k_begin=0,
     if save:
         _save_cache(cache)
     return result
+
+
+def tune_call(fn, kernels=('fq', 'adjoint'), reps=3, device=None):
+    """Time ``fn()`` (any workload built on the pair kernels, e.g. a batched
+    PDFPotential.evaluate or batch_fq call) under every variant of
+    ``kernels`` in turn, keeping the fastest of each (the kernels are tuned
+    one after the other, the others at their current variant).
+
+    Returns {kernel: {'best': index, 'ms': {index: median ms}}}."""
+    ctx = context(device)
+    result = {}
+    for kern in kernels:
+        ms = {}
+        for idx, _ in variants(kern):
+            ctx.set_variant(kern, idx)
+            ms[idx] = _time(fn, reps)
+        best = min(ms, key=ms.get)
+        ctx.set_variant(kern, best)
+        result[kern] = {'best': best, 'ms': ms}
+    return result
+
+
+class variant_scope:
+    """Context manager restoring the device context's variants on exit
+    (variants are per context, so tuning one workload would otherwise
+    change the launch shapes of every later call)."""
+
+    def __init__(self, device=None):
+        self.ctx = context(device)
+
+    def __enter__(self):
+        self.saved = {k: self.ctx.get_variant(k) for k in KERNELS}
+        return self.ctx
+
+    def __exit__(self, *exc):
+        for k, v in self.saved.items():
+            self.ctx.set_variant(k, v)
+        return False
 
 
 def apply_cached(n_atoms, n_bins_computed, n_species, device=None):
