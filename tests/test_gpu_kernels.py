@@ -270,8 +270,25 @@ def test_autotune_selects_and_caches(D, tmp_path, monkeypatch):
     ctx.set_variant('grad_fq', 0)
     got = autotune.apply_cached(200, 300, 1)
     assert got == {'fq': res['fq']['best'], 'grad_fq': res['grad_fq']['best']}
-    ctx.set_variant('fq', 0)
+    ctx.set_variant('fq', DEFAULT_FQ_VARIANT)
     ctx.set_variant('grad_fq', 0)
+
+
+DEFAULT_FQ_VARIANT = 18
+
+
+def test_new_context_starts_on_the_group_reduction_variant(D):
+    from pyiid_gb300 import autotune
+    from pyiid_gb300._native import Context
+    ctx = Context(0)
+    try:
+        assert ctx.get_variant('fq') == DEFAULT_FQ_VARIANT
+        assert ctx.get_variant('grad_fq') == 0
+        assert ctx.get_variant('adjoint') == 0
+    finally:
+        ctx.close()
+    info = dict(autotune.variants('fq'))[DEFAULT_FQ_VARIANT]
+    assert (info['bins_per_thread'], info['pairs_per_thread']) == (24, -3)
 
 
 def test_batch_fq_uneven_alloys_matches_oracle(D):
