@@ -34,6 +34,12 @@ N_ATOMS, A_PT, SIGMA, SEED = 20000, 3.92, 0.02, 2
 QMIN, QMAX, QBIN = 0.5, 30.0, 0.02
 FLOPS_GRAD_TERM = 20   # flop-equivalents per unordered pair-bin of dF/dx
 FLOPS_F_TERM = 10      # ... of F(Q)
+# FP32 lane operations the packed dF/dx inner loop issues per ordered
+# pair-bin: per two bins 4 FFMA2/FADD2 of the recurrence and the derivative
+# factor plus 3 FFMA2 of the x, y, z accumulation, plus 1 FADD2 of the bin
+# factor (8 packed instructions = 16 lane operations per two bins).
+LANE_OPS_GRAD_LOOP = 8
+FP32_LANES_PER_SM = 128
 
 
 def workload(n_atoms=None):
@@ -240,7 +246,8 @@ def run_gpu(args, rank, world, local):
 
     workloads = {}
     if rank == 0 and not args.no_workloads:
-        for name, fn in (('batched_fq_256_alloys', run_batched),
+        for name, fn in (('fq_grad_au1000', run_fq_grad_au1000),
+                         ('batched_fq_256_alloys', run_batched),
                          ('hmc_64_chains_au1000', run_hmc),
                          ('delayed_acceptance_au1000', run_delayed_acceptance),
                          ('gcmc_au500', run_gcmc),
@@ -286,9 +293,30 @@ def run_gpu(args, rank, world, local):
         },
         'clocks': clk.summary(),
     }
+    line['roofline']['issue'] = issue_roofline(
+        torch, dev, pairs, k_ret, g_ms, line['clocks'].get('sm_mhz'),
+        line['roofline']['kernel'])
     if workloads:
         line['workloads'] = workloads
     return line
+
+
+def issue_roofline(torch, dev, pairs, k_ret, g_ms, sm_mhz, kernel):
+    """FP32 issue roofline of the dF/dx launch: lane operations its inner
+    loop issues per second (each unordered pair-bin is evaluated for both
+    atoms) over the SMs' FP32 lane capacity at the median SM clock sampled
+    during the timed region.  Seeds and pair records are not counted."""
+    if kernel != 'gradfq2_kernel' or not sm_mhz:
+        return None
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    achieved = 2 * pairs * k_ret * LANE_OPS_GRAD_LOOP / (g_ms * 1e-3) / 1e12
+    peak = sms * FP32_LANES_PER_SM * sm_mhz * 1e6 / 1e12
+    return {'lane_ops_per_ordered_pair_bin': LANE_OPS_GRAD_LOOP,
+            'achieved': achieved, 'peak': peak, 'unit': 'T lane-op/s',
+            'frac': achieved / peak,
+            'peak_source': f'{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x '
+                           f'{sm_mhz:.0f} MHz (median sampled clock)',
+            'counted': 'inner loop only (per-pair seeds and records excluded)'}
 
 
 def traffic_from_profile():
@@ -366,6 +394,97 @@ def _run_batched(torch, steps):
             'pair_bin_terms_per_s': pairs * 498 / (ms * 1e-3),
             'fq_variant': tuned['fq']['best'],
             'launch': 'CUDA graph replay: 1 pair-sum + 1 finishing kernel'}
+
+
+def run_fq_grad_au1000(torch, reps=100, cpu_reps=2):
+    """1,000-atom fcc Au (a = 4.08, sigma = 0.05, Q 0.1-25 step 0.05): exact
+    F(Q) + full dF/dx of one configuration per evaluation, device-resident
+    and end to end (host positions in, F and dF/dx back to pinned host), with
+    the launch shapes tuned on this size; beside it full evaluations of the
+    FP32 port of the reference CPU path on all host cores, same inputs."""
+    from pyiid_gb300 import autotune
+    with autotune.variant_scope():
+        return _run_fq_grad_au1000(torch, reps, cpu_reps)
+
+
+def _run_fq_grad_au1000(torch, reps, cpu_reps):
+    from pyiid_gb300 import autotune, debye, structures
+    from pyiid_gb300.scatter_factors import species_tables
+    n, qbin = 1000, 0.05
+    pos = structures.displaced(structures.fcc_nearest(4.08, n), 0.05, 4)
+    n_bins, k_begin = 500, 2
+    sp, tab, _ = species_tables([79] * n, qbin, n_bins)
+    pos_d = torch.as_tensor(pos, device='cuda')
+    fq = torch.empty(n_bins, dtype=torch.float32, device='cuda')
+    grad = torch.empty((n, 3, n_bins), dtype=torch.float32, device='cuda')
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device='cuda')
+
+    def evaluate():
+        debye.fq(pos_d, sp, tab, qbin, k_begin, out=fq)
+        debye.grad_fq(pos_d, sp, tab, qbin, k_begin, out=grad)
+
+    tuned = autotune.tune_call(evaluate, kernels=('fq', 'grad_fq'), reps=5)
+    for _ in range(3):
+        evaluate()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    torch.cuda.synchronize()
+    for s, e in ev:
+        flush.zero_()
+        s.record(stream)
+        evaluate()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([s.elapsed_time(e) for s, e in ev]))
+    h_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    h_pos.copy_(torch.as_tensor(pos))
+    h_fq = torch.empty(n_bins, dtype=torch.float32, pin_memory=True)
+    h_grad = torch.empty((n, 3, n_bins), dtype=torch.float32, pin_memory=True)
+    e2e = []
+    for i in range(reps + 1):
+        flush.zero_()
+        s, e = (torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True))
+        s.record(stream)
+        pos_d.copy_(h_pos, non_blocking=True)
+        evaluate()
+        h_fq.copy_(fq, non_blocking=True)
+        h_grad.copy_(grad, non_blocking=True)
+        e.record(stream)
+        e.synchronize()
+        if i:
+            e2e.append(s.elapsed_time(e))
+    e2e_ms = float(np.mean(e2e))
+    assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
+
+    from oracle import build_oracle, debye_c
+    build_oracle.build()
+    per_atom = tab[sp]
+    pairs = n * (n - 1) // 2
+    debye_c.port_tasks(pos, per_atom, qbin, 2048, pairs, True, True)
+    t = []
+    for _ in range(cpu_reps):
+        t0 = time.perf_counter()
+        _, _, used = debye_c.port_tasks(pos, per_atom, qbin, 2048, pairs,
+                                        True, True)
+        t.append(time.perf_counter() - t0)
+    cpu = 1.0 / float(np.mean(t))
+    gpu = 1e3 / ms
+    return {'workload': '1000-atom fcc Au, exact F(Q) + full dF/dx, '
+                        'Q 0.1-25 step 0.05 (498 bins returned)',
+            'pairs': pairs, 'ms_per_eval': ms, 'evals_per_s': gpu,
+            'e2e_evals_per_s': 1e3 / e2e_ms,
+            'e2e_bytes': {'h2d': int(h_pos.numel() * 4),
+                          'd2h': int((h_fq.numel() + h_grad.numel()) * 4)},
+            'variants': {k: v['best'] for k, v in tuned.items()},
+            'l2': 'flushed between timed evaluations (256 MiB write)',
+            'cpu_port': {'evals_per_s': cpu, 'cores': int(used),
+                         'sample': f'{cpu_reps} full evaluations (all pairs, '
+                                   f'F and dF/dx, {n_bins} bins) after one '
+                                   'warm-up'},
+            'gpu_over_cpu_port': gpu / cpu,
+            'e2e_over_cpu_port': 1e3 / e2e_ms / cpu}
 
 
 def run_hmc(torch, iters=6):
@@ -704,6 +823,7 @@ def _run_nuts(torch, iters):
 
 
 WORKLOADS = {
+    'fq_grad_au1000': lambda torch, **kw: run_fq_grad_au1000(torch, **kw),
     'batched_fq_256_alloys': lambda torch, **kw: run_batched(torch, **kw),
     'hmc_64_chains_au1000': lambda torch, **kw: run_hmc(torch, **kw),
     'delayed_acceptance_au1000':
