@@ -178,22 +178,30 @@ def run_gpu(args, rank, world, local):
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
     ctx = context(local)
 
-    def step():
+    def separate():
         debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
         debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
 
+    def fused():
+        debye.fq_grad(pos_d, sp, tab, QBIN, k_begin, out_fq=fq, out_grad=grad)
+
     for _ in range(args.warmup):
-        step()
+        separate()
+        fused()
     torch.cuda.synchronize()
     tuned = None
+    step = fused
     if not args.no_tune:
         from pyiid_gb300 import autotune
         res = autotune.tune(pos_d, sp, tab, QBIN, k_begin, reps=2)
+        res.update(autotune.tune_call(fused, kernels=('fq_grad',), reps=2))
         tuned = {k: dict(zip(('bins_per_thread', 'pairs_per_thread',
                               'threads'), autotune.variants(k)[v['best']][1]
                              .values())) for k, v in res.items()}
-        step()
+        # the faster of one pass (F and dF/dx together) and two passes
+        step = min((fused, separate), key=lambda fn: time_ms(torch, fn, 3))
         torch.cuda.synchronize()
+    one_pass = step is fused
     stream = torch.cuda.current_stream()
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)]
           for _ in range(args.steps)]
@@ -206,9 +214,13 @@ def run_gpu(args, rank, world, local):
         for i in range(args.steps):
             flush.zero_()
             ev[i][0].record(stream)
-            debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
-            ev[i][1].record(stream)
-            debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
+            if one_pass:
+                fused()
+                ev[i][1].record(stream)
+            else:
+                debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
+                ev[i][1].record(stream)
+                debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
             ev[i][2].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -232,8 +244,7 @@ def run_gpu(args, rank, world, local):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record(stream)
         pos_d.copy_(h_pos, non_blocking=True)
-        debye.fq(pos_d, sp, tab, QBIN, k_begin, out=fq)
-        debye.grad_fq(pos_d, sp, tab, QBIN, k_begin, out=grad)
+        step()
         h_fq.copy_(fq, non_blocking=True)
         h_grad.copy_(grad, non_blocking=True)
         e.record(stream)
@@ -264,7 +275,23 @@ def run_gpu(args, rank, world, local):
         return None
     g_ms = float(np.mean(t_g))
     f_ms = float(np.mean(t_f))
-    achieved = pairs * k_ret * FLOPS_GRAD_TERM / (g_ms * 1e-3) / 1e12
+    if one_pass:
+        # the F and dF/dx of a step come from one launch: its time is t_f
+        kernel = 'fqgrad2_kernel'
+        k_ms = f_ms
+        kernel_ms = {'fq_grad': f_ms}
+        flops_term = FLOPS_GRAD_TERM + FLOPS_F_TERM
+        # F(Q) adds 1 lane op per ordered pair-bin on the tiles J >= I
+        lane_ops = LANE_OPS_GRAD_LOOP + 0.5
+    else:
+        kernel = ('gradfq2_kernel' if (tuned is None or
+                                       tuned['grad_fq']['pairs_per_thread']
+                                       <= 0) else 'gradfq_kernel')
+        k_ms = g_ms
+        kernel_ms = {'fq': f_ms, 'grad_fq': g_ms}
+        flops_term = FLOPS_GRAD_TERM
+        lane_ops = LANE_OPS_GRAD_LOOP
+    achieved = pairs * k_ret * flops_term / (k_ms * 1e-3) / 1e12
     line = {
         'metric': METRIC, 'value': value, 'unit': 'evals/s', 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
@@ -272,8 +299,11 @@ def run_gpu(args, rank, world, local):
         'dtype': 'fp32 (FP64 final reductions)', 'data': 'synthetic (seeded fcc Pt)',
         'config': config_dict(n_bins, k_begin,
                               {'parallelism': f'replica x{world}',
-                               'launch_shapes': tuned or 'defaults'}, n),
-        'kernel_ms': {'fq': f_ms, 'grad_fq': g_ms},
+                               'launch_shapes': tuned or 'defaults',
+                               'path': ('one pass (pyiid_fq_grad)' if one_pass
+                                        else 'two passes (pyiid_fq, '
+                                             'pyiid_grad_fq)')}, n),
+        'kernel_ms': kernel_ms,
         'pair_bin_terms_per_s': 2 * pairs * k_ret / (ms_step * 1e-3),
         'wall_s_timed_region': wall,
         'gpu_launches': int(launches),
@@ -282,36 +312,35 @@ def run_gpu(args, rank, world, local):
                 'd2h_bytes_per_step': int(h_fq.numel() * 4 + h_grad.numel() * 4)},
         'roofline': {
             'bound': 'fp32',
-            'kernel': ('gradfq2_kernel' if (tuned is None or
-                                            tuned['grad_fq']['pairs_per_thread']
-                                            <= 0) else 'gradfq_kernel'),
+            'kernel': kernel,
             'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
             'frac': achieved / peak if peak else None,
             'peak_source': 'measured live: cuBLAS SGEMM 8192^3 (TF32 off)',
-            'algorithmic_flops_per_launch': pairs * k_ret * FLOPS_GRAD_TERM,
-            'traffic': traffic_from_profile(),
+            'algorithmic_flops_per_launch': pairs * k_ret * flops_term,
+            'traffic': traffic_from_profile(kernel),
         },
         'clocks': clk.summary(),
     }
     line['roofline']['issue'] = issue_roofline(
-        torch, dev, pairs, k_ret, g_ms, line['clocks'].get('sm_mhz'),
-        line['roofline']['kernel'])
+        torch, dev, pairs, k_ret, k_ms, line['clocks'].get('sm_mhz'), kernel,
+        lane_ops)
     if workloads:
         line['workloads'] = workloads
     return line
 
 
-def issue_roofline(torch, dev, pairs, k_ret, g_ms, sm_mhz, kernel):
-    """FP32 issue roofline of the dF/dx launch: lane operations its inner
-    loop issues per second (each unordered pair-bin is evaluated for both
-    atoms) over the SMs' FP32 lane capacity at the median SM clock sampled
-    during the timed region.  Seeds and pair records are not counted."""
-    if kernel != 'gradfq2_kernel' or not sm_mhz:
+def issue_roofline(torch, dev, pairs, k_ret, k_ms, sm_mhz, kernel, lane_ops):
+    """FP32 issue roofline of the dF/dx (or one-pass F + dF/dx) launch:
+    lane operations its inner loop issues per second (each unordered
+    pair-bin is evaluated for both atoms) over the SMs' FP32 lane capacity
+    at the median SM clock sampled during the timed region.  Seeds and pair
+    records are not counted."""
+    if kernel not in ('gradfq2_kernel', 'fqgrad2_kernel') or not sm_mhz:
         return None
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    achieved = 2 * pairs * k_ret * LANE_OPS_GRAD_LOOP / (g_ms * 1e-3) / 1e12
+    achieved = 2 * pairs * k_ret * lane_ops / (k_ms * 1e-3) / 1e12
     peak = sms * FP32_LANES_PER_SM * sm_mhz * 1e6 / 1e12
-    return {'lane_ops_per_ordered_pair_bin': LANE_OPS_GRAD_LOOP,
+    return {'lane_ops_per_ordered_pair_bin': lane_ops,
             'achieved': achieved, 'peak': peak, 'unit': 'T lane-op/s',
             'frac': achieved / peak,
             'peak_source': f'{sms} SMs x {FP32_LANES_PER_SM} FP32 lanes x '
@@ -319,9 +348,23 @@ def issue_roofline(torch, dev, pairs, k_ret, g_ms, sm_mhz, kernel):
             'counted': 'inner loop only (per-pair seeds and records excluded)'}
 
 
-def traffic_from_profile():
-    """DRAM bytes per gradfq launch from the committed ncu summary, if any."""
-    p = os.path.join(REPO, 'profiles', 'gradfq2_kernel_pt20000.md')
+def time_ms(torch, fn, reps):
+    """Mean CUDA-event time of fn() over reps calls after one warm call."""
+    fn()
+    s, e = (torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True))
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    e.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def traffic_from_profile(kernel):
+    """DRAM bytes per launch of the 20,000-atom workload's dominant kernel
+    from its committed ncu summary, if any."""
+    p = os.path.join(REPO, 'profiles', f'{kernel}_pt20000.md')
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -419,11 +462,16 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
     grad = torch.empty((n, 3, n_bins), dtype=torch.float32, device='cuda')
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device='cuda')
 
-    def evaluate():
+    def separate():
         debye.fq(pos_d, sp, tab, qbin, k_begin, out=fq)
         debye.grad_fq(pos_d, sp, tab, qbin, k_begin, out=grad)
 
-    tuned = autotune.tune_call(evaluate, kernels=('fq', 'grad_fq'), reps=5)
+    def fused():
+        debye.fq_grad(pos_d, sp, tab, qbin, k_begin, out_fq=fq, out_grad=grad)
+
+    tuned = autotune.tune_call(separate, kernels=('fq', 'grad_fq'), reps=5)
+    tuned.update(autotune.tune_call(fused, kernels=('fq_grad',), reps=5))
+    evaluate = min((fused, separate), key=lambda fn: time_ms(torch, fn, 5))
     for _ in range(3):
         evaluate()
     stream = torch.cuda.current_stream()
@@ -478,6 +526,8 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
             'e2e_bytes': {'h2d': int(h_pos.numel() * 4),
                           'd2h': int((h_fq.numel() + h_grad.numel()) * 4)},
             'variants': {k: v['best'] for k, v in tuned.items()},
+            'path': ('one pass (pyiid_fq_grad)' if evaluate is fused
+                     else 'two passes (pyiid_fq, pyiid_grad_fq)'),
             'l2': 'flushed between timed evaluations (256 MiB write)',
             'cpu_port': {'evals_per_s': cpu, 'cores': int(used),
                          'sample': f'{cpu_reps} full evaluations (all pairs, '

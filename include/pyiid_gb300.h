@@ -122,6 +122,20 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
                   int n_species, int n_bins, double qbin, int k_begin,
                   float *grad);
 
+/* F(Q) and its gradient from one pass over the pairs: fq as pyiid_fq and
+ * grad as pyiid_grad_fq return them (same conventions, same tolerances; the
+ * pair terms are summed in a different order).  The gradient kernel already
+ * generates sin(Q_k r) for every ordered pair and bin, so F(Q) costs one
+ * more packed FMA per two bins instead of a second pass.  Replaces the
+ * get_fq + get_grad_fq pair of calls a calculator makes on one
+ * configuration (elasticscatter/__init__.py:304-341 and :477-496).
+ *   fq   : device float [n_bins]
+ *   grad : device float [n_atoms][3][n_bins] */
+int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
+                  const int32_t *species, int n_atoms, const float *scatter,
+                  int n_species, int n_bins, double qbin, int k_begin,
+                  float *fq, float *grad);
+
 /* ------------------------------------------------------------------------ *
  * F(Q) -> G(r).
  *
@@ -410,7 +424,8 @@ int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy, float *g_w1,
  * the fastest.  No reference counterpart (the reference's numba launches are
  * fixed, atomics/gpu_atomics.py:120-184).
  *   kernel: PYIID_KERNEL_FQ (pyiid_fq and the F(Q) part of the batched call),
- *           PYIID_KERNEL_GRAD_FQ (pyiid_grad_fq) or PYIID_KERNEL_ADJOINT
+ *           PYIID_KERNEL_GRAD_FQ (pyiid_grad_fq), PYIID_KERNEL_FQ_GRAD
+ *           (pyiid_fq_grad) or PYIID_KERNEL_ADJOINT
  *           (the gradient of pyiid_batch_potential_grad: variant 0 evaluates
  *           each unordered pair once, variant 1 twice).
  *   params (pyiid_variant_info): {bins per thread, pairs per thread, threads
@@ -418,7 +433,12 @@ int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy, float *g_w1,
  *   kernels (0: one pair per thread at a time, -2: two interleaved, -3/-4:
  *   the per-tile-pair group reduction at 3/4 CTAs per SM).  A new context
  *   starts on F(Q) variant 18 ({24, -3, 256}), variant 0 of the others. */
-enum { PYIID_KERNEL_FQ = 0, PYIID_KERNEL_GRAD_FQ = 1, PYIID_KERNEL_ADJOINT = 2 };
+enum {
+  PYIID_KERNEL_FQ = 0,
+  PYIID_KERNEL_GRAD_FQ = 1,
+  PYIID_KERNEL_ADJOINT = 2,
+  PYIID_KERNEL_FQ_GRAD = 3
+};
 int pyiid_variant_count(int kernel);
 int pyiid_variant_info(int kernel, int variant, int *params, int n_params);
 int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant);

@@ -36,6 +36,8 @@ _SIGNATURES = {
                           _c_dbl, _c_int, _vp]),
     'pyiid_grad_fq': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
                                _c_int, _c_dbl, _c_int, _vp]),
+    'pyiid_fq_grad': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
+                               _c_int, _c_dbl, _c_int, _vp, _vp]),
     'pyiid_batch_fq': (_c_int, [_vp, _vp, _i32p, _i32p, _c_int, _f32p,
                                 _c_int, _c_int, _c_dbl, _c_int, _vp]),
     'pyiid_pdf': (_c_int, [_vp, _vp, _c_int, _c_int, _c_dbl, _c_dbl, _f64p,
@@ -82,7 +84,7 @@ _SIGNATURES = {
     'pyiid_get_variant': (_c_int, [_vp, _c_int]),
 }
 
-KERNELS = {'fq': 0, 'grad_fq': 1, 'adjoint': 2}
+KERNELS = {'fq': 0, 'grad_fq': 1, 'adjoint': 2, 'fq_grad': 3}
 
 
 class NativeError(RuntimeError):

@@ -62,6 +62,14 @@ struct GradEntry {
   GradVariant v;
   GradKernel k;
 };
+using FqGradKernel = void (*)(const float *, const int *, const int4 *,
+                              const int2 *, float, float, int, int, int,
+                              const float *, int, float *, const float *,
+                              double *);
+struct FqGradEntry {
+  GradVariant v;
+  FqGradKernel k;
+};
 
 // NP <= 0 marks the packed (FP32x2) even/odd kernels: 0 one pair per
 // thread at a time, -2 two pairs interleaved, -3 (and -4) the per-tile-pair
@@ -97,6 +105,19 @@ const GradEntry kGradTable[] = {
     {{24, 8, 1}, gradfq_kernel<24, 8, 1, 2>},
     {{16, 4, 1}, gradfq_kernel<16, 4, 1, 6>},
 };
+// F(Q) + dF/dx in one pass (packed kernels only)
+const FqGradEntry kFqGradTable[] = {
+    {{24, 8, 0}, fqgrad2_kernel<24, 8, 2>},
+    {{32, 8, 0}, fqgrad2_kernel<32, 8, 1>},
+    {{16, 8, 0}, fqgrad2_kernel<16, 8, 2>},
+    {{32, 16, 0}, fqgrad2_kernel<32, 16, 1>},
+    {{24, 16, 0}, fqgrad2_kernel<24, 16, 1>},
+};
+constexpr int kNumFqGrad = sizeof(kFqGradTable) / sizeof(kFqGradTable[0]);
+size_t fqgrad_smem(const GradVariant &v) {
+  return 3 * kTile * kTile * sizeof(float4) +
+         2 * (size_t)v.CPC * v.CPC * v.L * sizeof(float);
+}
 constexpr int kNumFq = sizeof(kFqTable) / sizeof(kFqTable[0]);
 // Default F(Q) launch shape of a new context: {24, -3}, the per-tile-pair
 // group reduction at 3 CTAs per SM.  It is the fastest shape on batches of
@@ -211,6 +232,7 @@ struct pyiid_ctx {
   int fq_variant = kDefaultFq;
   int grad_variant = 0;
   int adj_variant = 0;  // 0: symmetric (each pair once), 1: owner-computes
+  int fqgrad_variant = 0;
 };
 
 namespace {
@@ -581,6 +603,11 @@ int set_attrs(pyiid_ctx *ctx) {
                       kGradTable[i].k,
                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                       3 * kTile * kTile * (int)sizeof(float4)));
+  for (int i = 0; i < kNumFqGrad; ++i)
+    CUDA_TRY(ctx, cudaFuncSetAttribute(
+                      kFqGradTable[i].k,
+                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                      (int)fqgrad_smem(kFqGradTable[i].v)));
   for (int i = 0; i < kNumFq; ++i)
     CUDA_TRY(ctx, cudaFuncSetAttribute(
                       kFqTable[i].k,
@@ -807,6 +834,59 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
     LAUNCH_CHECK(ctx);
   }
   if (kbo > 0)
+    CUDA_TRY(ctx, cudaMemset2DAsync(grad, (size_t)n_bins * sizeof(float), 0,
+                                    (size_t)kbo * sizeof(float),
+                                    (size_t)3 * n_atoms, ctx->stream));
+  return PYIID_OK;
+}
+
+int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
+                  const int32_t *species, int n_atoms, const float *scatter,
+                  int n_species, int n_bins, double qbin, int k_begin,
+                  float *fq, float *grad) {
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  const int32_t offsets[2] = {0, n_atoms};
+  TRY(check_common(ctx, 1, offsets, n_species, n_bins, qbin, k_begin));
+  if (!fq || (!grad && n_atoms > 0))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "null output pointer");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  Layout *L;
+  TRY(get_layout(ctx, species, offsets, 1, n_species, &L));
+  float *d_ftab;
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, &d_ftab));
+  double *d_na;
+  TRY(get_na(ctx, L, scatter, n_bins, &d_na));
+  const int kbo = std::min(k_begin, n_bins);
+  const int kb0 = kbo & ~1;
+  const int n_tiles = (int)L->tiles.size();
+  double *fpart = nullptr;
+  if (n_atoms > 0 && kb0 < n_bins) {
+    void *p;
+    TRY(ensure(ctx, "coef",
+               (size_t)n_species * n_species * n_bins * sizeof(float), &p));
+    float *coef = static_cast<float *>(p);
+    gradfq_coef_kernel<<<64, 256, 0, ctx->stream>>>(d_na, d_ftab, n_species,
+                                                    n_bins, 1, coef);
+    LAUNCH_CHECK(ctx);
+    TRY(ensure(ctx, "fqgrad_part", (size_t)n_tiles * n_bins * sizeof(double),
+               &p));
+    fpart = static_cast<double *>(p);
+    const FqGradEntry &E = kFqGradTable[ctx->fqgrad_variant];
+    const int Lb = E.v.L, cpc = E.v.CPC;
+    const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    float dq_hi, dq_lo;
+    split_double(qbin, dq_hi, dq_lo);
+    dim3 grid((unsigned)n_tiles, (chunks_total + cpc - 1) / cpc);
+    E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
+        positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
+        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart);
+    LAUNCH_CHECK(ctx);
+  }
+  fqgrad_finish_kernel<<<(n_bins + 127) / 128, 128, 0, ctx->stream>>>(
+      fpart, 0, fpart ? n_tiles : 0, d_na, n_bins, fpart ? kbo : n_bins, fq);
+  LAUNCH_CHECK(ctx);
+  if (kbo > 0 && n_atoms > 0)
     CUDA_TRY(ctx, cudaMemset2DAsync(grad, (size_t)n_bins * sizeof(float), 0,
                                     (size_t)kbo * sizeof(float),
                                     (size_t)3 * n_atoms, ctx->stream));
@@ -1371,6 +1451,8 @@ int pyiid_variant_count(int kernel) {
       return kNumGrad;
     case PYIID_KERNEL_ADJOINT:
       return 2;
+    case PYIID_KERNEL_FQ_GRAD:
+      return kNumFqGrad;
     default:
       return -1;
   }
@@ -1389,6 +1471,12 @@ int pyiid_variant_info(int kernel, int variant, int *params, int n_params) {
     params[0] = kGradTable[variant].v.L;
     params[1] = kGradTable[variant].v.NP;
     params[2] = kTile * kGradTable[variant].v.CPC;
+    return PYIID_OK;
+  }
+  if (kernel == PYIID_KERNEL_FQ_GRAD && variant >= 0 && variant < kNumFqGrad) {
+    params[0] = kFqGradTable[variant].v.L;
+    params[1] = kFqGradTable[variant].v.NP;
+    params[2] = kTile * kFqGradTable[variant].v.CPC;
     return PYIID_OK;
   }
   if (kernel == PYIID_KERNEL_ADJOINT && (variant == 0 || variant == 1)) {
@@ -1411,6 +1499,8 @@ int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant) {
     ctx->fq_variant = variant;
   else if (kernel == PYIID_KERNEL_GRAD_FQ)
     ctx->grad_variant = variant;
+  else if (kernel == PYIID_KERNEL_FQ_GRAD)
+    ctx->fqgrad_variant = variant;
   else
     ctx->adj_variant = variant;
   return PYIID_OK;
@@ -1421,6 +1511,7 @@ int pyiid_get_variant(const pyiid_ctx *ctx, int kernel) {
   if (kernel == PYIID_KERNEL_FQ) return ctx->fq_variant;
   if (kernel == PYIID_KERNEL_GRAD_FQ) return ctx->grad_variant;
   if (kernel == PYIID_KERNEL_ADJOINT) return ctx->adj_variant;
+  if (kernel == PYIID_KERNEL_FQ_GRAD) return ctx->fqgrad_variant;
   return -1;
 }
 

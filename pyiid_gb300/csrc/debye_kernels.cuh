@@ -656,28 +656,52 @@ __global__ void __launch_bounds__(kBlock, MINB)
 // dF/dx, packed.  Records per (a, b), stored [b][a]:
 //   a = (th_hi, th_lo, kappa, sigma2)
 //   b = (beta ch, beta sh, beta, gamma')   beta = -1/r^3, gamma' = -r dq/(2 ch)
-//   c = (dx, dy, dz, 0)
+//   c = (dx, dy, dz, -r^2)
 // Per two bins and ordered pair: FFMA2 (w) + FADD2 (u) + FFMA2 (g) +
 // 3 FFMA2 (accumulate) + FFMA2 (t) + FADD2 (k gamma') = 8 instructions.
-template <int L, int CPC, int MINB>
-__global__ void __launch_bounds__(kTile * CPC, MINB)
-    gradfq2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
-                   const int4 *__restrict__ tiles,
-                   const int2 *__restrict__ cfg_tiles, float dq_hi,
-                   float dq_lo, int kb0, int chunks_total, int n_bins,
-                   const float *__restrict__ coef, int n_species,
-                   float *__restrict__ out) {
+//
+// WITH_F also returns the F(Q) pair sums of the same pass.  The recurrence
+// variable t_m = beta sin(phi + m theta2) gives the Debye term
+// sin(Q_k r)/r = sigma2^m t_m (-r^2): one more FFMA2 per two bins into
+// per-thread FP32 sums af, taken only on tiles J >= I so that every
+// unordered pair is counted once (the diagonal tile holds both orders of its
+// pairs and is weighted 1/2).  Every kFGroup J tiles (at each change of the
+// J species, and alone for the diagonal tile) the sums of the warp's atoms
+// are combined by shuffles and added, times f_sa f_sb, to the warp's row of
+// shared memory with Kahan-compensated FP32 additions (FP64 arithmetic is
+// too slow on this part to run per flush); the CTA writes the FP64
+// fixed-order sum of its warps' rows to fpart[tile I][k], and
+// S_k = sum_I fpart[I][k].
+constexpr int kFGroup = 4;
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
+
+template <int L, int CPC, bool WITH_F>
+__device__ __forceinline__ void gradfq2_body(
+    const float *__restrict__ pos, const int *__restrict__ perm,
+    const int4 *__restrict__ tiles, const int2 *__restrict__ cfg_tiles,
+    float dq_hi, float dq_lo, int kb0, int chunks_total, int n_bins,
+    const float *__restrict__ coef, int n_species, float *__restrict__ out,
+    const float *__restrict__ ftab, double *__restrict__ fpart) {
   static_assert(L % 2 == 0, "L must be even");
+  static_assert(32 % CPC == 0, "a warp must hold whole atoms");
   constexpr int M = L / 2;
   extern __shared__ float4 smem[];
   float4 *recA = smem;
   float4 *recB = smem + kTile * kTile;
   float4 *recC = smem + 2 * kTile * kTile;
+  // WITH_F: per warp [CPC][L] FP32 F(Q) sums and their Kahan compensations
+  // behind the records
+  float *fsum = reinterpret_cast<float *>(smem + 3 * kTile * kTile);
+  float *fcmp = fsum + CPC * CPC * L;
   __shared__ float4 sI[kTile], sJ[kTile];
 
   const int4 ti = tiles[blockIdx.x];
   const int2 ct = cfg_tiles[ti.z];
   const int tid = threadIdx.x;
+  const int lane = tid & 31;
   const int al = tid / CPC;
   const int chunk = blockIdx.y * CPC + tid % CPC;
   const bool active = (al < ti.y) && (chunk < chunks_total);
@@ -685,15 +709,20 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
   const float kf = (float)kbase;
 
   if (tid < ti.y) sI[tid] = load_atom(pos, perm, ti.x + tid);
+  if constexpr (WITH_F)
+    for (int i = tid; i < 2 * CPC * CPC * L; i += blockDim.x) fsum[i] = 0.f;
 
   float2 ax[M], ay[M], az[M];
+  float2 af[M];
 #pragma unroll
   for (int m = 0; m < M; ++m) {
     ax[m] = f2(0.f);
     ay[m] = f2(0.f);
     az[m] = f2(0.f);
+    if constexpr (WITH_F) af[m] = f2(0.f);
   }
   int cur_sb = -1;
+  int f_tiles = 0, f_sb = 0;
   bool first_flush = true;
   const int out_row = active ? perm[ti.x + al] : 0;
 
@@ -734,9 +763,52 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
     first_flush = false;
   };
 
+  // all threads take part (shuffles); lanes < CPC end with their chunk's sum
+  auto flush_f = [&](int sb, float scale) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+#pragma unroll
+      for (int off = CPC; off < 32; off *= 2) {
+        af[m].x += __shfl_xor_sync(0xffffffffu, af[m].x, off);
+        af[m].y += __shfl_xor_sync(0xffffffffu, af[m].y, off);
+      }
+    }
+    if (lane < CPC) {
+      const int kb = kb0 + (blockIdx.y * CPC + lane) * L;
+      const int r0 = (tid >> 5) * CPC * L + lane * L;
+      const float *fa = ftab + (size_t)ti.w * n_bins;
+      const float *fb = ftab + (size_t)sb * n_bins;
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          const int k = kb + 2 * m + e;
+          if (k < n_bins) {
+            const float y = __fsub_rn(
+                __fmul_rn(__fmul_rn(fa[k], fb[k]),
+                          scale * (e ? af[m].y : af[m].x)),
+                fcmp[r0 + 2 * m + e]);
+            const float s0 = fsum[r0 + 2 * m + e];
+            const float s1 = __fadd_rn(s0, y);
+            fcmp[r0 + 2 * m + e] = __fsub_rn(__fsub_rn(s1, s0), y);
+            fsum[r0 + 2 * m + e] = s1;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) af[m] = f2(0.f);
+  };
+
   for (int tj = ct.x; tj < ct.y; ++tj) {
     const int4 tJ = tiles[tj];
     if (cur_sb >= 0 && tJ.w != cur_sb) flush(cur_sb, false);
+    if constexpr (WITH_F) {
+      if (f_tiles > 0 && (tJ.w != f_sb || f_tiles == kFGroup)) {
+        flush_f(f_sb, 1.f);
+        f_tiles = 0;
+      }
+    }
     cur_sb = tJ.w;
     __syncthreads();
     if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
@@ -757,14 +829,15 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
         const float gam = -p.r * dq_hi / (2.0f * p.ch);
         ra = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
         rb = make_float4(beta * p.ch, beta * p.sh, beta, gam);
-        rc = make_float4(dx, dy, dz, 0.f);
+        rc = make_float4(dx, dy, dz, WITH_F ? -(p.r * p.r) : 0.f);
       }
       recA[q] = ra;
       recB[q] = rb;
       recC[q] = rc;
     }
     __syncthreads();
-    if (active) {
+    auto pair_loop = [&](auto use_f) {
+      constexpr bool UF = WITH_F && decltype(use_f)::value;
       for (int b = 0; b < tJ.y; ++b) {
         const int q = b * kTile + al;
         const float4 ra = recA[q];
@@ -780,6 +853,7 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
         const float2 dx2 = f2(rc.x), dy2 = f2(rc.y), dz2 = f2(rc.z);
         const float2 sx2 = f2(ra.w * rc.x), sy2 = f2(ra.w * rc.y),
                      sz2 = f2(ra.w * rc.z);
+        const float2 fe2 = f2(rc.w), fo2 = f2(ra.w * rc.w);
 #pragma unroll
         for (int m = 0; m < M; ++m) {
           const float2 wn = __ffma2_rn(km, t, w);
@@ -789,19 +863,97 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
             ax[m] = __ffma2_rn(gk, sx2, ax[m]);
             ay[m] = __ffma2_rn(gk, sy2, ay[m]);
             az[m] = __ffma2_rn(gk, sz2, az[m]);
+            if constexpr (UF) af[m] = __ffma2_rn(t, fo2, af[m]);
           } else {
             ax[m] = __ffma2_rn(gk, dx2, ax[m]);
             ay[m] = __ffma2_rn(gk, dy2, ay[m]);
             az[m] = __ffma2_rn(gk, dz2, az[m]);
+            if constexpr (UF) af[m] = __ffma2_rn(t, fe2, af[m]);
           }
           t = __ffma2_rn(kp, wn, t);
           w = wn;
           kg = __fadd2_rn(kg, dkg);
         }
       }
+    };
+    const bool count_f = WITH_F && tj >= (int)blockIdx.x;
+    if (active) {
+      if (count_f)
+        pair_loop(BoolTag<true>());
+      else
+        pair_loop(BoolTag<false>());
+    }
+    if constexpr (WITH_F) {
+      if (same) {
+        flush_f(tJ.w, 0.5f);
+      } else if (count_f) {
+        f_sb = tJ.w;
+        ++f_tiles;
+      }
     }
   }
   if (cur_sb >= 0) flush(cur_sb, true);
+  if constexpr (WITH_F) {
+    if (f_tiles > 0) flush_f(f_sb, 1.f);
+    __syncthreads();
+    for (int i = tid; i < CPC * L; i += blockDim.x) {
+      const int c = i / L;
+      const int ch = blockIdx.y * CPC + c;
+      const int k = kb0 + ch * L + i % L;
+      if (ch < chunks_total && k < n_bins) {
+        double sum = 0.0;
+        for (int wp = 0; wp < CPC; ++wp)
+          sum += (double)fsum[wp * CPC * L + i] - (double)fcmp[wp * CPC * L + i];
+        fpart[(size_t)blockIdx.x * n_bins + k] = sum;
+      }
+    }
+  }
+}
+
+template <int L, int CPC, int MINB>
+__global__ void __launch_bounds__(kTile * CPC, MINB)
+    gradfq2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                   const int4 *__restrict__ tiles,
+                   const int2 *__restrict__ cfg_tiles, float dq_hi,
+                   float dq_lo, int kb0, int chunks_total, int n_bins,
+                   const float *__restrict__ coef, int n_species,
+                   float *__restrict__ out) {
+  gradfq2_body<L, CPC, false>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
+                              chunks_total, n_bins, coef, n_species, out,
+                              nullptr, nullptr);
+}
+
+// F(Q) pair sums and dF/dx in one pass (see gradfq2_body).  Dynamic shared
+// memory: 3 kTile^2 float4 records + 2 CPC * CPC * L floats.
+template <int L, int CPC, int MINB>
+__global__ void __launch_bounds__(kTile * CPC, MINB)
+    fqgrad2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                   const int4 *__restrict__ tiles,
+                   const int2 *__restrict__ cfg_tiles, float dq_hi,
+                   float dq_lo, int kb0, int chunks_total, int n_bins,
+                   const float *__restrict__ coef, int n_species,
+                   float *__restrict__ out, const float *__restrict__ ftab,
+                   double *__restrict__ fpart) {
+  gradfq2_body<L, CPC, true>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
+                             chunks_total, n_bins, coef, n_species, out, ftab,
+                             fpart);
+}
+
+// F(Q) of the fused pass: S_k = sum over the tiles [t0, t1) of the
+// configuration of fpart[tile][k] (fixed order), F_k as fq_finish_kernel.
+__global__ void fqgrad_finish_kernel(const double *__restrict__ fpart,
+                                     int t0, int t1, const double *__restrict__ na,
+                                     int n_bins, int kb_out,
+                                     float *__restrict__ fq) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_bins) return;
+  float v = 0.f;
+  if (k >= kb_out) {
+    double s = 0.0;
+    for (int t = t0; t < t1; ++t) s += fpart[(size_t)t * n_bins + k];
+    v = fq_value(s, na[k]);
+  }
+  fq[k] = v;
 }
 
 // =================================================================== adjoint

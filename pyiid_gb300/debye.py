@@ -10,7 +10,7 @@ import torch
 
 from ._native import context, POTENTIALS, NativeError
 
-__all__ = ['fq', 'batch_fq', 'grad_fq', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
+__all__ = ['fq', 'batch_fq', 'grad_fq', 'fq_grad', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
            'batch_potential_grad', 'as_positions', 'mh_init', 'mh_steps',
            'mh_state_size', 'mh_views', 'mc_propose', 'mc_accept',
            'MOVE_DISPLACE', 'MOVE_INSERT', 'MOVE_REMOVE']
@@ -113,6 +113,39 @@ def grad_fq(positions, species, scatter, qbin, k_begin=0, out=None):
              tab.shape[0], tab.shape[1], float(qbin), int(k_begin),
              ctypes.c_void_p(out.data_ptr()))
     return out
+
+
+def fq_grad(positions, species, scatter, qbin, k_begin=0, out_fq=None,
+            out_grad=None):
+    """F(Q) [K] and the reference-convention gradient [N, 3, K] from one
+    pass over the pairs (pyiid_fq_grad): the values fq() and grad_fq()
+    return, with the pair terms summed in another order."""
+    import ctypes
+    pos = as_positions(positions)
+    n = pos.shape[0]
+    sp = _np(species, np.int32)
+    tab = _np(scatter, np.float32)
+    k = tab.shape[1]
+    if out_fq is None:
+        out_fq = torch.empty(k, dtype=torch.float32, device=pos.device)
+    else:
+        _check_dev(out_fq, 'out_fq', torch.float32)
+        if out_fq.numel() != k:
+            raise NativeError(f'out_fq must hold {k} floats')
+    if out_grad is None:
+        out_grad = torch.empty((n, 3, k), dtype=torch.float32,
+                               device=pos.device)
+    else:
+        _check_dev(out_grad, 'out_grad', torch.float32)
+        if out_grad.numel() != n * 3 * k:
+            raise NativeError(f'out_grad must hold {n} x 3 x {k} floats')
+    ctx = context(pos.device.index)
+    ctx.call('pyiid_fq_grad', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
+             tab.shape[0], k, float(qbin), int(k_begin),
+             ctypes.c_void_p(out_fq.data_ptr()),
+             ctypes.c_void_p(out_grad.data_ptr()))
+    return out_fq, out_grad
 
 
 def pdf(fq_t, qstep, rstep, rgrid, qmin):

@@ -1,0 +1,173 @@
+"""One-pass F(Q) + gradient (pyiid_fq_grad) against the FP64 oracle and
+against the separate F(Q) and gradient calls.
+
+Tolerances as the separate calls' (norm-wise relative to the oracle):
+F(Q) <= 1e-5, gradient <= 1e-4.  The fused F(Q) takes every unordered pair
+once (tiles J >= I, the diagonal tile's two orders at weight 1/2), sums
+groups of 4 J tiles in FP32 and beyond that with compensation, so it agrees
+with pyiid_fq to rounding, not bitwise.
+"""
+import numpy as np
+import pytest
+
+from oracle import debye_np as O
+from pyiid_gb300 import structures as S
+from pyiid_gb300.scatter_factors import species_tables
+
+pytestmark = pytest.mark.gpu
+
+TOL_F = 1e-5
+TOL_G = 1e-4
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope='module')
+def D():
+    from pyiid_gb300 import debye
+    return debye
+
+
+def alloy(n, seed, edge):
+    nums = list(np.random.default_rng(seed).choice([78, 79], n))
+    return S.random_cube(n, edge, seed), nums
+
+
+CASES = [
+    ('au2', np.array([[0, 0, 0], [3, 0, 0]], np.float32), [79, 79]),
+    ('rand77', S.random_cube(77, 14.0, 2), [79] * 77),
+    ('alloy50', *alloy(50, 3, 12.0)),
+    # more than 4 J tiles of one species (the FP32 groups are flushed
+    # inside a species block) and a species change after a partial group
+    ('fcc249', S.displaced(S.fcc_sphere(4.08, 10.0), 0.05, 1), [79] * 249),
+    ('alloy300', *alloy(300, 5, 18.0)),
+    ('three_species', S.random_cube(170, 16.0, 7),
+     list(np.random.default_rng(7).choice([46, 78, 79], 170))),
+]
+
+
+@pytest.mark.parametrize('name,pos,numbers', CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize('qbin,nbins,kb', [(0.05, 500, 2), (0.1, 250, 3)])
+def test_fq_grad_matches_oracle(D, name, pos, numbers, qbin, nbins, kb):
+    sp, tab, _ = species_tables(numbers, qbin, nbins)
+    f, g = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
+    f, g = f.cpu().numpy(), g.cpu().numpy()
+    want_f = O.fq(pos, tab[sp], qbin)
+    want_g = O.grad_fq(pos, tab[sp], qbin)
+    assert np.all(f[:kb] == 0) and np.all(g[:, :, :kb] == 0)
+    assert rel(f[kb:], want_f[kb:]) <= TOL_F, rel(f[kb:], want_f[kb:])
+    assert rel(g[:, :, kb:], want_g[:, :, kb:]) <= TOL_G
+
+
+def test_fq_grad_agrees_with_the_separate_calls(D):
+    pos, nums = alloy(260, 11, 17.0)
+    qbin, nb, kb = 0.05, 500, 2
+    sp, tab, _ = species_tables(nums, qbin, nb)
+    f, g = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
+    f1 = D.fq(pos, sp, tab, qbin, k_begin=kb)
+    g1 = D.grad_fq(pos, sp, tab, qbin, k_begin=kb)
+    assert rel(f.cpu().numpy(), f1.cpu().numpy()) <= 1e-6
+    assert rel(g.cpu().numpy(), g1.cpu().numpy()) <= 1e-6
+
+
+def test_every_fq_grad_variant_matches_oracle(D):
+    from pyiid_gb300 import autotune
+    from pyiid_gb300._native import context
+    pos, nums = alloy(140, 21, 14.0)
+    qbin, nb, kb = 0.05, 500, 3
+    sp, tab, _ = species_tables(nums, qbin, nb)
+    want_f = O.fq(pos, tab[sp], qbin)
+    want_g = O.grad_fq(pos, tab[sp], qbin)
+    ctx = context()
+    old = ctx.get_variant('fq_grad')
+    try:
+        for idx, info in autotune.variants('fq_grad'):
+            ctx.set_variant('fq_grad', idx)
+            f, g = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
+            f, g = f.cpu().numpy(), g.cpu().numpy()
+            assert rel(f[kb:], want_f[kb:]) <= TOL_F, (idx, info)
+            assert rel(g[:, :, kb:], want_g[:, :, kb:]) <= TOL_G, (idx, info)
+    finally:
+        ctx.set_variant('fq_grad', old)
+
+
+def test_fq_grad_edge_cases(D):
+    qbin, nb = 0.1, 250
+    sp1, tab1, _ = species_tables([79], qbin, nb)
+    for n in (0, 1):
+        f, g = D.fq_grad(np.zeros((n, 3), np.float32), sp1[:n], tab1, qbin)
+        assert f.shape == (nb,) and np.all(f.cpu().numpy() == 0)
+        assert g.shape == (n, 3, nb) and np.all(g.cpu().numpy() == 0)
+    # coincident atoms: F is 0 in every bin, their gradient rows are 0
+    pos = np.array([[0, 0, 0], [0, 0, 0], [3, 0, 0]], np.float32)
+    sp3, tab3, _ = species_tables([79] * 3, qbin, nb)
+    f, g = D.fq_grad(pos, sp3, tab3, qbin)
+    assert np.all(f.cpu().numpy() == 0)
+    g = g.cpu().numpy()
+    want = O.grad_fq(pos, tab3[sp3], qbin)
+    assert np.all(g[:2] == 0)
+    assert rel(g[2], want[2]) <= TOL_G
+    # k_begin at and beyond the grid: everything 0
+    pos2 = S.random_cube(10, 5.0, 9)
+    sp, tab, _ = species_tables([79] * 10, qbin, nb)
+    for kb in (nb, nb + 5):
+        f, g = D.fq_grad(pos2, sp, tab, qbin, k_begin=kb)
+        assert np.all(f.cpu().numpy() == 0) and np.all(g.cpu().numpy() == 0)
+
+
+def test_fq_grad_repeatable_bitwise(D):
+    pos, nums = alloy(200, 4, 15.0)
+    sp, tab, _ = species_tables(nums, 0.05, 500)
+    a = [t.cpu().numpy() for t in D.fq_grad(pos, sp, tab, 0.05)]
+    b = [t.cpu().numpy() for t in D.fq_grad(pos, sp, tab, 0.05)]
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_fq_grad_rejects_wrong_output_sizes(D):
+    import torch
+    from pyiid_gb300._native import NativeError
+    pos = S.random_cube(8, 5.0, 1)
+    sp, tab, _ = species_tables([79] * 8, 0.1, 50)
+    with pytest.raises(NativeError):
+        D.fq_grad(pos, sp, tab, 0.1,
+                  out_fq=torch.empty(49, dtype=torch.float32, device='cuda'))
+    with pytest.raises(NativeError):
+        D.fq_grad(pos, sp, tab, 0.1,
+                  out_grad=torch.empty((8, 3, 49), dtype=torch.float32,
+                                       device='cuda'))
+
+
+def test_fq_grad_large_particle_sampled(D):
+    """2000-atom fcc Pt on the Q 0.5-30 step 0.02 grid: F(Q) on every 16th
+    bin and the full gradient rows of 12 seeded atoms against FP64 sums."""
+    pos = S.displaced(S.fcc_nearest(3.92, 2000), 0.02, 2)
+    qbin, nb, kb = 0.02, 1500, 25
+    sp, tab, _ = species_tables([78] * len(pos), qbin, nb)
+    f, g = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
+    f, g = f.cpu().numpy(), g.cpu().numpy()
+    q = pos.astype(np.float32).astype(np.float64)
+    fa = tab[0].astype(np.float64)
+    na = O.normalization(tab[sp])
+    idx = np.arange(kb, nb, 16)
+    Q = idx * qbin
+    s = np.zeros(len(idx))
+    for i0 in range(1, len(q)):
+        d = np.sqrt(((q[i0] - q[:i0]) ** 2).sum(1))
+        s += (np.sin(Q[None] * d[:, None]) / d[:, None]).sum(0)
+    want_f = 2 * s * fa[idx] ** 2 / na[idx]
+    assert rel(f[idx], want_f) <= TOL_F, rel(f[idx], want_f)
+    Qa = np.arange(nb) * qbin
+    rows = np.random.default_rng(12).choice(len(q), 12, replace=False)
+    for a in rows:
+        d = q[a] - np.delete(q, a, axis=0)            # [N-1, 3]
+        r = np.sqrt((d * d).sum(1))[:, None]
+        qr = Qa[None] * r
+        w = (Qa[None] * np.cos(qr) - np.sin(qr) / r) / r ** 2
+        want = -(fa * fa)[None, :] * np.einsum('jk,jc->ck', w, d) / na
+        assert rel(g[a, :, kb:], want[:, kb:]) <= TOL_G, (a, rel(g[a, :, kb:],
+                                                                 want[:, kb:]))
