@@ -88,6 +88,8 @@ const FqEntry kFqTable[] = {
     {{32, -3}, fq_pair3_kernel<32, 3>}, {{32, -4}, fq_pair3_kernel<32, 4>},
     {{24, -3}, fq_pair3_kernel<24, 3>}, {{24, -4}, fq_pair3_kernel<24, 4>},
     {{16, -4}, fq_pair3_kernel<16, 4>},
+    {{48, -3}, fq_pair3_kernel<48, 3>}, {{40, -3}, fq_pair3_kernel<40, 3>},
+    {{56, -3}, fq_pair3_kernel<56, 3>},
 };
 // (the last template argument is the minimum resident CTAs per SM, i.e. the
 // register budget: 2 x 256 threads -> 128 registers, 3 x 256 -> 85)
@@ -116,7 +118,7 @@ const FqGradEntry kFqGradTable[] = {
 constexpr int kNumFqGrad = sizeof(kFqGradTable) / sizeof(kFqGradTable[0]);
 size_t fqgrad_smem(const GradVariant &v) {
   return 3 * kTile * kTile * sizeof(float4) +
-         2 * (size_t)v.CPC * v.CPC * v.L * sizeof(float);
+         (2 * (size_t)v.CPC * v.CPC * v.L + kTile * kTile) * sizeof(float);
 }
 constexpr int kNumFq = sizeof(kFqTable) / sizeof(kFqTable[0]);
 // Default F(Q) launch shape of a new context: {24, -3}, the per-tile-pair
@@ -131,7 +133,7 @@ constexpr int kNumGrad = sizeof(kGradTable) / sizeof(kGradTable[0]);
 size_t fq_smem(const FqVariant &v, int n_chunks = -1) {
   if (v.NP <= -3) {  // records / group scratch + FP64 per-bin accumulators
     const size_t acc = n_chunks < 0 ? 32768 : (size_t)n_chunks * v.L * 8;
-    return 2 * kTile * kTile * sizeof(float4) + acc;
+    return (size_t)fq3_scratch_floats(v.L) * sizeof(float) + acc;
   }
   return 2 * kTile * kTile * sizeof(float4) +
          2 * (size_t)v.L * kBlock * sizeof(float);

@@ -413,7 +413,9 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
 // Same work decomposition as the kernels above, on the even/odd formulation
 // of pair_math.cuh: one packed instruction advances bins k and k+1.
 // F(Q) per two bins and pair: FFMA2 + FFMA2 (recurrence) + FADD2/FFMA2.
-// Records: a = (th_hi, th_lo, kappa, sigma2), b = (ch/r, sh/r, 1/r, 0).
+// Records: a = (th_hi, th_lo, kappa, sigma2), b = (ch/r, sin theta, 1/r,
+// cos theta); sh/r is (kappa/2)/r, and the odd slot's seed is the even one
+// rotated by theta (seed_sincos2r).
 // NP = 2: each thread advances two pairs together (independent recurrence
 // chains for the FMA pipe; the two-FMA dependency of one chain is what
 // limits NP = 1); a missing second pair has zero records.
@@ -470,7 +472,7 @@ __global__ void __launch_bounds__(kBlock, 2)
       PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
                                  dq_lo, dx, dy, dz);
       recA[q] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
-      recB[q] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
+      recB[q] = make_float4(p.ch * p.inv_r, p.sth, p.inv_r, p.cth);
     }
     __syncthreads();
     if (active && np > 0) {
@@ -486,9 +488,11 @@ __global__ void __launch_bounds__(kBlock, 2)
           const float4 ra = recA[ok ? qq : q];
           const float4 rb = ok ? recB[qq] : make_float4(0.f, 0.f, 0.f, 0.f);
           float2 s, co;
-          seed_sincos2(kf, ra.x, ra.y, s, co);
+          seed_sincos2r(kf, ra.x, ra.y, rb.y, rb.w, s, co);
+          // sh / r = (kappa / 2) / r, bitwise the product the record held
+          const float shr = __fmul_rn(0.5f * ra.z, rb.z);
           t[p] = __fmul2_rn(f2(rb.z), s);
-          w[p] = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+          w[p] = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(shr)));
           kp[p] = f2(ra.z);
           km[p] = f2(-ra.z);
           sg[p] = f2(ra.w);
@@ -545,13 +549,20 @@ __global__ void __launch_bounds__(kBlock, 2)
   }
 }
 
+// Floats of the record / group-scratch region of fq_pair3_kernel: the two
+// record arrays, or n_groups * n_chunks * L <= kBlock * L group sums.
+__host__ __device__ constexpr int fq3_scratch_floats(int L) {
+  return kBlock * L > 2 * kTile * kTile * 4 ? kBlock * L
+                                            : 2 * kTile * kTile * 4;
+}
+
 // F(Q) pair sums with the group reduction done per tile pair: after each
 // tile pair the groups' FP32 register sums go through the (then idle)
 // record buffer, are added in a fixed order and accumulated per bin in FP64
 // shared memory.  No per-thread compensated sums are kept, so the kernel
 // fits MINB CTAs per SM (e.g. 4 x 256 threads at <= 64 registers) instead
-// of two.  Dynamic shared memory: 2*32*32 float4 records (>= n_groups *
-// n_chunks * L floats of group scratch) + n_chunks * L doubles.
+// of two.  Dynamic shared memory: fq3_scratch_floats(L) floats of records
+// and group scratch + n_chunks * L doubles.
 template <int L, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB)
     fq_pair3_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
@@ -560,14 +571,12 @@ __global__ void __launch_bounds__(kBlock, MINB)
                     int kb0, int n_chunks, int n_groups, int n_bins,
                     double *__restrict__ partial) {
   static_assert(L % 2 == 0, "L must be even");
-  static_assert(kBlock * L <= 2 * kTile * kTile * 4,
-                "group scratch must fit the record buffer");
   constexpr int M = L / 2;
   extern __shared__ float4 smem[];
   float4 *recA = smem;
   float4 *recB = smem + kTile * kTile;
   float *scratch = reinterpret_cast<float *>(smem);
-  double *acc64 = reinterpret_cast<double *>(smem + 2 * kTile * kTile);
+  double *acc64 = reinterpret_cast<double *>(scratch + fq3_scratch_floats(L));
   __shared__ float4 sI[kTile], sJ[kTile];
 
   const int4 it = items[blockIdx.x];
@@ -604,7 +613,7 @@ __global__ void __launch_bounds__(kBlock, MINB)
       PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
                                  dq_lo, dx, dy, dz);
       recA[q] = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
-      recB[q] = make_float4(p.ch * p.inv_r, p.sh * p.inv_r, p.inv_r, 0.f);
+      recB[q] = make_float4(p.ch * p.inv_r, p.sth, p.inv_r, p.cth);
     }
     __syncthreads();
     float2 acc[M];
@@ -615,9 +624,10 @@ __global__ void __launch_bounds__(kBlock, MINB)
         const float4 ra = recA[q];
         const float4 rb = recB[q];
         float2 s, co;
-        seed_sincos2(kf, ra.x, ra.y, s, co);
+        seed_sincos2r(kf, ra.x, ra.y, rb.y, rb.w, s, co);
+        const float shr = __fmul_rn(0.5f * ra.z, rb.z);
         float2 t = __fmul2_rn(f2(rb.z), s);
-        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(shr)));
         const float2 kp = f2(ra.z), km = f2(-ra.z), sg = f2(ra.w);
 #pragma unroll
         for (int m = 0; m < M; ++m) {
@@ -655,8 +665,12 @@ __global__ void __launch_bounds__(kBlock, MINB)
 
 // dF/dx, packed.  Records per (a, b), stored [b][a]:
 //   a = (th_hi, th_lo, kappa, sigma2)
-//   b = (beta ch, beta sh, beta, gamma')   beta = -1/r^3, gamma' = -r dq/(2 ch)
-//   c = (dx, dy, dz, -r^2)
+//   b = (beta ch, sin theta, beta, gamma')   beta = -1/r^3,
+//                                            gamma' = -r dq/(2 ch)
+//   c = (dx, dy, dz, -r^2 with F(Q), else cos theta)
+// beta sh = (kappa/2) beta is rebuilt from a and b; with F(Q), cos theta
+// sits in a fourth array d.  The odd slot's seed is the even one rotated by
+// theta (seed_sincos2r).
 // Per two bins and ordered pair: FFMA2 (w) + FADD2 (u) + FFMA2 (g) +
 // 3 FFMA2 (accumulate) + FFMA2 (t) + FADD2 (k gamma') = 8 instructions.
 //
@@ -696,6 +710,7 @@ __device__ __forceinline__ void gradfq2_body(
   // behind the records
   float *fsum = reinterpret_cast<float *>(smem + 3 * kTile * kTile);
   float *fcmp = fsum + CPC * CPC * L;
+  float *recD = fcmp + CPC * CPC * L;  // WITH_F: cos theta of each record
   __shared__ float4 sI[kTile], sJ[kTile];
 
   const int4 ti = tiles[blockIdx.x];
@@ -828,8 +843,13 @@ __device__ __forceinline__ void gradfq2_body(
         const float beta = -(p.inv_r * p.inv_r * p.inv_r);
         const float gam = -p.r * dq_hi / (2.0f * p.ch);
         ra = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
-        rb = make_float4(beta * p.ch, beta * p.sh, beta, gam);
-        rc = make_float4(dx, dy, dz, WITH_F ? -(p.r * p.r) : 0.f);
+        // beta sh is rebuilt as (kappa/2) beta; its slot and c.w (recD
+        // with F(Q)) carry (sin theta, cos theta) for the rotated odd seed
+        rb = make_float4(beta * p.ch, p.sth, beta, gam);
+        rc = make_float4(dx, dy, dz, WITH_F ? -(p.r * p.r) : p.cth);
+        if constexpr (WITH_F) recD[q] = p.cth;
+      } else if constexpr (WITH_F) {
+        recD[q] = 0.f;
       }
       recA[q] = ra;
       recB[q] = rb;
@@ -844,9 +864,10 @@ __device__ __forceinline__ void gradfq2_body(
         const float4 rb = recB[q];
         const float4 rc = recC[q];
         float2 s, co;
-        seed_sincos2(kf, ra.x, ra.y, s, co);
+        seed_sincos2r(kf, ra.x, ra.y, rb.y, WITH_F ? recD[q] : rc.w, s, co);
+        const float bsh = __fmul_rn(0.5f * ra.z, rb.z);
         float2 t = __fmul2_rn(f2(rb.z), s);
-        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(rb.y)));
+        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(bsh)));
         float2 kg = make_float2(kf * rb.w, (kf + 1.0f) * rb.w);
         const float2 dkg = f2(2.0f * rb.w);
         const float2 kp = f2(ra.z), km = f2(-ra.z);
@@ -924,7 +945,8 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
 }
 
 // F(Q) pair sums and dF/dx in one pass (see gradfq2_body).  Dynamic shared
-// memory: 3 kTile^2 float4 records + 2 CPC * CPC * L floats.
+// memory: 3 kTile^2 float4 records + 2 CPC * CPC * L floats + kTile^2
+// floats (cos theta).
 template <int L, int CPC, int MINB>
 __global__ void __launch_bounds__(kTile * CPC, MINB)
     fqgrad2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
@@ -1020,7 +1042,8 @@ __global__ void __launch_bounds__(kBlock)
         float2 ae = f2(0.f), ao = f2(0.f), be = f2(0.f), bo = f2(0.f);
         for (int blk = 0; blk < kh; blk += RS / 2) {
           float2 s, co;
-          seed_sincos2((float)(kb0 + 2 * blk), p.th_hi, p.th_lo, s, co);
+          seed_sincos2r((float)(kb0 + 2 * blk), p.th_hi, p.th_lo, p.sth,
+                        p.cth, s, co);
           float2 t = __fmul2_rn(f2(beta), s);
           float2 w = __ffma2_rn(co, c1, __fmul2_rn(s, c2));
           const float4 *tb = tab + blk;
@@ -1149,7 +1172,8 @@ __global__ void __launch_bounds__(kBlock)
         float2 ae = f2(0.f), ao = f2(0.f), be = f2(0.f), bo = f2(0.f);
         for (int blk = 0; blk < kh; blk += RS / 2) {
           float2 s, co;
-          seed_sincos2((float)(kb0 + 2 * blk), p.th_hi, p.th_lo, s, co);
+          seed_sincos2r((float)(kb0 + 2 * blk), p.th_hi, p.th_lo, p.sth,
+                        p.cth, s, co);
           float2 t = __fmul2_rn(f2(beta), s);
           float2 w = __ffma2_rn(co, c1, __fmul2_rn(s, c2));
           const float4 *tb = stab + blk;

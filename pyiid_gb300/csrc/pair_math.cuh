@@ -159,6 +159,7 @@ struct PairPhase2 {
   float sigma2;         // (-1)^M
   float kappa;          // 2 sin(theta2 / 2)
   float sh, ch;         // sin, cos of theta2 / 2
+  float sth, cth;       // sin, cos of theta (a quarter-turn rotation of sh, ch)
   float r, inv_r;
 };
 
@@ -206,6 +207,13 @@ __device__ __forceinline__ PairPhase2 pair_phase2(float ax, float ay, float az,
   p.sh = __fmaf_rn(hc, hl, hs);
   p.ch = __fmaf_rn(-hs, hl, hc);
   p.kappa = 2.0f * p.sh;
+  // theta = theta2 / 2 + M pi / 2: rotate (sh, ch) by M quarter turns
+  switch (mi & 3) {
+    case 0: p.sth = p.sh;  p.cth = p.ch;  break;
+    case 1: p.sth = p.ch;  p.cth = -p.sh; break;
+    case 2: p.sth = -p.sh; p.cth = -p.ch; break;
+    default: p.sth = -p.ch; p.cth = p.sh; break;
+  }
   p.r = rh;
   p.inv_r = __frcp_rn(rh);
   return p;
@@ -218,6 +226,19 @@ __device__ __forceinline__ void seed_sincos2(float k0, float th_hi,
                                              float2 &c) {
   seed_sincos(k0, th_hi, th_lo, s.x, c.x);
   seed_sincos(k0 + 1.0f, th_hi, th_lo, s.y, c.y);
+}
+
+// Seeds of both slots from one reduced phase: (sin, cos) of k0*theta as in
+// seed_sincos, then those of (k0+1)*theta by the angle-addition rotation with
+// the pair's (sin theta, cos theta).  One reduction and one hardware sin/cos
+// instead of two; the rotation adds about two roundings.
+__device__ __forceinline__ void seed_sincos2r(float k0, float th_hi,
+                                              float th_lo, float sth,
+                                              float cth, float2 &s,
+                                              float2 &c) {
+  seed_sincos(k0, th_hi, th_lo, s.x, c.x);
+  s.y = __fmaf_rn(c.x, sth, __fmul_rn(s.x, cth));
+  c.y = __fmaf_rn(-s.x, sth, __fmul_rn(c.x, cth));
 }
 
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
