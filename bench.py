@@ -258,6 +258,7 @@ def run_gpu(args, rank, world, local):
     workloads = {}
     if rank == 0 and not args.no_workloads:
         for name, fn in (('fq_grad_au1000', run_fq_grad_au1000),
+                         ('pdf_transforms_au1000', run_pdf_transforms),
                          ('batched_fq_256_alloys', run_batched),
                          ('hmc_64_chains_au1000', run_hmc),
                          ('delayed_acceptance_au1000', run_delayed_acceptance),
@@ -324,6 +325,13 @@ def run_gpu(args, rank, world, local):
     line['roofline']['issue'] = issue_roofline(
         torch, dev, pairs, k_ret, k_ms, line['clocks'].get('sm_mhz'), kernel,
         lane_ops)
+    # the same launch against HBM: its ncu DRAM bytes over its time
+    hbm, traffic = measured_hbm_gbs(), line['roofline']['traffic']
+    if hbm and traffic:
+        gbs = traffic / (k_ms * 1e-3) / 1e9
+        line['roofline']['hbm'] = {
+            'achieved': gbs, 'peak': hbm, 'unit': 'GB/s', 'frac': gbs / hbm,
+            'peak_source': 'MEASURED_PEAKS.json hbm_gbs (measured copy)'}
     if workloads:
         line['workloads'] = workloads
     return line
@@ -535,6 +543,74 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
                                    'warm-up'},
             'gpu_over_cpu_port': gpu / cpu,
             'e2e_over_cpu_port': 1e3 / e2e_ms / cpu}
+
+
+def measured_hbm_gbs():
+    """HBM copy bandwidth measured on this part (MEASURED_PEAKS.json)."""
+    try:
+        with open(os.path.join(REPO, 'MEASURED_PEAKS.json')) as f:
+            return float(json.load(f)['hbm_gbs'])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
+def run_pdf_transforms(torch, reps=50):
+    """The F(Q) -> G(r) transforms on the 1,000-atom Au grids (Q_pdf step
+    0.0756865, 330 bins; r 0-40 step 0.01, 4000 points):
+      forward: G(r) of 64 configurations per call (pyiid_pdf); algorithmic
+               bytes per configuration 4 K' R (T) + 4 K' + 8 R;
+      grad_pdf: the compat [N, 3, K'] -> [N, 3, R] map at N = 1000
+               (pyiid_grad_pdf): 2 (3N) K' R flops, 4 (3N) K' + 8 (3N) R
+               bytes (+ T).
+    Device-resident inputs, CUDA events, mean over reps calls."""
+    from pyiid_gb300 import debye
+    from pyiid_gb300.sampling import experiment_grids
+    exp, qb, nb, rg = experiment_grids(None)
+    n_r, b, n = len(rg), 64, 1000
+    g = torch.Generator(device='cuda').manual_seed(7)
+    fq = torch.randn((b, nb), device='cuda', generator=g)
+    gfq = torch.randn((n, 3, nb), device='cuda', generator=g)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        s, e = (torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True))
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        e.synchronize()
+        return s.elapsed_time(e) / reps
+
+    fwd = lambda: debye.pdf(fq, qb, exp['rstep'], rg, exp['qmin'])  # noqa: E731
+    bwd = lambda: debye.grad_pdf(gfq, qb, exp['rstep'], rg, exp['qmin'])  # noqa: E731
+    ms_f = timed(fwd)
+    ms_g = timed(bwd)
+    assert torch.isfinite(fwd()).all() and torch.isfinite(bwd()).all()
+    hbm = measured_hbm_gbs()
+    fwd_bytes = b * (4 * nb * n_r + 4 * nb + 8 * n_r)
+    g_flops = 2 * 3 * n * nb * n_r
+    g_bytes = 4 * 3 * n * nb + 8 * 3 * n * n_r + 4 * nb * n_r
+    peak = fp32_peak_tflops(torch, torch.device('cuda'))
+    fwd_gbs = fwd_bytes / (ms_f * 1e-3) / 1e9
+    return {
+        'workload': 'G(r) transforms, 1000-atom Au grids (K\' 330, R 4000)',
+        'forward': {'configs': b, 'ms': ms_f,
+                    'algorithmic_bytes': fwd_bytes,
+                    'achieved_gbs': fwd_gbs,
+                    'hbm_peak_gbs': hbm,
+                    'note': 'T (5.3 MB) is read from L2 after the first '
+                            'configuration of a call, so the algorithmic '
+                            'rate can exceed the HBM copy rate'},
+        'grad_pdf': {'n_atoms': n, 'ms': ms_g, 'flops': g_flops,
+                     'achieved_tflops': g_flops / (ms_g * 1e-3) / 1e12,
+                     'fp32_peak_tflops': peak,
+                     'frac': g_flops / (ms_g * 1e-3) / 1e12 / peak,
+                     'algorithmic_bytes': g_bytes,
+                     'achieved_gbs': g_bytes / (ms_g * 1e-3) / 1e9,
+                     'hbm_peak_gbs': hbm},
+    }
 
 
 def run_hmc(torch, iters=6):
@@ -874,6 +950,8 @@ def _run_nuts(torch, iters):
 
 WORKLOADS = {
     'fq_grad_au1000': lambda torch, **kw: run_fq_grad_au1000(torch, **kw),
+    'pdf_transforms_au1000':
+        lambda torch, **kw: run_pdf_transforms(torch, **kw),
     'batched_fq_256_alloys': lambda torch, **kw: run_batched(torch, **kw),
     'hmc_64_chains_au1000': lambda torch, **kw: run_hmc(torch, **kw),
     'delayed_acceptance_au1000':

@@ -211,57 +211,126 @@ __global__ void gradfq_coef_kernel(const double *__restrict__ na,
   }
 }
 
-// Compat G(r) gradient: out[row][i] = sum_k A[row][k] T[k][i] (FP32 GEMM,
-// 128x128 CTA tile, 8x8 per thread, FP64 output).  Rows are the 3N rows of a
-// reference-convention grad_fq.
+// Compat G(r) gradient: out[row][i] = sum_{k >= kmin} A[row][k] T[k][i]
+// (FP32 products and sums, FP64 output).  Rows are the 3N rows of a
+// reference-convention grad_fq.  CTA tile 128 x 128 with K steps of 16;
+// thread (ty, tx) = (tid / 16, tid % 16) owns rows ty*8 .. ty*8+7 and
+// columns tx*4 .. +3 and 64 + tx*4 .. +3.  The next K step's tiles are
+// fetched into registers while the current one is multiplied from shared
+// memory (two buffers, one barrier per step).  A (row-major [rows][n_bins])
+// is read along k and transposed into sA[k][row] (rows padded to 132 floats:
+// 2-way conflicts on the stores, 16-byte aligned float4 reads); T is read as
+// float4 along r when n_r % 4 == 0.
+constexpr int kGemmTile = 128;
+constexpr int kGemmK = 16;
+constexpr int kGemmPad = 132;
+
 __global__ void __launch_bounds__(256)
     gemm_rows_T_kernel(const float *__restrict__ A, const float *__restrict__ T,
                        int n_rows, int n_bins, int n_r, int kmin,
                        double *__restrict__ out) {
-  __shared__ float sA[8][128 + 4];
-  __shared__ float sB[8][128 + 4];
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int row0 = blockIdx.y * 128, col0 = blockIdx.x * 128;
+  __shared__ __align__(16) float sA[2][kGemmK][kGemmPad];
+  __shared__ __align__(16) float sB[2][kGemmK][kGemmTile];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int row0 = blockIdx.y * kGemmTile, col0 = blockIdx.x * kGemmTile;
+  const bool vec_t = (n_r % 4) == 0;
+
+  float ra[8];
+  float4 rb[2];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = e * 256 + tid;
+      const int gr = row0 + (idx >> 4), gk = k0 + (idx & 15);
+      ra[e] = (gr < n_rows && gk < n_bins) ? A[(size_t)gr * n_bins + gk] : 0.f;
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int idx = e * 256 + tid;
+      const int gk = k0 + (idx >> 5), gc = col0 + (idx & 31) * 4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gk < n_bins) {
+        const float *src = T + (size_t)gk * n_r + gc;
+        if (vec_t && gc + 3 < n_r) {
+          v = *reinterpret_cast<const float4 *>(src);
+        } else {
+          if (gc < n_r) v.x = src[0];
+          if (gc + 1 < n_r) v.y = src[1];
+          if (gc + 2 < n_r) v.z = src[2];
+          if (gc + 3 < n_r) v.w = src[3];
+        }
+      }
+      rb[e] = v;
+    }
+  };
+  auto stash = [&](int buf) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = e * 256 + tid;
+      sA[buf][idx & 15][idx >> 4] = ra[e];
+    }
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int idx = e * 256 + tid;
+      *reinterpret_cast<float4 *>(&sB[buf][idx >> 5][(idx & 31) * 4]) = rb[e];
+    }
+  };
+
   float acc[8][8];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
-  for (int k0 = kmin; k0 < n_bins; k0 += 8) {
-    // load A tile: 128 rows x 8 k  (256 threads x 4 elements)
-    for (int e = threadIdx.x; e < 128 * 8; e += 256) {
-      const int r = e / 8, kk = e % 8;
-      const int gr = row0 + r, gk = k0 + kk;
-      sA[kk][r] = (gr < n_rows && gk < n_bins) ? A[(size_t)gr * n_bins + gk] : 0.f;
-    }
-    for (int e = threadIdx.x; e < 128 * 8; e += 256) {
-      const int kk = e / 128, c = e % 128;
-      const int gk = k0 + kk, gc = col0 + c;
-      sB[kk][c] = (gk < n_bins && gc < n_r) ? T[(size_t)gk * n_r + gc] : 0.f;
-    }
-    __syncthreads();
+
+  if (kmin < n_bins) {
+    fetch(kmin);
+    stash(0);
+  }
+  __syncthreads();
+  int buf = 0;
+  for (int k0 = kmin; k0 < n_bins; k0 += kGemmK) {
+    const bool more = k0 + kGemmK < n_bins;
+    if (more) fetch(k0 + kGemmK);
 #pragma unroll
-    for (int kk = 0; kk < 8; ++kk) {
-      float a[8], bb[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) a[i] = sA[kk][ty * 8 + i];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) bb[j] = sB[kk][tx + 16 * j];
+    for (int kk = 0; kk < kGemmK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4 *>(&sA[buf][kk][ty * 8]);
+      const float4 a1 =
+          *reinterpret_cast<const float4 *>(&sA[buf][kk][ty * 8 + 4]);
+      const float4 b0 = *reinterpret_cast<const float4 *>(&sB[buf][kk][tx * 4]);
+      const float4 b1 =
+          *reinterpret_cast<const float4 *>(&sB[buf][kk][64 + tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
     }
+    if (more) stash(buf ^ 1);
     __syncthreads();
+    buf ^= 1;
   }
+
+  const bool vec_o = (n_r % 2) == 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int gr = row0 + ty * 8 + i;
     if (gr >= n_rows) continue;
+    double *orow = out + (size_t)gr * n_r;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int gc = col0 + tx + 16 * j;
-      if (gc < n_r) out[(size_t)gr * n_r + gc] = (double)acc[i][j];
+    for (int h = 0; h < 2; ++h) {
+      const int gc = col0 + h * 64 + tx * 4;
+#pragma unroll
+      for (int j = 0; j < 4; j += 2) {
+        const double v0 = acc[i][h * 4 + j], v1 = acc[i][h * 4 + j + 1];
+        if (vec_o && gc + j + 1 < n_r) {
+          *reinterpret_cast<double2 *>(orow + gc + j) = make_double2(v0, v1);
+        } else {
+          if (gc + j < n_r) orow[gc + j] = v0;
+          if (gc + j + 1 < n_r) orow[gc + j + 1] = v1;
+        }
+      }
     }
   }
 }
