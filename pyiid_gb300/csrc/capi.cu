@@ -48,8 +48,8 @@ struct GradVariant {
 };
 
 using FqKernel = void (*)(const float *, const int *, const int4 *,
-                          const int4 *, float, float, int, int, int, int,
-                          double *);
+                          const int4 *, const int *, float, float, int, int,
+                          int, int, double *);
 using GradKernel = void (*)(const float *, const int *, const int4 *,
                             const int2 *, float, float, int, int, int,
                             const float *, int, float *);
@@ -164,6 +164,7 @@ struct Layout {
   std::vector<int4> tiles;
   std::vector<int2> cfg_tiles;
   std::vector<int4> items;
+  std::vector<int> item_order;  // launch order: items by decreasing pairs
   std::vector<int> key_item_begin;
   std::vector<int2> spair_species;
   std::vector<double> pair_counts;  // [n_configs][n_spairs]
@@ -190,6 +191,7 @@ struct Layout {
   int4 *d_tiles = nullptr;
   int2 *d_cfg_tiles = nullptr;
   int4 *d_items = nullptr;
+  int *d_item_order = nullptr;
   int *d_key_item_begin = nullptr;
   int2 *d_spair = nullptr;
 };
@@ -312,6 +314,7 @@ void free_layout(Layout *L) {
   cudaFree(L->d_tiles);
   cudaFree(L->d_cfg_tiles);
   cudaFree(L->d_items);
+  cudaFree(L->d_item_order);
   cudaFree(L->d_key_item_begin);
   cudaFree(L->d_spair);
   cudaFree(L->d_adj_ioff);
@@ -407,6 +410,22 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
   for (const int4 &it : L->items) L->key_item_begin[it.w + 1]++;
   for (int k = 0; k < nkeys; ++k) L->key_item_begin[k + 1] += L->key_item_begin[k];
   {
+    // largest items first: the pair kernels' last wave then holds the
+    // smallest items instead of the largest ones of the last configuration
+    const int ni = (int)L->items.size();
+    std::vector<double> pairs(ni, 0.0);
+    for (int i = 0; i < ni; ++i) {
+      const int4 it = L->items[i];
+      const double na = L->tiles[it.x].y;
+      for (int J = it.y; J < it.z; ++J)
+        pairs[i] += (J == it.x) ? na * (na - 1) / 2 : na * L->tiles[J].y;
+    }
+    L->item_order.resize(ni);
+    for (int i = 0; i < ni; ++i) L->item_order[i] = i;
+    std::stable_sort(L->item_order.begin(), L->item_order.end(),
+                     [&](int a, int b) { return pairs[a] > pairs[b]; });
+  }
+  {
     const int ni = (int)L->items.size(), nt = (int)L->tiles.size();
     L->adj_ioff.resize(ni);
     L->adj_joff.resize(ni);
@@ -440,6 +459,7 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
   TRY(upload(ctx, &L->d_tiles, L->tiles));
   TRY(upload(ctx, &L->d_cfg_tiles, L->cfg_tiles));
   TRY(upload(ctx, &L->d_items, L->items));
+  TRY(upload(ctx, &L->d_item_order, L->item_order));
   TRY(upload(ctx, &L->d_key_item_begin, L->key_item_begin));
   TRY(upload(ctx, &L->d_spair, L->spair_species));
   L->mitem_begin.push_back((int)L->mitems.size());
@@ -671,8 +691,8 @@ int run_fq(pyiid_ctx *ctx, const Layout *L, const float *positions,
     partial = static_cast<double *>(p);
     dim3 grid(n_items, n_cb);
     E.k<<<grid, kBlock, fq_smem(E.v, n_chunks), ctx->stream>>>(
-        positions, L->d_perm, L->d_tiles, L->d_items, dq_hi, dq_lo, kb0,
-        n_chunks, n_groups, n_bins, partial);
+        positions, L->d_perm, L->d_tiles, L->d_items, L->d_item_order, dq_hi,
+        dq_lo, kb0, n_chunks, n_groups, n_bins, partial);
     LAUNCH_CHECK(ctx);
   }
   dim3 g2((n_bins + 127) / 128, L->n_configs);
@@ -1058,8 +1078,8 @@ int pyiid_batch_potential_grad(pyiid_ctx *ctx, const float *positions,
     if (!L->items.empty()) {
       adjoint_sym_kernel<kAdjRS><<<(unsigned)L->items.size(), kBlock,
                                    (kp / 2) * sizeof(float4), ctx->stream>>>(
-          positions, L->d_perm, L->d_tiles, L->d_items, dq_hi, dq_lo, kb0, kp,
-          tabs, n_species, L->d_adj_ioff, L->d_adj_joff, part);
+          positions, L->d_perm, L->d_tiles, L->d_items, L->d_item_order, dq_hi,
+          dq_lo, kb0, kp, tabs, n_species, L->d_adj_ioff, L->d_adj_joff, part);
       LAUNCH_CHECK(ctx);
     }
     adjoint_reduce_kernel<<<(unsigned)L->tiles.size(), 96, 0, ctx->stream>>>(
@@ -1683,9 +1703,9 @@ extern "C" int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
     const int n_chunks = (chunks_total + n_cb - 1) / n_cb;
     const int n_groups = kBlock / n_chunks;
     dim3 grid(n_items, n_cb);
-    E.k<<<grid, kBlock, fq_smem(E.v, n_chunks), st>>>(positions, d_perm, d_tiles,
-                                            d_items, dq_hi, dq_lo, kb0,
-                                            n_chunks, n_groups, n_bins, d_part);
+    E.k<<<grid, kBlock, fq_smem(E.v, n_chunks), st>>>(
+        positions, d_perm, d_tiles, d_items, nullptr, dq_hi, dq_lo, kb0,
+        n_chunks, n_groups, n_bins, d_part);
     LAUNCH_CHECK(ctx);
   }
   dim3 g2((n_bins + 127) / 128, 1);

@@ -38,7 +38,9 @@ __device__ __forceinline__ float4 load_atom(const float *__restrict__ pos,
 }
 
 // ===================================================================== F(Q)
-// One CTA per work item (tile I, tiles [J0, J1) of one species pair).  Thread
+// One CTA per work item (tile I, tiles [J0, J1) of one species pair); CTA b
+// takes item order[b] (largest items first, so that the last wave holds the
+// small ones; nullptr: item b), and writes partial row `item`.  Thread
 // (chunk c, group g) accumulates bins [kbase, kbase+L) over the pairs q = g,
 // g + n_groups, ... of every tile pair, NP pairs at a time (independent
 // recurrences interleaved for instruction-level parallelism).  Per pair the
@@ -74,7 +76,8 @@ template <int L, int NP>
 __global__ void __launch_bounds__(kBlock, 2)
     fq_pair_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                    const int4 *__restrict__ tiles,
-                   const int4 *__restrict__ items, float dq_hi, float dq_lo,
+                   const int4 *__restrict__ items,
+                   const int *__restrict__ order, float dq_hi, float dq_lo,
                    int kb0, int n_chunks, int n_groups, int n_bins,
                    double *__restrict__ partial) {
   extern __shared__ float4 smem[];
@@ -85,7 +88,8 @@ __global__ void __launch_bounds__(kBlock, 2)
   float *kC = kS + L * blockDim.x;
   __shared__ float4 sI[kTile], sJ[kTile];
 
-  const int4 it = items[blockIdx.x];
+  const int item = order ? order[blockIdx.x] : (int)blockIdx.x;
+  const int4 it = items[item];
   const int4 ti = tiles[it.x];
   const int tid = threadIdx.x;
   const int c = tid % n_chunks;
@@ -181,7 +185,7 @@ __global__ void __launch_bounds__(kBlock, 2)
   }
   const int nk = n_chunks * L;
   const int kfirst = kb0 + blockIdx.y * nk;
-  double *out = partial + (size_t)blockIdx.x * n_bins;
+  double *out = partial + (size_t)item * n_bins;
   for (int i = tid; i < nk; i += blockDim.x) {
     const int k = kfirst + i;
     if (k < n_bins) out[k] = red[i];
@@ -423,7 +427,8 @@ template <int L, int NP = 1>
 __global__ void __launch_bounds__(kBlock, 2)
     fq_pair2_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                     const int4 *__restrict__ tiles,
-                    const int4 *__restrict__ items, float dq_hi, float dq_lo,
+                    const int4 *__restrict__ items,
+                   const int *__restrict__ order, float dq_hi, float dq_lo,
                     int kb0, int n_chunks, int n_groups, int n_bins,
                     double *__restrict__ partial) {
   static_assert(L % 2 == 0, "L must be even");
@@ -435,7 +440,8 @@ __global__ void __launch_bounds__(kBlock, 2)
   float *kC = kS + L * blockDim.x;
   __shared__ float4 sI[kTile], sJ[kTile];
 
-  const int4 it = items[blockIdx.x];
+  const int item = order ? order[blockIdx.x] : (int)blockIdx.x;
+  const int4 it = items[item];
   const int4 ti = tiles[it.x];
   const int tid = threadIdx.x;
   const int c = tid % n_chunks;
@@ -542,7 +548,7 @@ __global__ void __launch_bounds__(kBlock, 2)
   }
   const int nk = n_chunks * L;
   const int kfirst = kb0 + blockIdx.y * nk;
-  double *out = partial + (size_t)blockIdx.x * n_bins;
+  double *out = partial + (size_t)item * n_bins;
   for (int i = tid; i < nk; i += blockDim.x) {
     const int k = kfirst + i;
     if (k < n_bins) out[k] = red[i];
@@ -567,7 +573,8 @@ template <int L, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB)
     fq_pair3_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
                     const int4 *__restrict__ tiles,
-                    const int4 *__restrict__ items, float dq_hi, float dq_lo,
+                    const int4 *__restrict__ items,
+                   const int *__restrict__ order, float dq_hi, float dq_lo,
                     int kb0, int n_chunks, int n_groups, int n_bins,
                     double *__restrict__ partial) {
   static_assert(L % 2 == 0, "L must be even");
@@ -579,7 +586,8 @@ __global__ void __launch_bounds__(kBlock, MINB)
   double *acc64 = reinterpret_cast<double *>(scratch + fq3_scratch_floats(L));
   __shared__ float4 sI[kTile], sJ[kTile];
 
-  const int4 it = items[blockIdx.x];
+  const int item = order ? order[blockIdx.x] : (int)blockIdx.x;
+  const int4 it = items[item];
   const int4 ti = tiles[it.x];
   const int tid = threadIdx.x;
   const int c = tid % n_chunks;
@@ -656,7 +664,7 @@ __global__ void __launch_bounds__(kBlock, MINB)
   }
   __syncthreads();
   const int kfirst = kb0 + blockIdx.y * nk;
-  double *out = partial + (size_t)blockIdx.x * n_bins;
+  double *out = partial + (size_t)item * n_bins;
   for (int i = tid; i < nk; i += blockDim.x) {
     const int k = kfirst + i;
     if (k < n_bins) out[k] = acc64[i];
@@ -1119,7 +1127,8 @@ __global__ void __launch_bounds__(kBlock)
     adjoint_sym_kernel(const float *__restrict__ pos,
                        const int *__restrict__ perm,
                        const int4 *__restrict__ tiles,
-                       const int4 *__restrict__ items, float dq_hi,
+                       const int4 *__restrict__ items,
+                       const int *__restrict__ order, float dq_hi,
                        float dq_lo, int kb0, int kp,
                        const float4 *__restrict__ tabs, int n_species,
                        const int *__restrict__ ioff,
@@ -1131,7 +1140,8 @@ __global__ void __launch_bounds__(kBlock)
   __shared__ float sred[kBlock / kTile][kTile][3];
   __shared__ float sjac[kJMaxTiles][kTile][3];
 
-  const int4 it = items[blockIdx.x];
+  const int item = order ? order[blockIdx.x] : (int)blockIdx.x;
+  const int4 it = items[item];
   const int4 ti = tiles[it.x];
   const int tid = threadIdx.x;
   const int lane = tid % kTile;
@@ -1240,14 +1250,14 @@ __global__ void __launch_bounds__(kBlock)
   sred[grp][lane][1] = gy;
   sred[grp][lane][2] = gz;
   __syncthreads();
-  float *pi = part + ioff[blockIdx.x];
+  float *pi = part + ioff[item];
   for (int i = tid; i < kTile * 3; i += blockDim.x) {
     const int a = i / 3, c = i % 3;
     float sum = 0.f;
     for (int gg = 0; gg < ngrp; ++gg) sum += sred[gg][a][c];
     pi[i] = sum;
   }
-  float *pj = part + joff[blockIdx.x];
+  float *pj = part + joff[item];
   for (int i = tid; i < (it.z - it.y) * kTile * 3; i += blockDim.x)
     pj[i] = (&sjac[0][0][0])[i];
 }

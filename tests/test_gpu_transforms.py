@@ -1,0 +1,57 @@
+"""The F(Q) -> G(r) maps on the GPU against the oracle's T matrix: the
+compat gradient transform (pyiid_grad_pdf, a tiled FP32 GEMM with FP64
+output) over several CTA tiles, both load paths (n_r a multiple of 4 or
+not), K not a multiple of the 16-bin step and qmin > 0 (rows below kmin
+skipped); and the batched forward transform (pyiid_pdf).
+Tolerance: norm-wise relative 1e-5 (FP32 products and sums of K terms)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import debye_np as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope='module')
+def D():
+    from pyiid_gb300 import debye
+    return debye
+
+
+@pytest.mark.parametrize('n,k,n_r,qmin', [(150, 333, 4001, 0.4),
+                                          (43, 330, 4000, 0.0),
+                                          (1, 17, 130, 0.0),
+                                          (200, 64, 257, 1.0)])
+def test_grad_pdf_matches_oracle(D, n, k, n_r, qmin):
+    rng = np.random.default_rng(n + k)
+    g = rng.standard_normal((n, 3, k)).astype(np.float32)
+    qstep, rstep = 0.0756865, 0.01
+    rg = np.arange(n_r) * rstep
+    got = D.grad_pdf(torch.as_tensor(g, device='cuda'), qstep, rstep, rg,
+                     qmin).cpu().numpy()
+    want = O.grad_pdf(g, rstep, qstep, rg, qmin)
+    assert got.shape == (n, 3, n_r)
+    assert rel(got, want) <= TOL, rel(got, want)
+
+
+@pytest.mark.parametrize('b,k,n_r,qmin', [(64, 330, 4000, 0.0),
+                                          (3, 333, 4001, 0.5)])
+def test_batched_pdf_matches_oracle(D, b, k, n_r, qmin):
+    rng = np.random.default_rng(b)
+    f = rng.standard_normal((b, k)).astype(np.float32)
+    qstep, rstep = 0.0756865, 0.01
+    rg = np.arange(n_r) * rstep
+    got = D.pdf(torch.as_tensor(f, device='cuda'), qstep, rstep, rg,
+                qmin).cpu().numpy()
+    T = O.tmatrix(k, rstep, qstep, rg, qmin)
+    want = f.astype(np.float64) @ T
+    assert rel(got, want) <= TOL, rel(got, want)
