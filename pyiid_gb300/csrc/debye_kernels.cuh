@@ -556,10 +556,12 @@ __global__ void __launch_bounds__(kBlock, 2)
 }
 
 // Floats of the record / group-scratch region of fq_pair3_kernel: the two
-// record arrays, or n_groups * n_chunks * L <= kBlock * L group sums.
+// record arrays, or the group sums n_groups * n_chunks * (L + 1) <=
+// kBlock * (L + 1) (rows padded to the odd stride L + 1: the chunks of a
+// warp then fall on distinct banks).
 __host__ __device__ constexpr int fq3_scratch_floats(int L) {
-  return kBlock * L > 2 * kTile * kTile * 4 ? kBlock * L
-                                            : 2 * kTile * kTile * 4;
+  return kBlock * (L + 1) > 2 * kTile * kTile * 4 ? kBlock * (L + 1)
+                                                  : 2 * kTile * kTile * 4;
 }
 
 // F(Q) pair sums with the group reduction done per tile pair: after each
@@ -648,17 +650,20 @@ __global__ void __launch_bounds__(kBlock, MINB)
       }
     }
     __syncthreads();  // records are dead: reuse them as group scratch
+    constexpr int Lp = L + 1;
+    const int nkp = n_chunks * Lp;
     if (active) {
 #pragma unroll
       for (int m = 0; m < M; ++m) {
-        scratch[g * nk + c * L + 2 * m] = acc[m].x;
-        scratch[g * nk + c * L + 2 * m + 1] = acc[m].y;
+        scratch[g * nkp + c * Lp + 2 * m] = acc[m].x;
+        scratch[g * nkp + c * Lp + 2 * m + 1] = acc[m].y;
       }
     }
     __syncthreads();
     for (int i = tid; i < nk; i += blockDim.x) {
+      const int off = (i / L) * Lp + i % L;
       float sum = 0.f;
-      for (int gg = 0; gg < n_groups; ++gg) sum += scratch[gg * nk + i];
+      for (int gg = 0; gg < n_groups; ++gg) sum += scratch[gg * nkp + off];
       acc64[i] += (double)sum;
     }
   }
