@@ -52,3 +52,26 @@ def test_null_context_is_rejected():
     assert lib.pyiid_set_stream(None, None) != 0
     assert lib.pyiid_synchronize(None) != 0
     assert lib.pyiid_launch_count(None) == -1
+
+
+def test_variant_tables_are_described_without_a_gpu():
+    """Launch-shape tables (host-only calls): counts, parameters, and the
+    context's default F(Q) shape {24, -3} at index 18."""
+    from pyiid_gb300 import _native
+    from pyiid_gb300.autotune import variants
+    lib = _native.load()
+    for kern, k in _native.KERNELS.items():
+        n = lib.pyiid_variant_count(k)
+        assert n >= 2, kern
+        v = variants(kern)
+        assert [i for i, _ in v] == list(range(n))
+        for _, info in v:
+            assert info['bins_per_thread'] > 0 and info['threads'] > 0
+    assert lib.pyiid_variant_count(99) == -1
+    p = (ctypes.c_int32 * 3)()
+    assert lib.pyiid_variant_info(0, 10 ** 6, p, 3) != 0
+    fq = dict(variants('fq'))
+    assert (fq[18]['bins_per_thread'], fq[18]['pairs_per_thread']) == (24, -3)
+    for _, info in variants('fq_grad'):
+        assert info['pairs_per_thread'] == 0          # packed kernels only
+        assert info['threads'] % 32 == 0 and 32 % (info['threads'] // 32) == 0
