@@ -136,6 +136,32 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
                   int n_species, int n_bins, double qbin, int k_begin,
                   float *fq, float *grad);
 
+/* One configuration split across processes (one per GPU, e.g. a single
+ * large particle): the species-sorted atom tiles are cut into n_parts
+ * contiguous ranges of nearly equal work, and part `part` evaluates the
+ * pairs its tiles own in one pass (as pyiid_fq_grad):
+ *   sums : device double [n_bins]  raw Debye sums S_k of its pairs (0 for
+ *          k < k_begin); add them over the parts (one all-reduce of K
+ *          doubles) and pass the total to pyiid_fq_from_sums for F(Q);
+ *   grad : device float [n_atoms][3][n_bins]: the complete gradient rows of
+ *          its atoms (each part sweeps all atoms for its rows); rows of
+ *          other parts are left untouched, so no gradient exchange is needed;
+ *   rows : host int32 [n_atoms] or NULL: 1 for the atoms whose rows it wrote.
+ * The parts' rows partition the atoms.  Has no reference counterpart (the
+ * reference's multi-GPU farm splits pair chunks and sums [N][3][K] arrays on
+ * the host, gpu_wrappers/gpu_wrap.py:287-314). */
+int pyiid_fq_grad_part(pyiid_ctx *ctx, const float *positions,
+                       const int32_t *species, int n_atoms,
+                       const float *scatter, int n_species, int n_bins,
+                       double qbin, int k_begin, int part, int n_parts,
+                       double *sums, float *grad, int32_t *rows);
+
+/* F(Q) [n_bins] (device float) from the summed raw sums of all parts:
+ * F_k = 2 nan_to_num(S_k / na_k) for k >= k_begin, 0 below. */
+int pyiid_fq_from_sums(pyiid_ctx *ctx, const int32_t *species, int n_atoms,
+                       const float *scatter, int n_species, int n_bins,
+                       int k_begin, const double *sums, float *fq);
+
 /* ------------------------------------------------------------------------ *
  * F(Q) -> G(r).
  *

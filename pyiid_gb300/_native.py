@@ -38,6 +38,11 @@ _SIGNATURES = {
                                _c_int, _c_dbl, _c_int, _vp]),
     'pyiid_fq_grad': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
                                _c_int, _c_dbl, _c_int, _vp, _vp]),
+    'pyiid_fq_grad_part': (_c_int, [_vp, _vp, _i32p, _c_int, _f32p, _c_int,
+                                    _c_int, _c_dbl, _c_int, _c_int, _c_int,
+                                    _vp, _vp, _i32p]),
+    'pyiid_fq_from_sums': (_c_int, [_vp, _i32p, _c_int, _f32p, _c_int,
+                                    _c_int, _c_int, _vp, _vp]),
     'pyiid_batch_fq': (_c_int, [_vp, _vp, _i32p, _i32p, _c_int, _f32p,
                                 _c_int, _c_int, _c_dbl, _c_int, _vp]),
     'pyiid_pdf': (_c_int, [_vp, _vp, _c_int, _c_int, _c_dbl, _c_dbl, _f64p,

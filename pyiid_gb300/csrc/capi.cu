@@ -65,7 +65,7 @@ struct GradEntry {
 using FqGradKernel = void (*)(const float *, const int *, const int4 *,
                               const int2 *, float, float, int, int, int,
                               const float *, int, float *, const float *,
-                              double *);
+                              double *, int);
 struct FqGradEntry {
   GradVariant v;
   FqGradKernel k;
@@ -902,16 +902,120 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
     dim3 grid((unsigned)n_tiles, (chunks_total + cpc - 1) / cpc);
     E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
-        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart);
+        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart, 0);
     LAUNCH_CHECK(ctx);
   }
   fqgrad_finish_kernel<<<(n_bins + 127) / 128, 128, 0, ctx->stream>>>(
-      fpart, 0, fpart ? n_tiles : 0, d_na, n_bins, fpart ? kbo : n_bins, fq);
+      fpart, 0, fpart ? n_tiles : 0, d_na, n_bins, fpart ? kbo : n_bins, fq,
+      nullptr);
   LAUNCH_CHECK(ctx);
   if (kbo > 0 && n_atoms > 0)
     CUDA_TRY(ctx, cudaMemset2DAsync(grad, (size_t)n_bins * sizeof(float), 0,
                                     (size_t)kbo * sizeof(float),
                                     (size_t)3 * n_atoms, ctx->stream));
+  return PYIID_OK;
+}
+
+int pyiid_fq_grad_part(pyiid_ctx *ctx, const float *positions,
+                       const int32_t *species, int n_atoms,
+                       const float *scatter, int n_species, int n_bins,
+                       double qbin, int k_begin, int part, int n_parts,
+                       double *sums, float *grad, int32_t *rows) {
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  const int32_t offsets[2] = {0, n_atoms};
+  TRY(check_common(ctx, 1, offsets, n_species, n_bins, qbin, k_begin));
+  if (n_parts < 1 || part < 0 || part >= n_parts)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "part %d of %d", part, n_parts);
+  if (!sums || (!grad && n_atoms > 0))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "null output pointer");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  TRY(set_attrs(ctx));
+  Layout *L;
+  TRY(get_layout(ctx, species, offsets, 1, n_species, &L));
+  float *d_ftab;
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, &d_ftab));
+  double *d_na;
+  TRY(get_na(ctx, L, scatter, n_bins, &d_na));
+  // contiguous tile range of this part, balanced by lane operations: every
+  // tile sweeps all atoms for the gradient (8 per ordered pair-bin) and the
+  // atoms of tiles J >= I for F(Q) (1 per pair-bin)
+  const int n_tiles = (int)L->tiles.size();
+  std::vector<double> cum(n_tiles + 1, 0.0), suffix(n_tiles + 1, 0.0);
+  for (int t = n_tiles - 1; t >= 0; --t)
+    suffix[t] = suffix[t + 1] + L->tiles[t].y;
+  for (int t = 0; t < n_tiles; ++t)
+    cum[t + 1] = cum[t] + (double)L->tiles[t].y *
+                              (8.0 * n_atoms + suffix[t]);
+  auto edge = [&](int p) {
+    if (p <= 0) return 0;
+    if (p >= n_parts) return n_tiles;
+    const double target = cum[n_tiles] * p / n_parts;
+    return (int)(std::lower_bound(cum.begin(), cum.end(), target) -
+                 cum.begin());
+  };
+  const int t0 = std::min(edge(part), n_tiles);
+  const int t1 = std::max(t0, std::min(edge(part + 1), n_tiles));
+  if (rows) {
+    std::fill(rows, rows + n_atoms, 0);
+    for (int t = t0; t < t1; ++t)
+      for (int a = 0; a < L->tiles[t].y; ++a)
+        rows[L->perm[L->tiles[t].x + a]] = 1;
+  }
+  const int kbo = std::min(k_begin, n_bins);
+  const int kb0 = kbo & ~1;
+  double *fpart = nullptr;
+  if (t1 > t0 && kb0 < n_bins) {
+    void *p;
+    TRY(ensure(ctx, "coef",
+               (size_t)n_species * n_species * n_bins * sizeof(float), &p));
+    float *coef = static_cast<float *>(p);
+    gradfq_coef_kernel<<<64, 256, 0, ctx->stream>>>(d_na, d_ftab, n_species,
+                                                    n_bins, 1, coef);
+    LAUNCH_CHECK(ctx);
+    TRY(ensure(ctx, "fqgrad_part", (size_t)n_tiles * n_bins * sizeof(double),
+               &p));
+    fpart = static_cast<double *>(p);
+    const FqGradEntry &E = kFqGradTable[ctx->fqgrad_variant];
+    const int Lb = E.v.L, cpc = E.v.CPC;
+    const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    float dq_hi, dq_lo;
+    split_double(qbin, dq_hi, dq_lo);
+    dim3 grid((unsigned)(t1 - t0), (chunks_total + cpc - 1) / cpc);
+    E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
+        positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
+        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart, t0);
+    LAUNCH_CHECK(ctx);
+  }
+  fqgrad_finish_kernel<<<(n_bins + 127) / 128, 128, 0, ctx->stream>>>(
+      fpart, t0, fpart ? t1 : t0, d_na, n_bins, kbo, nullptr, sums);
+  LAUNCH_CHECK(ctx);
+  if (kbo > 0 && t1 > t0) {
+    zero_low_bins_kernel<<<t1 - t0, 128, 0, ctx->stream>>>(
+        L->d_perm, L->d_tiles, t0, kbo, n_bins, grad);
+    LAUNCH_CHECK(ctx);
+  }
+  return PYIID_OK;
+}
+
+int pyiid_fq_from_sums(pyiid_ctx *ctx, const int32_t *species, int n_atoms,
+                       const float *scatter, int n_species, int n_bins,
+                       int k_begin, const double *sums, float *fq) {
+  if (n_atoms < 0) return fail(ctx, PYIID_ERR_INVALID_ARG, "n_atoms < 0");
+  const int32_t offsets[2] = {0, n_atoms};
+  TRY(check_common(ctx, 1, offsets, n_species, n_bins, 1.0, k_begin));
+  if (!sums || !fq)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "null pointer");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  Layout *L;
+  TRY(get_layout(ctx, species, offsets, 1, n_species, &L));
+  float *d_ftab;  // keys the normalisation cache to this table
+  TRY(get_ftab(ctx, scatter, n_species, n_bins, &d_ftab));
+  double *d_na;
+  TRY(get_na(ctx, L, scatter, n_bins, &d_na));
+  const int kb_out = n_atoms > 0 ? std::min(k_begin, n_bins) : n_bins;
+  fq_from_sums_kernel<<<(n_bins + 127) / 128, 128, 0, ctx->stream>>>(
+      sums, d_na, n_bins, kb_out, fq);
+  LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }
 

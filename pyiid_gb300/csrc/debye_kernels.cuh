@@ -711,7 +711,9 @@ __device__ __forceinline__ void gradfq2_body(
     const int4 *__restrict__ tiles, const int2 *__restrict__ cfg_tiles,
     float dq_hi, float dq_lo, int kb0, int chunks_total, int n_bins,
     const float *__restrict__ coef, int n_species, float *__restrict__ out,
-    const float *__restrict__ ftab, double *__restrict__ fpart) {
+    const float *__restrict__ ftab, double *__restrict__ fpart, int tile0) {
+  // tile I of this CTA (tile0: first tile of a part of the tile list)
+  const int I = tile0 + (int)blockIdx.x;
   static_assert(L % 2 == 0, "L must be even");
   static_assert(32 % CPC == 0, "a warp must hold whole atoms");
   constexpr int M = L / 2;
@@ -726,7 +728,7 @@ __device__ __forceinline__ void gradfq2_body(
   float *recD = fcmp + CPC * CPC * L;  // WITH_F: cos theta of each record
   __shared__ float4 sI[kTile], sJ[kTile];
 
-  const int4 ti = tiles[blockIdx.x];
+  const int4 ti = tiles[I];
   const int2 ct = cfg_tiles[ti.z];
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -841,7 +843,7 @@ __device__ __forceinline__ void gradfq2_body(
     __syncthreads();
     if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
     __syncthreads();
-    const bool same = (tj == (int)blockIdx.x);
+    const bool same = (tj == I);
     for (int q = tid; q < kTile * kTile; q += blockDim.x) {
       const int b = q / kTile, a = q % kTile;
       float4 ra = make_float4(0.f, 0.f, 0.f, 1.f);
@@ -910,7 +912,7 @@ __device__ __forceinline__ void gradfq2_body(
         }
       }
     };
-    const bool count_f = WITH_F && tj >= (int)blockIdx.x;
+    const bool count_f = WITH_F && tj >= I;
     if (active) {
       if (count_f)
         pair_loop(BoolTag<true>());
@@ -938,7 +940,7 @@ __device__ __forceinline__ void gradfq2_body(
         double sum = 0.0;
         for (int wp = 0; wp < CPC; ++wp)
           sum += (double)fsum[wp * CPC * L + i] - (double)fcmp[wp * CPC * L + i];
-        fpart[(size_t)blockIdx.x * n_bins + k] = sum;
+        fpart[(size_t)I * n_bins + k] = sum;
       }
     }
   }
@@ -954,7 +956,7 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
                    float *__restrict__ out) {
   gradfq2_body<L, CPC, false>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
                               chunks_total, n_bins, coef, n_species, out,
-                              nullptr, nullptr);
+                              nullptr, nullptr, 0);
 }
 
 // F(Q) pair sums and dF/dx in one pass (see gradfq2_body).  Dynamic shared
@@ -968,27 +970,55 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
                    float dq_lo, int kb0, int chunks_total, int n_bins,
                    const float *__restrict__ coef, int n_species,
                    float *__restrict__ out, const float *__restrict__ ftab,
-                   double *__restrict__ fpart) {
+                   double *__restrict__ fpart, int tile0) {
   gradfq2_body<L, CPC, true>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
                              chunks_total, n_bins, coef, n_species, out, ftab,
-                             fpart);
+                             fpart, tile0);
 }
 
 // F(Q) of the fused pass: S_k = sum over the tiles [t0, t1) of the
 // configuration of fpart[tile][k] (fixed order), F_k as fq_finish_kernel.
+// With sums != nullptr the raw S_k (0 below kb_out) go there instead (one
+// part of a configuration split across processes; pyiid_fq_from_sums
+// finishes the summed parts).
 __global__ void fqgrad_finish_kernel(const double *__restrict__ fpart,
                                      int t0, int t1, const double *__restrict__ na,
                                      int n_bins, int kb_out,
-                                     float *__restrict__ fq) {
+                                     float *__restrict__ fq,
+                                     double *__restrict__ sums) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_bins) return;
-  float v = 0.f;
-  if (k >= kb_out) {
-    double s = 0.0;
+  double s = 0.0;
+  if (k >= kb_out)
     for (int t = t0; t < t1; ++t) s += fpart[(size_t)t * n_bins + k];
-    v = fq_value(s, na[k]);
+  if (sums) {
+    sums[k] = s;
+  } else {
+    fq[k] = (k >= kb_out) ? fq_value(s, na[k]) : 0.f;
   }
-  fq[k] = v;
+}
+
+// F_k = 2 nan_to_num(S_k / na_k) for k >= kb_out (0 below) from summed raw
+// sums (the finishing step of a configuration split across processes).
+__global__ void fq_from_sums_kernel(const double *__restrict__ sums,
+                                    const double *__restrict__ na, int n_bins,
+                                    int kb_out, float *__restrict__ fq) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_bins) return;
+  fq[k] = (k >= kb_out) ? fq_value(sums[k], na[k]) : 0.f;
+}
+
+// Zeroes bins [0, kb) of the gradient rows of the atoms of tiles [t0, t1).
+__global__ void zero_low_bins_kernel(const int *__restrict__ perm,
+                                     const int4 *__restrict__ tiles, int t0,
+                                     int kb, int n_bins,
+                                     float *__restrict__ grad) {
+  const int4 t = tiles[t0 + blockIdx.x];
+  for (int i = threadIdx.x; i < t.y * 3 * kb; i += blockDim.x) {
+    const int a = i / (3 * kb), rest = i % (3 * kb);
+    const int c = rest / kb, k = rest % kb;
+    grad[((size_t)perm[t.x + a] * 3 + c) * n_bins + k] = 0.f;
+  }
 }
 
 // =================================================================== adjoint

@@ -10,7 +10,8 @@ import torch
 
 from ._native import context, POTENTIALS, NativeError
 
-__all__ = ['fq', 'batch_fq', 'grad_fq', 'fq_grad', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
+__all__ = ['fq', 'batch_fq', 'grad_fq', 'fq_grad', 'fq_grad_part',
+           'fq_from_sums', 'pdf', 'grad_pdf', 'potential', 'potential_grad',
            'batch_potential_grad', 'as_positions', 'mh_init', 'mh_steps',
            'mh_state_size', 'mh_views', 'mc_propose', 'mc_accept',
            'MOVE_DISPLACE', 'MOVE_INSERT', 'MOVE_REMOVE']
@@ -146,6 +147,53 @@ def fq_grad(positions, species, scatter, qbin, k_begin=0, out_fq=None,
              ctypes.c_void_p(out_fq.data_ptr()),
              ctypes.c_void_p(out_grad.data_ptr()))
     return out_fq, out_grad
+
+
+def fq_grad_part(positions, species, scatter, qbin, k_begin, part, n_parts,
+                 out_grad=None):
+    """One part of a configuration split across processes
+    (pyiid_fq_grad_part): (raw sums S_k [K] float64, gradient [N, 3, K] with
+    this part's rows written, bool mask [N] of those rows).  ``out_grad`` is
+    written only in this part's rows; a new one starts as zeros."""
+    import ctypes
+    pos = as_positions(positions)
+    n = pos.shape[0]
+    sp = _np(species, np.int32)
+    tab = _np(scatter, np.float32)
+    k = tab.shape[1]
+    if out_grad is None:
+        out_grad = torch.zeros((n, 3, k), dtype=torch.float32,
+                               device=pos.device)
+    else:
+        _check_dev(out_grad, 'out_grad', torch.float32)
+        if out_grad.numel() != n * 3 * k:
+            raise NativeError(f'out_grad must hold {n} x 3 x {k} floats')
+    sums = torch.empty(k, dtype=torch.float64, device=pos.device)
+    rows = np.zeros(max(n, 1), np.int32)
+    ctx = context(pos.device.index)
+    ctx.call('pyiid_fq_grad_part', ctypes.c_void_p(pos.data_ptr()),
+             _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
+             tab.shape[0], k, float(qbin), int(k_begin), int(part),
+             int(n_parts), ctypes.c_void_p(sums.data_ptr()),
+             ctypes.c_void_p(out_grad.data_ptr()), _ptr(rows, ctypes.c_int32))
+    return sums, out_grad, rows[:n].astype(bool)
+
+
+def fq_from_sums(species, scatter, k_begin, sums):
+    """F(Q) [K] from the raw sums of all parts (pyiid_fq_from_sums)."""
+    import ctypes
+    sp = _np(species, np.int32)
+    tab = _np(scatter, np.float32)
+    k = tab.shape[1]
+    _check_dev(sums, 'sums', torch.float64)
+    if sums.numel() != k:
+        raise NativeError(f'sums must hold {k} doubles')
+    out = torch.empty(k, dtype=torch.float32, device=sums.device)
+    ctx = context(sums.device.index)
+    ctx.call('pyiid_fq_from_sums', _ptr(sp, ctypes.c_int32), len(sp),
+             _ptr(tab, ctypes.c_float), tab.shape[0], k, int(k_begin),
+             ctypes.c_void_p(sums.data_ptr()), ctypes.c_void_p(out.data_ptr()))
+    return out
 
 
 def pdf(fq_t, qstep, rstep, rgrid, qmin):

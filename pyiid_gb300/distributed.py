@@ -1,4 +1,5 @@
-"""Configuration sharding across ranks (one process per GPU).
+"""Configuration sharding across ranks (one process per GPU), and one large
+configuration split across ranks (:func:`fq_grad_sharded`).
 
 Batches of configurations are independent units: rank r evaluates a
 contiguous slice of them and nothing crosses ranks on the data path.  The
@@ -11,7 +12,7 @@ ranks (:func:`max_over_ranks`).
 import numpy as np
 
 __all__ = ['pair_costs', 'shard_bounds', 'local_slice', 'gather_rows',
-           'max_over_ranks']
+           'max_over_ranks', 'fq_grad_sharded']
 
 
 def pair_costs(offsets):
@@ -80,3 +81,37 @@ def max_over_ranks(value, device=None, group=None):
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return float(t.item())
+
+
+def fq_grad_sharded(positions, species, scatter, qbin, k_begin=0, group=None,
+                    gather_grad=False, part_fn=None, finish_fn=None):
+    """F(Q) and its gradient of ONE configuration split across the ranks of
+    ``group`` (one GPU each).  Rank r evaluates part r of the tile list in one
+    pass (``pyiid_fq_grad_part``): the complete gradient rows of its atoms
+    and the raw Debye sums of the pairs its tiles own.  The only exchange is
+    an all-reduce of the K raw sums (float64), after which every rank forms
+    F(Q) (``pyiid_fq_from_sums``).  Gradient rows stay on their owner unless
+    ``gather_grad`` (an all-reduce of the zero-filled [N, 3, K] array).
+
+    part_fn(positions, species, scatter, qbin, k_begin, part, n_parts) ->
+    (sums, grad, rows) and finish_fn(species, scatter, k_begin, sums) -> fq
+    default to the device calls; they are parameters so that the exchange
+    can be exercised on CPU ranks.
+
+    Returns (fq [K], grad [N, 3, K], rows bool [N] of this rank's atoms)."""
+    import torch.distributed as dist
+    if part_fn is None or finish_fn is None:
+        from . import debye
+        part_fn = part_fn or debye.fq_grad_part
+        finish_fn = finish_fn or debye.fq_from_sums
+    if dist.is_available() and dist.is_initialized():
+        rank, world = dist.get_rank(group), dist.get_world_size(group)
+    else:
+        rank, world = 0, 1
+    sums, grad, rows = part_fn(positions, species, scatter, qbin, k_begin,
+                               rank, world)
+    if world > 1:
+        dist.all_reduce(sums, op=dist.ReduceOp.SUM, group=group)
+        if gather_grad:
+            dist.all_reduce(grad, op=dist.ReduceOp.SUM, group=group)
+    return finish_fn(species, scatter, k_begin, sums), grad, rows

@@ -89,3 +89,73 @@ def test_two_ranks_evaluate_their_slices_and_gather_in_order(tmp_path):
         ref = O.fq(p, np.repeat(tab, len(p), 0), 0.1)
         assert np.array_equal(full[c], ref)
     assert np.load(tmp_path / 'tmax.npy')[0] == 2.0
+
+
+def _sharded_worker(rank, world, port, out_dir):
+    """fq_grad_sharded's exchange on CPU ranks, with oracle stand-ins for the
+    device part (rank r owns atoms i = r mod world and the pairs (i, j < i))
+    and the device finish."""
+    import torch
+    import torch.distributed as dist
+    from oracle import debye_np as O
+    from pyiid_gb300.distributed import fq_grad_sharded
+    os.environ['MASTER_ADDR'] = '127.0.0.1'
+    os.environ['MASTER_PORT'] = str(port)
+    dist.init_process_group('gloo', rank=rank, world_size=world)
+    try:
+        rng = np.random.default_rng(5)
+        pos = rng.normal(0, 4, (23, 3))
+        tab = np.ones((1, 30), np.float32)
+        sp = np.zeros(len(pos), np.int32)
+
+        def part_fn(p, s, t, qbin, kb, part, n_parts):
+            f = t[s].astype(np.float64)
+            q = np.asarray(p, np.float32).astype(np.float64)
+            Q = np.arange(t.shape[1]) * qbin
+            sums = np.zeros(t.shape[1])
+            rows = np.arange(len(q)) % n_parts == part
+            for i in np.flatnonzero(rows):
+                r = np.sqrt(((q[i] - q[:i]) ** 2).sum(1))[:, None]
+                sums += (f[i] * f[:i] * np.sin(Q * r) / r).sum(0)
+            sums[:kb] = 0.0
+            grad = O.grad_fq(p, t[s], qbin)
+            grad[~rows] = 0.0
+            grad[:, :, :kb] = 0.0
+            return (torch.as_tensor(sums), torch.as_tensor(grad), rows)
+
+        def finish_fn(s, t, kb, sums):
+            with np.errstate(all='ignore'):
+                f = 2 * np.nan_to_num(sums.numpy() / O.normalization(t[s]))
+            f[:kb] = 0.0
+            return torch.as_tensor(f)
+
+        fq, grad, rows = fq_grad_sharded(pos, sp, tab, 0.1, 2,
+                                         gather_grad=True, part_fn=part_fn,
+                                         finish_fn=finish_fn)
+        np.save(os.path.join(out_dir, f'fq{rank}.npy'), fq.numpy())
+        np.save(os.path.join(out_dir, f'grad{rank}.npy'), grad.numpy())
+        np.save(os.path.join(out_dir, f'rows{rank}.npy'), rows)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_split_one_configuration_and_exchange_the_sums(tmp_path):
+    import torch.multiprocessing as mp
+    from oracle import debye_np as O
+    port = _free_port()
+    mp.spawn(_sharded_worker, args=(2, port, str(tmp_path)), nprocs=2,
+             join=True)
+    rng = np.random.default_rng(5)
+    pos = rng.normal(0, 4, (23, 3))
+    tab = np.ones((1, 30), np.float32)
+    want_f = O.fq(pos, np.repeat(tab, len(pos), 0), 0.1)
+    want_f[:2] = 0.0
+    want_g = O.grad_fq(pos, np.repeat(tab, len(pos), 0), 0.1)
+    want_g[:, :, :2] = 0.0
+    rows = [np.load(tmp_path / f'rows{r}.npy') for r in range(2)]
+    assert np.array_equal(rows[0] ^ rows[1], np.ones(len(pos), bool))
+    for r in range(2):
+        f = np.load(tmp_path / f'fq{r}.npy')
+        g = np.load(tmp_path / f'grad{r}.npy')
+        assert np.allclose(f, want_f, rtol=1e-12, atol=1e-12)
+        assert np.allclose(g, want_g, rtol=1e-12, atol=1e-12)

@@ -171,3 +171,41 @@ def test_fq_grad_large_particle_sampled(D):
         want = -(fa * fa)[None, :] * np.einsum('jk,jc->ck', w, d) / na
         assert rel(g[a, :, kb:], want[:, kb:]) <= TOL_G, (a, rel(g[a, :, kb:],
                                                                  want[:, kb:]))
+
+
+@pytest.mark.parametrize('n_parts', [1, 2, 3, 5])
+def test_parts_reassemble_one_configuration(D, n_parts):
+    """pyiid_fq_grad_part run for every part on one device: the parts' rows
+    partition the atoms and equal the one-call gradient bitwise (the same
+    CTAs run), and the summed raw sums give the one-call F(Q)."""
+    import torch
+    pos, nums = alloy(300, 8, 18.0)
+    qbin, nb, kb = 0.05, 500, 3
+    sp, tab, _ = species_tables(nums, qbin, nb)
+    f_ref, g_ref = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
+    f_ref, g_ref = f_ref.cpu().numpy(), g_ref.cpu().numpy()
+    total = torch.zeros(nb, dtype=torch.float64, device='cuda')
+    seen = np.zeros(len(pos), int)
+    for p in range(n_parts):
+        sums, g, rows = D.fq_grad_part(pos, sp, tab, qbin, kb, p, n_parts)
+        total += sums
+        seen += rows
+        g = g.cpu().numpy()
+        assert np.array_equal(g[rows], g_ref[rows]), p
+        assert np.all(g[~rows] == 0), p
+    assert np.all(seen == 1)
+    f = D.fq_from_sums(sp, tab, kb, total).cpu().numpy()
+    assert np.all(f[:kb] == 0)
+    assert rel(f, f_ref) <= 1e-6
+    assert rel(f[kb:], O.fq(pos, tab[sp], qbin)[kb:]) <= TOL_F
+
+
+def test_sharded_call_on_one_rank_is_the_one_pass_call(D):
+    from pyiid_gb300.distributed import fq_grad_sharded
+    pos, nums = alloy(120, 9, 13.0)
+    sp, tab, _ = species_tables(nums, 0.1, 250)
+    f, g, rows = fq_grad_sharded(pos, sp, tab, 0.1, 2)
+    f1, g1 = D.fq_grad(pos, sp, tab, 0.1, k_begin=2)
+    assert rows.all()
+    assert np.array_equal(g.cpu().numpy(), g1.cpu().numpy())
+    assert rel(f.cpu().numpy(), f1.cpu().numpy()) <= 1e-6
