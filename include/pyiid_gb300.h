@@ -129,8 +129,12 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
  * more packed FMA per two bins instead of a second pass.  Replaces the
  * get_fq + get_grad_fq pair of calls a calculator makes on one
  * configuration (elasticscatter/__init__.py:304-341 and :477-496).
- *   fq   : device float [n_bins]
- *   grad : device float [n_atoms][3][n_bins] */
+ *   fq   : float [n_bins]
+ *   grad : float [n_atoms][3][n_bins]
+ * Both outputs may be device memory or pinned host memory mapped into the
+ * device (cudaHostAlloc / cudaHostRegister): the kernel then stores the
+ * results over the host link while it computes, so no separate
+ * device-to-host copy follows (zero-copy).  Other pointers are rejected. */
 int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
                   const int32_t *species, int n_atoms, const float *scatter,
                   int n_species, int n_bins, double qbin, int k_begin,

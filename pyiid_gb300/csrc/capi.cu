@@ -648,6 +648,31 @@ int set_attrs(pyiid_ctx *ctx) {
   return PYIID_OK;
 }
 
+// A pointer the device can write for the output `what`: device or managed
+// memory as it is, pinned host memory through its device mapping (zero-copy:
+// the kernel's stores cross the host link while it computes); anything
+// else is rejected before any launch.
+int device_view(pyiid_ctx *ctx, void *p, void **out, const char *what) {
+  cudaPointerAttributes a;
+  const cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "%s: not a CUDA-visible pointer",
+                what);
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
+    *out = p;
+    return PYIID_OK;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+    *out = a.devicePointer;
+    return PYIID_OK;
+  }
+  return fail(ctx, PYIID_ERR_INVALID_ARG,
+              "%s must be device memory or pinned, device-mapped host memory",
+              what);
+}
+
 int check_common(pyiid_ctx *ctx, int n_configs, const int32_t *offsets,
                  int n_species, int n_bins, double qbin, int k_begin) {
   if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
@@ -872,6 +897,15 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
   if (!fq || (!grad && n_atoms > 0))
     return fail(ctx, PYIID_ERR_INVALID_ARG, "null output pointer");
   CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  {
+    void *v;
+    TRY(device_view(ctx, fq, &v, "fq"));
+    fq = static_cast<float *>(v);
+    if (n_atoms > 0) {
+      TRY(device_view(ctx, grad, &v, "grad"));
+      grad = static_cast<float *>(v);
+    }
+  }
   TRY(set_attrs(ctx));
   Layout *L;
   TRY(get_layout(ctx, species, offsets, 1, n_species, &L));

@@ -50,6 +50,16 @@ def _check_dev(t, name, dtype):
         raise NativeError(f'{name} must be a contiguous {dtype} tensor')
 
 
+def _check_out(t, name, dtype):
+    """An output the device can write: a CUDA tensor, or a pinned CPU tensor
+    (written in place by the kernel over the host link)."""
+    if isinstance(t, torch.Tensor) and not t.is_cuda and t.is_pinned():
+        if t.dtype != dtype or not t.is_contiguous():
+            raise NativeError(f'{name} must be a contiguous {dtype} tensor')
+        return
+    _check_dev(t, name, dtype)
+
+
 def fq(positions, species, scatter, qbin, k_begin=0, out=None):
     """Reduced structure factor [K] (bins from Q = 0; bins < k_begin are 0)."""
     import ctypes
@@ -120,7 +130,10 @@ def fq_grad(positions, species, scatter, qbin, k_begin=0, out_fq=None,
             out_grad=None):
     """F(Q) [K] and the reference-convention gradient [N, 3, K] from one
     pass over the pairs (pyiid_fq_grad): the values fq() and grad_fq()
-    return, with the pair terms summed in another order."""
+    return, with the pair terms summed in another order.  ``out_fq`` and
+    ``out_grad`` may be pinned CPU tensors: the kernel then writes the
+    results into host memory directly (no device-to-host copy; synchronise
+    the stream before reading them)."""
     import ctypes
     pos = as_positions(positions)
     n = pos.shape[0]
@@ -130,14 +143,14 @@ def fq_grad(positions, species, scatter, qbin, k_begin=0, out_fq=None,
     if out_fq is None:
         out_fq = torch.empty(k, dtype=torch.float32, device=pos.device)
     else:
-        _check_dev(out_fq, 'out_fq', torch.float32)
+        _check_out(out_fq, 'out_fq', torch.float32)
         if out_fq.numel() != k:
             raise NativeError(f'out_fq must hold {k} floats')
     if out_grad is None:
         out_grad = torch.empty((n, 3, k), dtype=torch.float32,
                                device=pos.device)
     else:
-        _check_dev(out_grad, 'out_grad', torch.float32)
+        _check_out(out_grad, 'out_grad', torch.float32)
         if out_grad.numel() != n * 3 * k:
             raise NativeError(f'out_grad must hold {n} x 3 x {k} floats')
     ctx = context(pos.device.index)

@@ -209,3 +209,35 @@ def test_sharded_call_on_one_rank_is_the_one_pass_call(D):
     assert rows.all()
     assert np.array_equal(g.cpu().numpy(), g1.cpu().numpy())
     assert rel(f.cpu().numpy(), f1.cpu().numpy()) <= 1e-6
+
+
+def test_zero_copy_outputs_in_pinned_host_memory(D):
+    """Pinned CPU outputs are written by the kernel over the host link and
+    equal the device outputs bitwise; pageable host memory is rejected
+    (Python check and the library's pointer check) before any launch."""
+    import ctypes
+    import torch
+    from pyiid_gb300._native import NativeError, context
+    pos, nums = alloy(150, 13, 14.0)
+    qbin, nb, kb = 0.05, 500, 3
+    sp, tab, _ = species_tables(nums, qbin, nb)
+    f, g = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
+    hf = torch.empty(nb, dtype=torch.float32, pin_memory=True)
+    hg = torch.empty((len(pos), 3, nb), dtype=torch.float32, pin_memory=True)
+    D.fq_grad(pos, sp, tab, qbin, k_begin=kb, out_fq=hf, out_grad=hg)
+    torch.cuda.synchronize()
+    assert torch.equal(hf, f.cpu()) and torch.equal(hg, g.cpu())
+    with pytest.raises(NativeError):
+        D.fq_grad(pos, sp, tab, qbin, out_fq=torch.empty(nb))
+    p = D.as_positions(pos)
+    page = np.zeros((len(pos), 3, nb), np.float32)
+    spi = np.ascontiguousarray(sp, np.int32)
+    tabf = np.ascontiguousarray(tab, np.float32)
+    with pytest.raises(NativeError):
+        context().call('pyiid_fq_grad', ctypes.c_void_p(p.data_ptr()),
+                       spi.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                       len(pos), tabf.ctypes.data_as(
+                           ctypes.POINTER(ctypes.c_float)),
+                       tab.shape[0], nb, qbin, kb,
+                       ctypes.c_void_p(f.data_ptr()),
+                       ctypes.c_void_p(page.ctypes.data))
