@@ -237,7 +237,7 @@ def run_gpu(args, rank, world, local):
     h_pos.copy_(torch.as_tensor(pos))
     h_fq = torch.empty(n_bins, dtype=torch.float32, pin_memory=True)
     h_grad = torch.empty((n, 3, n_bins), dtype=torch.float32, pin_memory=True)
-    e2e_steps = max(2, min(args.steps, 5))
+    e2e_steps = max(3, min(args.steps, 10))
     times = []
     for i in range(e2e_steps + 1):
         flush.zero_()
