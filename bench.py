@@ -527,6 +527,7 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
         t.append(time.perf_counter() - t0)
     cpu = 1.0 / float(np.mean(t))
     gpu = 1e3 / ms
+    single = single_config_au1000(torch)
     return {'workload': '1000-atom fcc Au, exact F(Q) + full dF/dx, '
                         'Q 0.1-25 step 0.05 (498 bins returned)',
             'pairs': pairs, 'ms_per_eval': ms, 'evals_per_s': gpu,
@@ -542,7 +543,31 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
                                    f'F and dF/dx, {n_bins} bins) after one '
                                    'warm-up'},
             'gpu_over_cpu_port': gpu / cpu,
-            'e2e_over_cpu_port': 1e3 / e2e_ms / cpu}
+            'e2e_over_cpu_port': 1e3 / e2e_ms / cpu,
+            'single_configuration': single}
+
+
+def single_config_au1000(torch, reps=50):
+    """One 1,000-atom Au configuration through the calls a drop-in Calc1D
+    or ElasticScatter user makes per step: the exact Rw and its gradient on
+    the PDF grid (pyiid_batch_potential_grad, one configuration) and F(Q)
+    on Q 0.1-25 step 0.05 (pyiid_fq)."""
+    from pyiid_gb300 import debye, structures
+    from pyiid_gb300.sampling import PDFPotential, experiment_grids
+    from pyiid_gb300.scatter_factors import species_tables
+    exp, qb, nb, rg = experiment_grids(None)
+    ref = structures.fcc_nearest(4.08, 1000).astype(np.float32)
+    sp, tab, _ = species_tables([79] * 1000, qb, nb)
+    f = debye.fq(ref, sp, tab, qb)
+    gobs = debye.pdf(f, qb, exp['rstep'], rg, exp['qmin']).cpu().numpy()
+    pot = PDFPotential([79] * 1000, gobs, None, conv=100.0, n_configs=1)
+    x = torch.as_tensor(structures.displaced(ref, 0.05, 4), device='cuda')
+    sp2, tab2, _ = species_tables([79] * 1000, 0.05, 500)
+    fo = torch.empty(500, device='cuda')
+    return {'potential_and_gradient_ms':
+                time_ms(torch, lambda: pot.evaluate(x), reps),
+            'fq_ms': time_ms(torch, lambda: debye.fq(x, sp2, tab2, 0.05, 2,
+                                                     out=fo), reps)}
 
 
 def measured_hbm_gbs():

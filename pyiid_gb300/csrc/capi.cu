@@ -65,7 +65,7 @@ struct GradEntry {
 using FqGradKernel = void (*)(const float *, const int *, const int4 *,
                               const int2 *, float, float, int, int, int,
                               const float *, int, float *, const float *,
-                              double *, int);
+                              double *, int, JSplit);
 struct FqGradEntry {
   GradVariant v;
   FqGradKernel k;
@@ -237,6 +237,7 @@ struct pyiid_ctx {
   int grad_variant = 0;
   int adj_variant = 0;  // 0: symmetric (each pair once), 1: owner-computes
   int fqgrad_variant = 0;
+  int n_sms = 0;  // streaming multiprocessors of the device
 };
 
 namespace {
@@ -389,17 +390,33 @@ int get_layout(pyiid_ctx *ctx, const int32_t *species, const int32_t *offsets,
         L->pair_counts[(size_t)c * L->n_spairs + sa * (sa + 1) / 2 + sb] =
             (sa == sb) ? na * (na - 1) / 2 : na * nb;
       }
-    // F(Q) items: tile I with runs of tiles J <= I of one species
-    for (int I = t0; I < t1; ++I) {
-      int J = t0;
-      while (J <= I) {
-        const int sJ = L->tiles[J].w;
-        int Je = J;
-        while (Je <= I && L->tiles[Je].w == sJ && Je - J < kJMax) ++Je;
-        const int sI = L->tiles[I].w;
-        const int sp = sI * (sI + 1) / 2 + sJ;
-        L->items.push_back(make_int4(I, J, Je, c * L->n_spairs + sp));
-        J = Je;
+  }
+  // F(Q) items: tile I with runs of at most jmax tiles J <= I of one
+  // species.  Runs are kJMax tiles long unless that leaves fewer than about
+  // four items per SM (small batches: one 1,000-atom particle has 32
+  // tiles), then shorter, so that the pair kernels still fill the GPU.
+  {
+    double tile_pairs = 0.0;
+    for (int c = 0; c < n_configs; ++c) {
+      const double T = L->cfg_tiles[c].y - L->cfg_tiles[c].x;
+      tile_pairs += T * (T + 1) / 2;
+    }
+    const double target = 4.0 * std::max(1, ctx->n_sms);
+    const int jmax =
+        std::max(1, std::min(kJMax, (int)std::floor(tile_pairs / target)));
+    for (int c = 0; c < n_configs; ++c) {
+      const int t0 = L->cfg_tiles[c].x, t1 = L->cfg_tiles[c].y;
+      for (int I = t0; I < t1; ++I) {
+        int J = t0;
+        while (J <= I) {
+          const int sJ = L->tiles[J].w;
+          int Je = J;
+          while (Je <= I && L->tiles[Je].w == sJ && Je - J < jmax) ++Je;
+          const int sI = L->tiles[I].w;
+          const int sp = sI * (sI + 1) / 2 + sJ;
+          L->items.push_back(make_int4(I, J, Je, c * L->n_spairs + sp));
+          J = Je;
+        }
       }
     }
   }
@@ -778,6 +795,7 @@ int pyiid_create(pyiid_ctx **out, int device) {
   pyiid_ctx *ctx = new (std::nothrow) pyiid_ctx();
   if (!ctx) return fail(nullptr, PYIID_ERR_OOM, "out of host memory");
   ctx->device = device;
+  ctx->n_sms = prop.multiProcessorCount;
   *out = ctx;
   return PYIID_OK;
 }
@@ -917,6 +935,7 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
   const int kb0 = kbo & ~1;
   const int n_tiles = (int)L->tiles.size();
   double *fpart = nullptr;
+  int n_split = 1;
   if (n_atoms > 0 && kb0 < n_bins) {
     void *p;
     TRY(ensure(ctx, "coef",
@@ -925,25 +944,61 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
     gradfq_coef_kernel<<<64, 256, 0, ctx->stream>>>(d_na, d_ftab, n_species,
                                                     n_bins, 1, coef);
     LAUNCH_CHECK(ctx);
-    TRY(ensure(ctx, "fqgrad_part", (size_t)n_tiles * n_bins * sizeof(double),
-               &p));
-    fpart = static_cast<double *>(p);
     const FqGradEntry &E = kFqGradTable[ctx->fqgrad_variant];
     const int Lb = E.v.L, cpc = E.v.CPC;
     const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    const int gy = (chunks_total + cpc - 1) / cpc;
+    // a configuration too small for two waves of CTAs splits the tiles J of
+    // every tile I over S <= 8 CTAs that write partial rows; S minimises
+    // waves / S (each CTA's work shrinks as 1/S), lightly penalising the
+    // partial rows each part adds
+    int per_sm = 0;
+    CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                      &per_sm, E.k, kTile * cpc, fqgrad_smem(E.v)));
+    const long long slots =
+        (long long)std::max(1, per_sm) * std::max(1, ctx->n_sms);
+    const long long ctas = (long long)n_tiles * gy;
+    if (ctas < 2 * slots) {
+      double best = 1e300;
+      for (int S = 1; S <= std::min(8, n_tiles); ++S) {
+        const double waves = std::ceil((double)(ctas * S) / (double)slots);
+        const double cost = waves / S * (1.0 + 0.02 * (S - 1));
+        if (cost < best) {
+          best = cost;
+          n_split = S;
+        }
+      }
+    }
+    TRY(ensure(ctx, "fqgrad_part",
+               (size_t)n_split * n_tiles * n_bins * sizeof(double), &p));
+    fpart = static_cast<double *>(p);
+    const size_t gsize = (size_t)n_atoms * 3 * n_bins;
+    float *gout = grad;
+    if (n_split > 1) {
+      TRY(ensure(ctx, "fqgrad_gpart", (size_t)n_split * gsize * sizeof(float),
+                 &p));
+      gout = static_cast<float *>(p);
+    }
     float dq_hi, dq_lo;
     split_double(qbin, dq_hi, dq_lo);
-    dim3 grid((unsigned)n_tiles, (chunks_total + cpc - 1) / cpc);
+    dim3 grid((unsigned)n_tiles, gy, n_split);
     E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
-        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart, 0);
+        chunks_total, n_bins, coef, n_species, gout, d_ftab, fpart, 0,
+        JSplit{n_split, gsize, (size_t)n_tiles * n_bins});
     LAUNCH_CHECK(ctx);
+    if (n_split > 1) {
+      combine_grad_parts_kernel<<<2 * std::max(1, ctx->n_sms), 256, 0,
+                                  ctx->stream>>>(gout, n_split, gsize, gsize,
+                                                 n_bins, kbo, grad);
+      LAUNCH_CHECK(ctx);
+    }
   }
-  fqgrad_finish_kernel<<<(n_bins + 127) / 128, 128, 0, ctx->stream>>>(
-      fpart, 0, fpart ? n_tiles : 0, d_na, n_bins, fpart ? kbo : n_bins, fq,
-      nullptr);
+  fqgrad_finish_kernel<<<(n_bins + 3) / 4, 128, 0, ctx->stream>>>(
+      fpart, 0, fpart ? n_split * n_tiles : 0, d_na, n_bins,
+      fpart ? kbo : n_bins, fq, nullptr);
   LAUNCH_CHECK(ctx);
-  if (kbo > 0 && n_atoms > 0)
+  if (kbo > 0 && n_atoms > 0 && n_split == 1)
     CUDA_TRY(ctx, cudaMemset2DAsync(grad, (size_t)n_bins * sizeof(float), 0,
                                     (size_t)kbo * sizeof(float),
                                     (size_t)3 * n_atoms, ctx->stream));
@@ -1017,10 +1072,11 @@ int pyiid_fq_grad_part(pyiid_ctx *ctx, const float *positions,
     dim3 grid((unsigned)(t1 - t0), (chunks_total + cpc - 1) / cpc);
     E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
-        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart, t0);
+        chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart, t0,
+        JSplit{1, 0, 0});
     LAUNCH_CHECK(ctx);
   }
-  fqgrad_finish_kernel<<<(n_bins + 127) / 128, 128, 0, ctx->stream>>>(
+  fqgrad_finish_kernel<<<(n_bins + 3) / 4, 128, 0, ctx->stream>>>(
       fpart, t0, fpart ? t1 : t0, d_na, n_bins, kbo, nullptr, sums);
   LAUNCH_CHECK(ctx);
   if (kbo > 0 && t1 > t0) {

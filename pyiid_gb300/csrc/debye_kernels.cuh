@@ -705,15 +705,30 @@ struct BoolTag {
   static constexpr bool value = B;
 };
 
+// Split of the tiles J of a configuration over gridDim.z = n CTAs per
+// (tile I, chunk block), for configurations too small to fill the GPU
+// otherwise: CTA z sweeps the z-th of n contiguous parts of the J tiles and
+// writes raw partial rows (no NaN mapping) at out + z * out_stride and its
+// F(Q) rows at fpart + z * fpart_stride; combine_grad_parts_kernel and the
+// finishing kernel add the parts in a fixed order.  n = 1: no split.
+struct JSplit {
+  int n;
+  size_t out_stride, fpart_stride;
+};
+
 template <int L, int CPC, bool WITH_F>
 __device__ __forceinline__ void gradfq2_body(
     const float *__restrict__ pos, const int *__restrict__ perm,
     const int4 *__restrict__ tiles, const int2 *__restrict__ cfg_tiles,
     float dq_hi, float dq_lo, int kb0, int chunks_total, int n_bins,
     const float *__restrict__ coef, int n_species, float *__restrict__ out,
-    const float *__restrict__ ftab, double *__restrict__ fpart, int tile0) {
+    const float *__restrict__ ftab, double *__restrict__ fpart, int tile0,
+    JSplit js) {
   // tile I of this CTA (tile0: first tile of a part of the tile list)
   const int I = tile0 + (int)blockIdx.x;
+  const int part = js.n > 1 ? (int)blockIdx.z : 0;
+  out += part * js.out_stride;
+  if constexpr (WITH_F) fpart += part * js.fpart_stride;
   static_assert(L % 2 == 0, "L must be even");
   static_assert(32 % CPC == 0, "a warp must hold whole atoms");
   constexpr int M = L / 2;
@@ -776,7 +791,7 @@ __device__ __forceinline__ void gradfq2_body(
             vy += o[n_bins + k];
             vz += o[2 * n_bins + k];
           }
-          if (last) {
+          if (last && js.n == 1) {
             vx = isnan(vx) ? 0.f : (isinf(vx) ? copysignf(3.402823466e38f, vx) : vx);
             vy = isnan(vy) ? 0.f : (isinf(vy) ? copysignf(3.402823466e38f, vy) : vy);
             vz = isnan(vz) ? 0.f : (isinf(vz) ? copysignf(3.402823466e38f, vz) : vz);
@@ -830,7 +845,10 @@ __device__ __forceinline__ void gradfq2_body(
     for (int m = 0; m < M; ++m) af[m] = f2(0.f);
   };
 
-  for (int tj = ct.x; tj < ct.y; ++tj) {
+  const int n_cfg_tiles = ct.y - ct.x;
+  const int j_end = ct.x + (int)((long long)(part + 1) * n_cfg_tiles / js.n);
+  for (int tj = ct.x + (int)((long long)part * n_cfg_tiles / js.n);
+       tj < j_end; ++tj) {
     const int4 tJ = tiles[tj];
     if (cur_sb >= 0 && tJ.w != cur_sb) flush(cur_sb, false);
     if constexpr (WITH_F) {
@@ -956,7 +974,7 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
                    float *__restrict__ out) {
   gradfq2_body<L, CPC, false>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
                               chunks_total, n_bins, coef, n_species, out,
-                              nullptr, nullptr, 0);
+                              nullptr, nullptr, 0, JSplit{1, 0, 0});
 }
 
 // F(Q) pair sums and dF/dx in one pass (see gradfq2_body).  Dynamic shared
@@ -970,10 +988,10 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
                    float dq_lo, int kb0, int chunks_total, int n_bins,
                    const float *__restrict__ coef, int n_species,
                    float *__restrict__ out, const float *__restrict__ ftab,
-                   double *__restrict__ fpart, int tile0) {
+                   double *__restrict__ fpart, int tile0, JSplit js) {
   gradfq2_body<L, CPC, true>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
                              chunks_total, n_bins, coef, n_species, out, ftab,
-                             fpart, tile0);
+                             fpart, tile0, js);
 }
 
 // F(Q) of the fused pass: S_k = sum over the tiles [t0, t1) of the
@@ -981,20 +999,70 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
 // With sums != nullptr the raw S_k (0 below kb_out) go there instead (one
 // part of a configuration split across processes; pyiid_fq_from_sums
 // finishes the summed parts).
+// One warp per bin: lanes take rows t0 + lane, t0 + lane + 32, ... and the
+// warp adds the lane sums in a fixed shuffle order (bitwise reproducible).
 __global__ void fqgrad_finish_kernel(const double *__restrict__ fpart,
                                      int t0, int t1, const double *__restrict__ na,
                                      int n_bins, int kb_out,
                                      float *__restrict__ fq,
                                      double *__restrict__ sums) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n_bins) return;
+  const int k = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (k >= n_bins) return;  // whole warps leave together
   double s = 0.0;
   if (k >= kb_out)
-    for (int t = t0; t < t1; ++t) s += fpart[(size_t)t * n_bins + k];
+    for (int t = t0 + lane; t < t1; t += 32) s += fpart[(size_t)t * n_bins + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane) return;
   if (sums) {
     sums[k] = s;
   } else {
     fq[k] = (k >= kb_out) ? fq_value(s, na[k]) : 0.f;
+  }
+}
+
+// grad[i] = nan_to_num(sum over parts p of parts[p * stride + i]) for bins
+// k >= kbo, 0 below: the J-split parts of gradfq2_body added in part order.
+// Four elements per thread (n, stride and both pointers 16-byte aligned:
+// n_bins % 4 == 0), else one.
+__device__ __forceinline__ float nan_to_num_f(float v) {
+  return isnan(v) ? 0.f : (isinf(v) ? copysignf(3.402823466e38f, v) : v);
+}
+
+__global__ void combine_grad_parts_kernel(const float *__restrict__ parts,
+                                          int n_parts, size_t stride,
+                                          size_t n, int n_bins, int kbo,
+                                          float *__restrict__ grad) {
+  const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nt = (size_t)gridDim.x * blockDim.x;
+  if (n_bins % 4 == 0) {
+    const float4 *p4 = reinterpret_cast<const float4 *>(parts);
+    float4 *g4 = reinterpret_cast<float4 *>(grad);
+    for (size_t i = t0; i < n / 4; i += nt) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int p = 0; p < n_parts; ++p) {
+        const float4 a = p4[p * (stride / 4) + i];
+        v.x += a.x;
+        v.y += a.y;
+        v.z += a.z;
+        v.w += a.w;
+      }
+      const int k = (int)((4 * i) % n_bins);
+      v.x = k >= kbo ? nan_to_num_f(v.x) : 0.f;
+      v.y = k + 1 >= kbo ? nan_to_num_f(v.y) : 0.f;
+      v.z = k + 2 >= kbo ? nan_to_num_f(v.z) : 0.f;
+      v.w = k + 3 >= kbo ? nan_to_num_f(v.w) : 0.f;
+      g4[i] = v;
+    }
+    return;
+  }
+  for (size_t i = t0; i < n; i += nt) {
+    float v = 0.f;
+    if ((int)(i % n_bins) >= kbo) {
+      for (int p = 0; p < n_parts; ++p) v += parts[p * stride + i];
+      v = nan_to_num_f(v);
+    }
+    grad[i] = v;
   }
 }
 
