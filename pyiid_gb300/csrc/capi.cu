@@ -52,7 +52,7 @@ using FqKernel = void (*)(const float *, const int *, const int4 *,
                           int, int, double *);
 using GradKernel = void (*)(const float *, const int *, const int4 *,
                             const int2 *, float, float, int, int, int,
-                            const float *, int, float *);
+                            const float *, int, float *, JSplit);
 
 struct FqEntry {
   FqVariant v;
@@ -690,6 +690,34 @@ int device_view(pyiid_ctx *ctx, void *p, void **out, const char *what) {
               what);
 }
 
+// Parts S <= min(8, n_tiles) over which the owner-computes gradient kernels
+// split the tiles J of one configuration when tiles x chunk blocks CTAs give
+// fewer than two waves: S minimises waves / S (each CTA's work shrinks as
+// 1/S), lightly penalising the partial rows every part adds.
+int choose_jsplit(pyiid_ctx *ctx, const void *kernel, int threads,
+                  size_t smem, int n_tiles, int gy, int *out) {
+  int per_sm = 0;
+  CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, kernel, threads, smem));
+  const long long slots =
+      (long long)std::max(1, per_sm) * std::max(1, ctx->n_sms);
+  const long long ctas = (long long)n_tiles * gy;
+  int best_s = 1;
+  if (ctas < 2 * slots) {
+    double best = 1e300;
+    for (int S = 1; S <= std::min(8, n_tiles); ++S) {
+      const double waves = std::ceil((double)(ctas * S) / (double)slots);
+      const double cost = waves / S * (1.0 + 0.02 * (S - 1));
+      if (cost < best) {
+        best = cost;
+        best_s = S;
+      }
+    }
+  }
+  *out = best_s;
+  return PYIID_OK;
+}
+
 int check_common(pyiid_ctx *ctx, int n_configs, const int32_t *offsets,
                  int n_species, int n_bins, double qbin, int k_begin) {
   if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
@@ -885,20 +913,42 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
   gradfq_coef_kernel<<<64, 256, 0, ctx->stream>>>(d_na, d_ftab, n_species,
                                                   n_bins, 1, coef);
   LAUNCH_CHECK(ctx);
+  int n_split = 1;
   if (kb0 < n_bins) {
     const GradEntry &E = kGradTable[ctx->grad_variant];
     const int Lb = E.v.L, cpc = E.v.CPC;
     const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
+    const int gy = (chunks_total + cpc - 1) / cpc;
+    const int n_tiles = (int)L->tiles.size();
+    const size_t smem = 3 * kTile * kTile * sizeof(float4);
+    // the packed kernels split the tiles J of a small configuration (the
+    // scalar ones never do)
+    if (E.v.NP == 0)
+      TRY(choose_jsplit(ctx, (const void *)E.k, kTile * cpc, smem, n_tiles,
+                        gy, &n_split));
+    const size_t gsize = (size_t)n_atoms * 3 * n_bins;
+    float *gout = grad;
+    if (n_split > 1) {
+      TRY(ensure(ctx, "grad_gpart", (size_t)n_split * gsize * sizeof(float),
+                 &p));
+      gout = static_cast<float *>(p);
+    }
     float dq_hi, dq_lo;
     split_double(qbin, dq_hi, dq_lo);
-    dim3 grid((unsigned)L->tiles.size(), (chunks_total + cpc - 1) / cpc);
-    E.k<<<grid, kTile * cpc, 3 * kTile * kTile * sizeof(float4),
-          ctx->stream>>>(positions, L->d_perm, L->d_tiles, L->d_cfg_tiles,
-                         dq_hi, dq_lo, kb0, chunks_total, n_bins, coef,
-                         n_species, grad);
+    dim3 grid((unsigned)n_tiles, gy, n_split);
+    E.k<<<grid, kTile * cpc, smem, ctx->stream>>>(
+        positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
+        chunks_total, n_bins, coef, n_species, gout,
+        JSplit{n_split, gsize, 0});
     LAUNCH_CHECK(ctx);
+    if (n_split > 1) {
+      combine_grad_parts_kernel<<<2 * std::max(1, ctx->n_sms), 256, 0,
+                                  ctx->stream>>>(gout, n_split, gsize, gsize,
+                                                 n_bins, kbo, grad);
+      LAUNCH_CHECK(ctx);
+    }
   }
-  if (kbo > 0)
+  if (kbo > 0 && n_split == 1)
     CUDA_TRY(ctx, cudaMemset2DAsync(grad, (size_t)n_bins * sizeof(float), 0,
                                     (size_t)kbo * sizeof(float),
                                     (size_t)3 * n_atoms, ctx->stream));
@@ -948,27 +998,9 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
     const int Lb = E.v.L, cpc = E.v.CPC;
     const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
     const int gy = (chunks_total + cpc - 1) / cpc;
-    // a configuration too small for two waves of CTAs splits the tiles J of
-    // every tile I over S <= 8 CTAs that write partial rows; S minimises
-    // waves / S (each CTA's work shrinks as 1/S), lightly penalising the
-    // partial rows each part adds
-    int per_sm = 0;
-    CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                      &per_sm, E.k, kTile * cpc, fqgrad_smem(E.v)));
-    const long long slots =
-        (long long)std::max(1, per_sm) * std::max(1, ctx->n_sms);
-    const long long ctas = (long long)n_tiles * gy;
-    if (ctas < 2 * slots) {
-      double best = 1e300;
-      for (int S = 1; S <= std::min(8, n_tiles); ++S) {
-        const double waves = std::ceil((double)(ctas * S) / (double)slots);
-        const double cost = waves / S * (1.0 + 0.02 * (S - 1));
-        if (cost < best) {
-          best = cost;
-          n_split = S;
-        }
-      }
-    }
+    // too few CTAs for two waves: split the tiles J over n_split CTAs
+    TRY(choose_jsplit(ctx, (const void *)E.k, kTile * cpc, fqgrad_smem(E.v),
+                      n_tiles, gy, &n_split));
     TRY(ensure(ctx, "fqgrad_part",
                (size_t)n_split * n_tiles * n_bins * sizeof(double), &p));
     fpart = static_cast<double *>(p);

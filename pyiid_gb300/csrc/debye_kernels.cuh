@@ -18,6 +18,18 @@ constexpr int kTile = 32;    // atoms per tile
 constexpr int kBlock = 256;  // threads per CTA of the pair kernels
 constexpr int kJMaxTiles = 32;  // max J tiles per F(Q) work item
 
+// Split of the tiles J of a configuration over gridDim.z = n CTAs per
+// (tile I, chunk block), for configurations too small to fill the GPU
+// otherwise: CTA z sweeps the z-th of n contiguous parts of the J tiles and
+// writes raw partial rows (no NaN mapping) at out + z * out_stride and its
+// F(Q) rows at fpart + z * fpart_stride; combine_grad_parts_kernel and the
+// finishing kernel add the parts in a fixed order.  n = 1: no split.
+struct JSplit {
+  int n;
+  size_t out_stride, fpart_stride;
+};
+
+
 // Tile descriptor: start (in sorted order), atom count, configuration, species.
 // (stored as int4)
 
@@ -286,7 +298,7 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
                   const int2 *__restrict__ cfg_tiles, float dq_hi,
                   float dq_lo, int kb0, int chunks_total, int n_bins,
                   const float *__restrict__ coef, int n_species,
-                  float *__restrict__ out) {
+                  float *__restrict__ out, JSplit /*no split: n == 1*/) {
   extern __shared__ float4 smem[];
   float4 *recA = smem;
   float4 *recB = smem + kTile * kTile;
@@ -705,17 +717,6 @@ struct BoolTag {
   static constexpr bool value = B;
 };
 
-// Split of the tiles J of a configuration over gridDim.z = n CTAs per
-// (tile I, chunk block), for configurations too small to fill the GPU
-// otherwise: CTA z sweeps the z-th of n contiguous parts of the J tiles and
-// writes raw partial rows (no NaN mapping) at out + z * out_stride and its
-// F(Q) rows at fpart + z * fpart_stride; combine_grad_parts_kernel and the
-// finishing kernel add the parts in a fixed order.  n = 1: no split.
-struct JSplit {
-  int n;
-  size_t out_stride, fpart_stride;
-};
-
 template <int L, int CPC, bool WITH_F>
 __device__ __forceinline__ void gradfq2_body(
     const float *__restrict__ pos, const int *__restrict__ perm,
@@ -971,10 +972,10 @@ __global__ void __launch_bounds__(kTile * CPC, MINB)
                    const int2 *__restrict__ cfg_tiles, float dq_hi,
                    float dq_lo, int kb0, int chunks_total, int n_bins,
                    const float *__restrict__ coef, int n_species,
-                   float *__restrict__ out) {
+                   float *__restrict__ out, JSplit js) {
   gradfq2_body<L, CPC, false>(pos, perm, tiles, cfg_tiles, dq_hi, dq_lo, kb0,
                               chunks_total, n_bins, coef, n_species, out,
-                              nullptr, nullptr, 0, JSplit{1, 0, 0});
+                              nullptr, nullptr, 0, js);
 }
 
 // F(Q) pair sums and dF/dx in one pass (see gradfq2_body).  Dynamic shared

@@ -266,3 +266,6 @@ def test_small_configurations_split_over_ctas(D, n):
     _, gd = D.fq_grad(dup, sp_d, tab, qbin, kb)
     gd = gd.cpu().numpy()
     assert np.all(gd[0] == 0) and np.all(gd[-1] == 0)
+    gd1 = D.grad_fq(dup, sp_d, tab, qbin, kb).cpu().numpy()
+    assert np.all(gd1[0] == 0) and np.all(gd1[-1] == 0)
+    assert rel(gd1, gd) <= 1e-6
