@@ -121,11 +121,12 @@ size_t fqgrad_smem(const GradVariant &v) {
          (2 * (size_t)v.CPC * v.CPC * v.L + kTile * kTile) * sizeof(float);
 }
 constexpr int kNumFq = sizeof(kFqTable) / sizeof(kFqTable[0]);
-// Default F(Q) launch shape of a new context: {24, -3}, the per-tile-pair
-// group reduction at 3 CTAs per SM.  It is the fastest shape on batches of
-// small configurations and within a few per cent of the fastest on single
-// configurations of 20,000 atoms; the autotuner may pick another.
-constexpr int kDefaultFq = 18;
+// Default F(Q) launch shape of a new context: {56, -3}, the per-tile-pair
+// group reduction with 56 bins per thread at 3 CTAs per SM.  The tuner
+// picks it on 330, 498 and 500-bin workloads (64 x 1,000 atoms, 256
+// alloys, one 1,000-atom particle) and it is within 1 % of the fastest at
+// 1,475 bins and 20,000 atoms; the autotuner may pick another.
+constexpr int kDefaultFq = 23;
 constexpr int kNumGrad = sizeof(kGradTable) / sizeof(kGradTable[0]);
 
 // Dynamic shared memory of an F(Q) launch with n_chunks chunks per CTA

@@ -274,7 +274,7 @@ def test_autotune_selects_and_caches(D, tmp_path, monkeypatch):
     ctx.set_variant('grad_fq', 0)
 
 
-DEFAULT_FQ_VARIANT = 18
+DEFAULT_FQ_VARIANT = 23
 
 
 def test_new_context_starts_on_the_group_reduction_variant(D):
@@ -288,7 +288,7 @@ def test_new_context_starts_on_the_group_reduction_variant(D):
     finally:
         ctx.close()
     info = dict(autotune.variants('fq'))[DEFAULT_FQ_VARIANT]
-    assert (info['bins_per_thread'], info['pairs_per_thread']) == (24, -3)
+    assert (info['bins_per_thread'], info['pairs_per_thread']) == (56, -3)
 
 
 def test_batch_fq_uneven_alloys_matches_oracle(D):

@@ -56,7 +56,7 @@ def test_null_context_is_rejected():
 
 def test_variant_tables_are_described_without_a_gpu():
     """Launch-shape tables (host-only calls): counts, parameters, and the
-    context's default F(Q) shape {24, -3} at index 18."""
+    context's default F(Q) shape {56, -3} at index 23."""
     from pyiid_gb300 import _native
     from pyiid_gb300.autotune import variants
     lib = _native.load()
@@ -71,7 +71,7 @@ def test_variant_tables_are_described_without_a_gpu():
     p = (ctypes.c_int32 * 3)()
     assert lib.pyiid_variant_info(0, 10 ** 6, p, 3) != 0
     fq = dict(variants('fq'))
-    assert (fq[18]['bins_per_thread'], fq[18]['pairs_per_thread']) == (24, -3)
+    assert (fq[23]['bins_per_thread'], fq[23]['pairs_per_thread']) == (56, -3)
     for _, info in variants('fq_grad'):
         assert info['pairs_per_thread'] == 0          # packed kernels only
         assert info['threads'] % 32 == 0 and 32 % (info['threads'] // 32) == 0
