@@ -140,9 +140,20 @@ size_t fq_smem(const FqVariant &v, int n_chunks = -1) {
          2 * (size_t)v.L * kBlock * sizeof(float);
 }
 
+// Cache key of host arrays (r grids, species, form-factor tables) that are
+// hashed on every call: eight bytes per step (an FNV-style multiply followed
+// by an xor-shift so that high bits reach the low ones), then the tail byte
+// by byte.  A 4,000-point r grid takes a few microseconds.
 uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) {
   const unsigned char *p = static_cast<const unsigned char *>(data);
-  for (size_t i = 0; i < n; ++i) {
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w;
+    std::memcpy(&w, p + i, 8);
+    h = (h ^ w) * 1099511628211ull;
+    h ^= h >> 29;
+  }
+  for (; i < n; ++i) {
     h ^= p[i];
     h *= 1099511628211ull;
   }

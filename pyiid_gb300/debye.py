@@ -30,11 +30,17 @@ def _ptr(a, ctype):
     return a.ctypes.data_as(ctypes.POINTER(ctype))
 
 
+_cuda_seen = False
+
+
 def as_positions(x, device=None):
     """float32 contiguous CUDA tensor [N, 3] from an array or tensor."""
-    if not torch.cuda.is_available():
-        raise NativeError('no CUDA device is visible; pyiid_gb300 runs only '
-                          'on a GB300 (sm_103a) GPU')
+    global _cuda_seen
+    if not _cuda_seen:  # a device, once seen, stays (the check costs µs)
+        if not torch.cuda.is_available():
+            raise NativeError('no CUDA device is visible; pyiid_gb300 runs '
+                              'only on a GB300 (sm_103a) GPU')
+        _cuda_seen = True
     if isinstance(x, torch.Tensor):
         t = x.detach()
         if not t.is_cuda:

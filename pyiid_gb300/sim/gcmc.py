@@ -32,6 +32,22 @@ from . import Ensemble
 
 __all__ = ['add_atom', 'del_atom', 'GrandCanonicalEnsemble']
 
+# ElasticScatter's per-atom caches on Atoms (rebuilt on demand whenever the
+# atom count differs from info['scatter_atoms'])
+_SCATTER_CACHE = ('F(Q) scatter', 'PDF scatter', 'GB300 species')
+
+
+def _copy_without_scatter_cache(atoms):
+    """atoms.copy() without the scatter caches: the O(N K) engine never
+    reads them, an insertion or removal invalidates them anyway, and at a
+    few hundred atoms copying them dominates the cost of a move."""
+    saved = {k: atoms.arrays.pop(k) for k in _SCATTER_CACHE
+             if k in atoms.arrays}
+    try:
+        return atoms.copy()
+    finally:
+        atoms.arrays.update(saved)
+
 
 def _insertion_position(atoms, random_state, resolution):
     """New-atom position as pyiid/sim/gcmc.py:44-51 draws it."""
@@ -199,7 +215,7 @@ class GrandCanonicalEnsemble(Ensemble):
         if not ok:
             return None
         eng.accept(MOVE_INSERT, 0, new_position)
-        atoms_prime = atoms.copy()
+        atoms_prime = _copy_without_scatter_cache(atoms)
         atoms_prime.append(Atom(new_symbol, np.asarray(new_position)))
         return self._attach(atoms_prime, atoms)
 
@@ -221,7 +237,7 @@ class GrandCanonicalEnsemble(Ensemble):
         if not ok:
             return None
         eng.accept(MOVE_REMOVE, idx)
-        atoms_prime = atoms.copy()
+        atoms_prime = _copy_without_scatter_cache(atoms)
         del atoms_prime[idx]
         return self._attach(atoms_prime, atoms)
 
