@@ -337,6 +337,115 @@ def run_gpu(args, rank, world, local):
     return line
 
 
+def run_gpu_sharded(args, rank, world, local):
+    """The 20,000-atom particle split across the ranks (strong scaling):
+    every rank evaluates its part of the tile list in one pass
+    (pyiid_fq_grad_part: its atoms' complete gradient rows and the raw Debye
+    sums of the pairs its tiles own), the K raw sums are all-reduced, and
+    every rank forms F(Q) (pyiid_fq_from_sums).  A step is one evaluation of
+    the one particle; the time is the maximum over ranks, including the
+    all-reduce."""
+    import torch
+    from pyiid_gb300 import autotune, debye
+    from pyiid_gb300._native import context
+    from pyiid_gb300.distributed import max_over_ranks
+    dev = torch.device('cuda', local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    pos, sp, tab, n_bins, k_begin = workload(args.n_atoms)
+    n = len(pos)
+    pairs = n * (n - 1) // 2
+    k_ret = n_bins - k_begin
+    pos_d = torch.as_tensor(pos, device=dev)
+    grad = torch.zeros((n, 3, n_bins), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    ctx = context(local)
+    out = {}
+
+    def step():
+        sums, _, rows = debye.fq_grad_part(pos_d, sp, tab, QBIN, k_begin,
+                                           rank, world, out_grad=grad)
+        if dist is not None:
+            dist.all_reduce(sums, op=dist.ReduceOp.SUM)
+        out['fq'] = debye.fq_from_sums(sp, tab, k_begin, sums)
+        out['rows'] = rows
+
+    for _ in range(args.warmup):
+        step()
+    if not args.no_tune:
+        autotune.tune_call(step, kernels=('fq_grad',), reps=2)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for s, e in ev:
+            flush.zero_()
+            s.record(stream)
+            step()
+            e.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = ctx.launches - launches0
+    ms_step = max_over_ranks(float(np.mean([s.elapsed_time(e) for s, e in ev])),
+                             device=dev)
+    own = torch.as_tensor(np.flatnonzero(out['rows']), device=dev)
+    h_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    h_pos.copy_(torch.as_tensor(pos))
+    h_fq = torch.empty(n_bins, dtype=torch.float32, pin_memory=True)
+    h_rows = torch.empty((len(own), 3, n_bins), dtype=torch.float32,
+                         pin_memory=True)
+    times = []
+    for i in range(max(3, min(args.steps, 10)) + 1):
+        flush.zero_()
+        s, e = (torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True))
+        s.record(stream)
+        pos_d.copy_(h_pos, non_blocking=True)
+        step()
+        h_fq.copy_(out['fq'], non_blocking=True)
+        h_rows.copy_(grad.index_select(0, own), non_blocking=True)
+        e.record(stream)
+        e.synchronize()
+        if i:
+            times.append(s.elapsed_time(e))
+    e2e_ms = max_over_ranks(float(np.mean(times)), device=dev)
+    assert torch.isfinite(grad).all() and out['fq'][k_begin:].abs().sum() > 0
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank != 0:
+        return None
+    return {
+        'metric': METRIC, 'value': 1.0 / (ms_step * 1e-3), 'unit': 'evals/s',
+        'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms_step, 'higher_is_better': True,
+        'scaling': 'strong', 'vs_baseline': None,
+        'dtype': 'fp32 (FP64 final reductions)',
+        'data': 'synthetic (seeded fcc Pt)',
+        'config': config_dict(n_bins, k_begin, {
+            'parallelism': f'one particle split over {world} ranks '
+                           '(tile ranges; all-reduce of the K raw sums)',
+            'path': 'pyiid_fq_grad_part + pyiid_fq_from_sums'}, n),
+        'pair_bin_terms_per_s': 2 * pairs * k_ret / (ms_step * 1e-3),
+        'wall_s_timed_region': wall,
+        'gpu_launches': int(launches),
+        'e2e': {'value': 1.0 / (e2e_ms * 1e-3), 'unit': 'evals/s',
+                'h2d_bytes_per_step': int(h_pos.numel() * 4),
+                'd2h_bytes_per_step': int(h_fq.numel() * 4 +
+                                          h_rows.numel() * 4)},
+        'clocks': clk.summary(),
+    }
+
+
 def issue_roofline(torch, dev, pairs, k_ret, k_ms, sm_mhz, kernel, lane_ops):
     """FP32 issue roofline of the dF/dx (or one-pass F + dF/dx) launch:
     lane operations its inner loop issues per second (each unordered
@@ -1002,6 +1111,9 @@ def main():
                     help='skip the CPU baseline sample')
     ap.add_argument('--no-workloads', action='store_true',
                     help='skip the batched and HMC secondary workloads')
+    ap.add_argument('--shard-particle', action='store_true',
+                    help='split the one particle across the ranks (strong '
+                         'scaling) instead of running replicas')
     ap.add_argument('--no-tune', action='store_true',
                     help='use the default launch shapes (no autotuning)')
     ap.add_argument('--only-workload', default=None,
@@ -1023,7 +1135,8 @@ def main():
     if args.impl == 'reference':
         line = run_reference(args, rank, world)
     else:
-        line = run_gpu(args, rank, world, local)
+        run = run_gpu_sharded if args.shard_particle else run_gpu
+        line = run(args, rank, world, local)
         if line is not None and world == 1 and not args.no_cpu:
             from oracle import build_oracle
             build_oracle.build()
