@@ -22,6 +22,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -83,7 +84,8 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(REPO, 'gpurun_out', f'clocks_{os.getpid()}.csv')
+        self.path = os.path.join(tempfile.gettempdir(),
+                                 f'pyiid_gb300_clocks_{os.getpid()}.csv')
 
     def __enter__(self):
         try:

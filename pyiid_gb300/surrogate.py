@@ -15,7 +15,7 @@ and only then with
     a2 = min(1, exp(-(E(x') - E(x)) / kT + (E~(x') - E~(x)) / kT))
 using the exact Debye energy E.  The product kernel satisfies detailed
 balance with respect to exp(-E/kT): the chain's target is unchanged and the
-exact potential remains the judge of every accepted move.
+exact potential still decides every accepted move.
 """
 import ctypes
 
