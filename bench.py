@@ -258,7 +258,9 @@ def run_gpu(args, rank, world, local):
     assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
 
     workloads = {}
-    if rank == 0 and not args.no_workloads:
+    # the secondary workloads are single-GPU measurements: N = 1 only (with
+    # N > 1 the other ranks would wait on rank 0 at the barrier below)
+    if world == 1 and not args.no_workloads:
         for name, fn in (('fq_grad_au1000', run_fq_grad_au1000),
                          ('pdf_transforms_au1000', run_pdf_transforms),
                          ('batched_fq_256_alloys', run_batched),
