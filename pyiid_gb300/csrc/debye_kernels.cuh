@@ -10,6 +10,8 @@
 // small finishing kernels apply them.
 #pragma once
 
+#include <cstdint>
+
 #include "pair_math.cuh"
 
 namespace pyiid {
@@ -1024,8 +1026,8 @@ __global__ void fqgrad_finish_kernel(const double *__restrict__ fpart,
 
 // grad[i] = nan_to_num(sum over parts p of parts[p * stride + i]) for bins
 // k >= kbo, 0 below: the J-split parts of gradfq2_body added in part order.
-// Four elements per thread (n, stride and both pointers 16-byte aligned:
-// n_bins % 4 == 0), else one.
+// Four elements per thread when n_bins % 4 == 0 and both pointers are
+// 16-byte aligned (the caller's gradient may be any float array), else one.
 __device__ __forceinline__ float nan_to_num_f(float v) {
   return isnan(v) ? 0.f : (isinf(v) ? copysignf(3.402823466e38f, v) : v);
 }
@@ -1036,7 +1038,9 @@ __global__ void combine_grad_parts_kernel(const float *__restrict__ parts,
                                           float *__restrict__ grad) {
   const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t nt = (size_t)gridDim.x * blockDim.x;
-  if (n_bins % 4 == 0) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(parts) |
+                         reinterpret_cast<uintptr_t>(grad)) & 15) == 0;
+  if (n_bins % 4 == 0 && aligned) {
     const float4 *p4 = reinterpret_cast<const float4 *>(parts);
     float4 *g4 = reinterpret_cast<float4 *>(grad);
     for (size_t i = t0; i < n / 4; i += nt) {

@@ -8,6 +8,7 @@
 // from HBM/L2 once per CTA column block.
 #pragma once
 
+#include <cstdint>
 #include <cuda_runtime.h>
 
 namespace pyiid {
@@ -312,7 +313,9 @@ __global__ void __launch_bounds__(256)
     buf ^= 1;
   }
 
-  const bool vec_o = (n_r % 2) == 0;
+  // double2 stores need 16-byte alignment of every row start
+  const bool vec_o =
+      (n_r % 2) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int gr = row0 + ty * 8 + i;
