@@ -269,3 +269,20 @@ def test_small_configurations_split_over_ctas(D, n):
     gd1 = D.grad_fq(dup, sp_d, tab, qbin, kb).cpu().numpy()
     assert np.all(gd1[0] == 0) and np.all(gd1[-1] == 0)
     assert rel(gd1, gd) <= 1e-6
+
+
+def test_split_combine_into_an_output_at_an_odd_offset(D):
+    """A small configuration (J-split, partial rows combined) written into a
+    gradient that starts 4 bytes past a 16-byte boundary: the combine takes
+    its scalar path and the result equals the aligned call bitwise."""
+    import torch
+    pos = S.displaced(S.fcc_nearest(4.08, 300), 0.05, 3)
+    qbin, nb, kb = 0.05, 500, 2
+    sp, tab, _ = species_tables([79] * 300, qbin, nb)
+    f, g = D.fq_grad(pos, sp, tab, qbin, kb)
+    big = torch.full((300 * 3 * nb + 4,), float('nan'), device='cuda')
+    out = big[1:1 + 300 * 3 * nb].view(300, 3, nb)
+    assert out.data_ptr() % 16 == 4
+    f2, g2 = D.fq_grad(pos, sp, tab, qbin, kb, out_grad=out)
+    assert torch.equal(g2, g) and torch.equal(f2, f)
+    assert torch.isnan(big[0]) and torch.isnan(big[-3:]).all()

@@ -55,3 +55,29 @@ def test_batched_pdf_matches_oracle(D, b, k, n_r, qmin):
     T = O.tmatrix(k, rstep, qstep, rg, qmin)
     want = f.astype(np.float64) @ T
     assert rel(got, want) <= TOL, rel(got, want)
+
+
+def test_grad_pdf_into_an_output_at_an_odd_offset(D):
+    """The compat gradient GEMM writing rows that start 8 bytes past a
+    16-byte boundary takes its scalar stores and equals the aligned call."""
+    import ctypes
+    from pyiid_gb300._native import context
+    n, k, n_r = 20, 330, 400
+    rng = np.random.default_rng(3)
+    g = torch.as_tensor(rng.standard_normal((n, 3, k)).astype(np.float32),
+                        device='cuda')
+    qstep, rstep = 0.0756865, 0.01
+    rg = np.arange(n_r) * rstep
+    want = D.grad_pdf(g, qstep, rstep, rg, 0.0)
+    big = torch.full((n * 3 * n_r + 2,), float('nan'), dtype=torch.float64,
+                     device='cuda')
+    ptr = big.data_ptr() + 8
+    assert ptr % 16 == 8
+    rgc = np.ascontiguousarray(rg, np.float64)
+    context().call('pyiid_grad_pdf', ctypes.c_void_p(g.data_ptr()), n, k,
+                   float(qstep), float(rstep),
+                   rgc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n_r,
+                   0.0, ctypes.c_void_p(ptr))
+    got = big[1:1 + n * 3 * n_r].view(n, 3, n_r)
+    assert torch.equal(got, want)
+    assert torch.isnan(big[0]) and torch.isnan(big[-1])
