@@ -877,7 +877,7 @@ __device__ __forceinline__ void gradfq2_body(
         PairPhase2 p = pair_phase2(pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dq_hi,
                                    dq_lo, dx, dy, dz);
         const float beta = -(p.inv_r * p.inv_r * p.inv_r);
-        const float gam = -p.r * dq_hi / (2.0f * p.ch);
+        const float gam = __fdividef(-p.r * dq_hi, 2.0f * p.ch);  // 2ch in [1.41, 2]
         ra = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
         // beta sh is rebuilt as (kappa/2) beta; its slot and c.w (recD
         // with F(Q)) carry (sin theta, cos theta) for the rotated odd seed
@@ -1153,7 +1153,7 @@ __global__ void __launch_bounds__(kBlock)
                                    dq_lo, dx, dy, dz);
         const float beta = -(p.inv_r * p.inv_r * p.inv_r);
         const float2 c1 = f2(beta * p.ch), c2 = f2(beta * p.sh);
-        const float gam = -p.r * dq_hi / (2.0f * p.ch);
+        const float gam = __fdividef(-p.r * dq_hi, 2.0f * p.ch);  // 2ch in [1.41, 2]
         const float2 kpos = f2(p.kappa), kneg = f2(-p.kappa);
         float2 ae = f2(0.f), ao = f2(0.f), be = f2(0.f), bo = f2(0.f);
         for (int blk = 0; blk < kh; blk += RS / 2) {
@@ -1285,7 +1285,7 @@ __global__ void __launch_bounds__(kBlock)
                                    dq_lo, dx, dy, dz);
         const float beta = -(p.inv_r * p.inv_r * p.inv_r);
         const float2 c1 = f2(beta * p.ch), c2 = f2(beta * p.sh);
-        const float gam = -p.r * dq_hi / (2.0f * p.ch);
+        const float gam = __fdividef(-p.r * dq_hi, 2.0f * p.ch);  // 2ch in [1.41, 2]
         const float2 kpos = f2(p.kappa), kneg = f2(-p.kappa);
         float2 ae = f2(0.f), ao = f2(0.f), be = f2(0.f), bo = f2(0.f);
         for (int blk = 0; blk < kh; blk += RS / 2) {

@@ -163,6 +163,26 @@ struct PairPhase2 {
   float r, inv_r;
 };
 
+// sin and cos of x for |x| <= pi/4 by their Taylor series about 0 through
+// x^9 and x^10 (coefficients 1/n!): the first omitted terms are below 2e-9
+// there, under float rounding; Horner evaluation adds about one rounding.
+__device__ __forceinline__ void sincos_quarter_turn(float x, float &s,
+                                                    float &c) {
+  const float x2 = x * x;
+  s = fmaf(x * x2,
+           fmaf(x2, fmaf(x2, fmaf(x2, 2.7557319e-6f, -1.9841270e-4f),
+                         8.3333333e-3f),
+                -1.6666667e-1f),
+           x);
+  c = fmaf(x2,
+           fmaf(x2,
+                fmaf(x2, fmaf(x2, fmaf(x2, -2.7557319e-7f, 2.4801587e-5f),
+                              -1.3888889e-3f),
+                     4.1666667e-2f),
+                -0.5f),
+           1.0f);
+}
+
 __device__ __forceinline__ PairPhase2 pair_phase2(float ax, float ay, float az,
                                                   float bx, float by, float bz,
                                                   float dq_hi, float dq_lo,
@@ -185,7 +205,8 @@ __device__ __forceinline__ PairPhase2 pair_phase2(float ax, float ay, float az,
   fast_two_sum(h2, lo, r2h, r2l);
   float rh = __fsqrt_rn(r2h);
   float res = __fmaf_rn(-rh, rh, r2h);
-  float rl = __fmul_rn(__fadd_rn(res, r2l), __fdiv_rn(0.5f, rh));
+  const float inv_r = __frcp_rn(rh);
+  float rl = __fmul_rn(__fadd_rn(res, r2l), 0.5f * inv_r);
   float th, tl;
   two_prod(dq_hi, rh, th, tl);
   tl = __fadd_rn(tl, __fmaf_rn(dq_hi, rl, __fmul_rn(dq_lo, rh)));
@@ -201,8 +222,8 @@ __device__ __forceinline__ PairPhase2 pair_phase2(float ax, float ay, float az,
   two_sum(x, y, q_hi, q_lo);
   int mi = (int)m;
   p.sigma2 = (mi & 1) ? -1.0f : 1.0f;
-  float hs, hc;
-  sincosf(0.5f * q_hi, &hs, &hc);
+  float hs, hc;  // |q_hi| <= pi/2
+  sincos_quarter_turn(0.5f * q_hi, hs, hc);
   const float hl = 0.5f * q_lo;
   p.sh = __fmaf_rn(hc, hl, hs);
   p.ch = __fmaf_rn(-hs, hl, hc);
@@ -215,7 +236,7 @@ __device__ __forceinline__ PairPhase2 pair_phase2(float ax, float ay, float az,
     default: p.sth = -p.ch; p.cth = p.sh; break;
   }
   p.r = rh;
-  p.inv_r = __frcp_rn(rh);
+  p.inv_r = inv_r;
   return p;
 }
 
