@@ -240,22 +240,48 @@ def run_gpu(args, rank, world, local):
     h_fq = torch.empty(n_bins, dtype=torch.float32, pin_memory=True)
     h_grad = torch.empty((n, 3, n_bins), dtype=torch.float32, pin_memory=True)
     e2e_steps = max(3, min(args.steps, 10))
-    times = []
-    for i in range(e2e_steps + 1):
-        flush.zero_()
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record(stream)
+
+    def copy_out():
+        # the step into device buffers, then explicit copies to pinned host
         pos_d.copy_(h_pos, non_blocking=True)
         step()
         h_fq.copy_(fq, non_blocking=True)
         h_grad.copy_(grad, non_blocking=True)
-        e.record(stream)
-        e.synchronize()
-        if i:
-            times.append(s.elapsed_time(e))
-    e2e_ms = max_over_ranks(float(np.mean(times)), device=dev)
+
+    def write_host():
+        # one pass whose kernels write F and dF/dx straight into the pinned
+        # host buffers over the host link, overlapped with the pair work
+        pos_d.copy_(h_pos, non_blocking=True)
+        debye.fq_grad(pos_d, sp, tab, QBIN, k_begin, out_fq=h_fq,
+                      out_grad=h_grad)
+
+    def e2e_time(fn):
+        times = []
+        for i in range(e2e_steps + 1):
+            flush.zero_()
+            s, e = (torch.cuda.Event(enable_timing=True),
+                    torch.cuda.Event(enable_timing=True))
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            if i:
+                times.append(s.elapsed_time(e))
+        return float(np.mean(times))
+
+    e2e_copy_ms = e2e_time(copy_out)
     # correctness guard on what was timed: finite, nonzero
     assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
+    h_grad.zero_()
+    e2e_host_ms = e2e_time(write_host)
+    # the host-written results are those of the same call on device buffers,
+    # bit for bit
+    fused()
+    assert torch.equal(h_grad, grad.cpu()) and torch.equal(h_fq, fq.cpu())
+    e2e_ms = max_over_ranks(min(e2e_copy_ms, e2e_host_ms), device=dev)
+    e2e_path = ('kernels write the pinned host outputs (pyiid_fq_grad)'
+                if e2e_host_ms < e2e_copy_ms else
+                'device outputs, then cudaMemcpyAsync to pinned host')
 
     workloads = {}
     # the secondary workloads are single-GPU measurements: N = 1 only (with
@@ -314,7 +340,9 @@ def run_gpu(args, rank, world, local):
         'gpu_launches': int(launches),
         'e2e': {'value': world / (e2e_ms * 1e-3), 'unit': 'evals/s',
                 'h2d_bytes_per_step': int(h_pos.numel() * 4),
-                'd2h_bytes_per_step': int(h_fq.numel() * 4 + h_grad.numel() * 4)},
+                'd2h_bytes_per_step': int(h_fq.numel() * 4 + h_grad.numel() * 4),
+                'path': e2e_path,
+                'ms_copy_out': e2e_copy_ms, 'ms_kernels_write_host': e2e_host_ms},
         'roofline': {
             'bound': 'fp32',
             'kernel': kernel,
@@ -610,22 +638,39 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
     h_pos.copy_(torch.as_tensor(pos))
     h_fq = torch.empty(n_bins, dtype=torch.float32, pin_memory=True)
     h_grad = torch.empty((n, 3, n_bins), dtype=torch.float32, pin_memory=True)
-    e2e = []
-    for i in range(reps + 1):
-        flush.zero_()
-        s, e = (torch.cuda.Event(enable_timing=True),
-                torch.cuda.Event(enable_timing=True))
-        s.record(stream)
+    def copy_out():
         pos_d.copy_(h_pos, non_blocking=True)
         evaluate()
         h_fq.copy_(fq, non_blocking=True)
         h_grad.copy_(grad, non_blocking=True)
-        e.record(stream)
-        e.synchronize()
-        if i:
-            e2e.append(s.elapsed_time(e))
-    e2e_ms = float(np.mean(e2e))
+
+    def write_host():
+        # the kernels write F and dF/dx straight into the pinned host buffers
+        pos_d.copy_(h_pos, non_blocking=True)
+        debye.fq_grad(pos_d, sp, tab, qbin, k_begin, out_fq=h_fq,
+                      out_grad=h_grad)
+
+    def e2e_time(fn):
+        e2e = []
+        for i in range(reps + 1):
+            flush.zero_()
+            s, e = (torch.cuda.Event(enable_timing=True),
+                    torch.cuda.Event(enable_timing=True))
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            if i:
+                e2e.append(s.elapsed_time(e))
+        return float(np.mean(e2e))
+
+    e2e_copy_ms = e2e_time(copy_out)
     assert torch.isfinite(grad).all() and fq[k_begin:].abs().sum() > 0
+    h_grad.zero_()
+    e2e_host_ms = e2e_time(write_host)
+    fused()
+    assert torch.equal(h_grad, grad.cpu()) and torch.equal(h_fq, fq.cpu())
+    e2e_ms = min(e2e_copy_ms, e2e_host_ms)
 
     from oracle import build_oracle, debye_c
     build_oracle.build()
@@ -647,6 +692,8 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
             'e2e_evals_per_s': 1e3 / e2e_ms,
             'e2e_bytes': {'h2d': int(h_pos.numel() * 4),
                           'd2h': int((h_fq.numel() + h_grad.numel()) * 4)},
+            'e2e_ms': {'copy_out': e2e_copy_ms,
+                       'kernels_write_host': e2e_host_ms},
             'variants': {k: v['best'] for k, v in tuned.items()},
             'path': ('one pass (pyiid_fq_grad)' if evaluate is fused
                      else 'two passes (pyiid_fq, pyiid_grad_fq)'),

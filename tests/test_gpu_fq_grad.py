@@ -212,14 +212,18 @@ def test_sharded_call_on_one_rank_is_the_one_pass_call(D):
     assert rel(f.cpu().numpy(), f1.cpu().numpy()) <= 1e-6
 
 
-def test_zero_copy_outputs_in_pinned_host_memory(D):
+# 150 atoms: J tiles split over CTAs, the combine writes the host rows;
+# 7,000 atoms (two species): one part, the pair kernel writes the host rows
+# itself and adds the second species block to what it wrote for the first
+@pytest.mark.parametrize('n,seed,edge', [(150, 13, 14.0), (7000, 17, 45.0)])
+def test_zero_copy_outputs_in_pinned_host_memory(D, n, seed, edge):
     """Pinned CPU outputs are written by the kernel over the host link and
     equal the device outputs bitwise; pageable host memory is rejected
     (Python check and the library's pointer check) before any launch."""
     import ctypes
     import torch
     from pyiid_gb300._native import NativeError, context
-    pos, nums = alloy(150, 13, 14.0)
+    pos, nums = alloy(n, seed, edge)
     qbin, nb, kb = 0.05, 500, 3
     sp, tab, _ = species_tables(nums, qbin, nb)
     f, g = D.fq_grad(pos, sp, tab, qbin, k_begin=kb)
