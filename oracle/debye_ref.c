@@ -32,15 +32,17 @@
 /* ------------------------------------------------------------ FP64 oracle */
 
 /* S_k for the requested bins: sum_{a>b} f_a f_b sin(Q_k r)/r, Q_k = k*qbin.
- * pos float32 [n][3], species [n], ftab [S][K]. */
+ * pos float32 [n][3], species [n], ftab [S][K].  Each bin's sum over the
+ * rows a is split across the threads (a handful of bins at 20,000 atoms
+ * still uses every core). */
 void oracle_pair_sums(const float *pos, const int32_t *species, int n,
                       const float *ftab, int n_bins, double qbin,
                       const int32_t *bins, int nb, double *out) {
-#pragma omp parallel for schedule(dynamic, 1)
   for (int ib = 0; ib < nb; ++ib) {
     const int k = bins[ib];
     const double Q = (double)k * qbin;
     double s = 0.0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : s)
     for (int a = 1; a < n; ++a) {
       const double fa = ftab[(size_t)species[a] * n_bins + k];
       double sa = 0.0;
