@@ -75,3 +75,54 @@ def test_variant_tables_are_described_without_a_gpu():
     for _, info in variants('fq_grad'):
         assert info['pairs_per_thread'] == 0          # packed kernels only
         assert info['threads'] % 32 == 0 and 32 % (info['threads'] // 32) == 0
+
+
+def header_prototypes():
+    """name -> (return type text, [parameter type texts]) from the header."""
+    src = open(os.path.join(REPO, 'include', 'pyiid_gb300.h')).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    src = re.sub(r'//[^\n]*', '', src)
+    protos = {}
+    for m in re.finditer(r'([A-Za-z_][\w\s\*]*?)\b(pyiid_[a-z_0-9]+)\s*\(([^)]*)\)\s*;',
+                         src):
+        ret, name, params = m.group(1).strip(), m.group(2), m.group(3)
+        params = ' '.join(params.split())
+        plist = [] if params in ('', 'void') else [p.strip()
+                                                   for p in params.split(',')]
+        protos[name] = (ret, plist)
+    return protos
+
+
+def _kind_of_c(t):
+    t = t.replace('const ', '')
+    if '*' in t:
+        return 'ptr'
+    base = t.split()[0]
+    return {'int': 'i32', 'int32_t': 'i32', 'int64_t': 'i64', 'size_t': 'u64',
+            'uint64_t': 'u64', 'float': 'f32', 'double': 'f64'}[base]
+
+
+def _kind_of_ctypes(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, 'contents'):
+        return 'ptr'
+    return {ctypes.c_int: 'i32', ctypes.c_int32: 'i32', ctypes.c_int64: 'i64',
+            ctypes.c_uint64: 'u64', ctypes.c_size_t: 'u64',
+            ctypes.c_float: 'f32', ctypes.c_double: 'f64'}[t]
+
+
+def test_binding_matches_every_prototype():
+    """Every ctypes declaration in _native has the header prototype's
+    argument count, and each argument and the return value the same kind
+    (pointer, 32/64-bit integer, float, double): a mismatch would pass
+    garbage through the C ABI without any error."""
+    from pyiid_gb300 import _native
+    protos = header_prototypes()
+    assert set(protos) == set(_native.symbols())
+    for name, (ret, params) in protos.items():
+        res, args = _native._SIGNATURES[name]
+        assert len(args) == len(params), (name, len(args), len(params))
+        for i, (c, py) in enumerate(zip(params, args)):
+            # drop the parameter name: the last identifier of the text
+            ctype = re.sub(r'\b\w+$', '', c).strip() or c
+            assert _kind_of_c(ctype) == _kind_of_ctypes(py), (name, i, c)
+        assert _kind_of_c(ret) == _kind_of_ctypes(res), (name, ret)
