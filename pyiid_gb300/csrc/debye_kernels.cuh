@@ -8,6 +8,16 @@
 //   D^{sa sb}_k = sum over pairs of that species pair of sin(Q_k r)/r.
 // The kernels therefore never read form factors in their inner loops; the
 // small finishing kernels apply them.
+//
+// Reference formulas restated (pyIID, pyiid/experiments/elasticscatter/):
+//   pair vectors and distances      kernels/cpu_flat.py:16-52
+//                                   (GPU twin kernels/gpu_flat.py:11-49)
+//   f_i f_j normalisation array     kernels/cpu_flat.py:57-74
+//   omega = sin(Q r)/r, F terms     kernels/cpu_flat.py:79-114, gpu_flat.py:73-112
+//   gradient of omega and of F      kernels/cpu_flat.py:122-194, gpu_flat.py:116-166
+//   gradient scatter (signs)        kernels/cpu_experimental.py:8-15
+//   sums, na, x2, nan_to_num        cpu_wrappers/flat_multi_cpu_wrap.py:22-102
+//   Rw / chi^2 gradients (adjoint)  kernels/master_kernel.py:293-376, 392-396
 #pragma once
 
 #include <cstdint>
@@ -220,6 +230,8 @@ __device__ __forceinline__ float fq_value(double s, double na) {
 // Finishing kernel for F(Q): for configuration b and bin k
 //   S_k  = sum_sp f_sa f_sb sum_{items of key (b, sp)} partial[item][k]
 //   F_k  = 2 * nan_to_num(float(S_k / na_k))
+// as wrap_fq does (cpu_wrappers/flat_multi_cpu_wrap.py:44-60: FP64 sum of the
+// FP32 pair terms, na = N mean_{i>j} f_i f_j, factor 2, nan_to_num).
 // na is precomputed per (config, bin) on the host in FP64 (it depends only on
 // species counts and form factors).  Configurations with < 2 atoms give 0.
 __global__ void fq_finish_kernel(const double *__restrict__ partial,
@@ -254,6 +266,10 @@ __global__ void fq_finish_kernel(const double *__restrict__ partial,
 }
 
 // ==================================================================== dF/dx
+// The value of wrap_fq_grad (cpu_wrappers/flat_multi_cpu_wrap.py:63-102):
+// row a = -(1/na) sum_b f_a f_b (Q cos(Q r) - sin(Q r)/r)/r^2 (x_a - x_b),
+// i.e. -1/2 dF/dx_a (kernels/cpu_flat.py:122-194 with the scatter signs of
+// kernels/cpu_experimental.py:8-15; no factor 2, nan_to_num of the rows).
 // Owner-computes: CTA (tile I, chunk block) with threads (atom a, chunk cl);
 // every thread sweeps all tiles J of its configuration and accumulates the
 // 3 x L gradient bins of its atom, so no atomics or partials are needed.
@@ -1095,6 +1111,10 @@ __global__ void zero_low_bins_kernel(const int *__restrict__ perm,
 }
 
 // =================================================================== adjoint
+// Exact position gradient of Rw or chi^2 (get_grad_rw / get_grad_chi_sq,
+// kernels/master_kernel.py:293-376, with get_grad_scale :392-396), which the
+// reference forms as a contraction of the [N, 3, R] grad_pdf array; both are
+// linear in dG, so the contraction moves back through G = T F to the bins:
 // d(potential)/dx_a = sum_b (x_a - x_b) s_ab,  s_ab = sum_k W^{sa sb}_k g_k(r_ab)
 // with W_k = 2 w_k f_sa f_sb / na_k and w = T c the back-projected G(r)
 // adjoint.  Owner-computes: CTA = tile I, thread (atom a = lane, group =

@@ -4,7 +4,11 @@
 // Moving atom a from x to x' changes only the N-1 pair terms that involve a:
 //   S'_k = S_k + f_sa(Q_k) sum_{j != a} f_sj(Q_k) [w(|x' - x_j|) - w(|x - x_j|)],
 //   w(r) = sin(Q_k r) / r,
-// so a proposal costs 2 (N-1) K sinusoid terms instead of N(N-1)/2 K.
+// so a proposal costs 2 (N-1) K sinusoid terms instead of N(N-1)/2 K.  (The
+// reference re-evaluates the whole configuration for every Monte Carlo
+// move: add_atom / del_atom in pyiid/sim/gcmc.py:13-114; its acceptance
+// rules are mh_accept, pyiid/sim/hmc.py:66-92, and the grand-canonical
+// rule of gcmc.py:13-114.)
 //
 // The potential needs G only through three scalars.  With G = T^T F (the
 // transform of the reference as a K x R matrix T), v = T gobs and the Gram

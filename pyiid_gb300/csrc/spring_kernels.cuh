@@ -1,4 +1,6 @@
-// spring_kernels.cuh -- spring potentials of pyiid/calc/spring_calc.py.
+// spring_kernels.cuh -- spring potentials of pyiid/calc/spring_calc.py:
+// spring_nrg / spring_force :99-144, voxel and atomwise energies :145-184,
+// the centre-of-mass spring :185-251 and the attractive spring :252-331.
 //
 // Pair springs (ordered pairs i != j, d_ij = q_j - q_i, r = |d_ij|, FP32 as
 // the reference's nxn kernels form them):

@@ -3,7 +3,9 @@
 // The reference's F -> G transform (zero pad, odd extension, inverse FFT,
 // linear interpolation onto the r grid) is a fixed linear map
 //   G(r_i) = sum_k F_k T[k][i]
-// (see the host builder of T for the derivation).  T is stored [n_bins][n_r]
+// (see the host builder of T for the derivation): get_pdf_at_qmin,
+// fft_fq_to_gr and fft_gr_to_fq of pyiid/experiments/elasticscatter/
+// kernels/master_kernel.py:39-203.  T is stored [n_bins][n_r]
 // in FP32, so G for a batch of configurations is a skinny GEMM streaming T
 // from HBM/L2 once per CTA column block.
 #pragma once
@@ -60,7 +62,8 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *scratch) {
   __syncthreads();
 }
 
-// Potential per configuration (one CTA each):
+// Potential per configuration (one CTA each), get_rw / get_chi_sq / get_scale
+// of kernels/master_kernel.py:206-266, 388-389:
 //   a = (gc.go)/(gc.gc); Rw: a <= 0 -> (1, 1), else sqrt(|go - a gc|^2/|go|^2)
 //   chi^2: s = a if a > 0 else 1, value = |go - s gc|^2
 // Optionally the adjoint vector c = d(value)/d(gcalc) exactly as the
@@ -212,7 +215,9 @@ __global__ void gradfq_coef_kernel(const double *__restrict__ na,
   }
 }
 
-// Compat G(r) gradient: out[row][i] = sum_{k >= kmin} A[row][k] T[k][i]
+// Compat G(r) gradient (grad_pdf, kernels/master_kernel.py:272-290: one
+// F -> G transform per row of the [N, 3, K] gradient):
+// out[row][i] = sum_{k >= kmin} A[row][k] T[k][i]
 // (FP32 products and sums, FP64 output).  Rows are the 3N rows of a
 // reference-convention grad_fq.  CTA tile 128 x 128 with K steps of 16;
 // thread (ty, tx) = (tid / 16, tid % 16) owns rows ty*8 .. ty*8+7 and
