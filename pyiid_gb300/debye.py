@@ -67,7 +67,12 @@ def _check_out(t, name, dtype):
 
 
 def fq(positions, species, scatter, qbin, k_begin=0, out=None):
-    """Reduced structure factor [K] (bins from Q = 0; bins < k_begin are 0)."""
+    """Reduced structure factor [K] (bins from Q = 0; bins < k_begin are 0).
+
+    The value of the reference processor callable ``self.fq`` before the
+    getter slices it (wrap_fq, pyiid/experiments/elasticscatter/
+    cpu_wrappers/flat_multi_cpu_wrap.py:22-60).
+    """
     import ctypes
     pos = as_positions(positions)
     n = pos.shape[0]
@@ -111,7 +116,11 @@ def batch_fq(positions, species, offsets, scatter, qbin, k_begin=0,
 
 def grad_fq(positions, species, scatter, qbin, k_begin=0, out=None):
     """Reference-convention gradient [N, 3, K] (= -1/2 dF/dx).  Every element
-    of ``out`` is written (bins < k_begin with 0)."""
+    of ``out`` is written (bins < k_begin with 0).
+
+    The value of ``self.grad`` (wrap_fq_grad, cpu_wrappers/
+    flat_multi_cpu_wrap.py:63-102 of pyiid/experiments/elasticscatter).
+    """
     import ctypes
     pos = as_positions(positions)
     n = pos.shape[0]
@@ -216,7 +225,11 @@ def fq_from_sums(species, scatter, k_begin, sums):
 
 
 def pdf(fq_t, qstep, rstep, rgrid, qmin):
-    """G(r) [B, R] (float64) for F(Q) rows [B, K] (or [K] -> [R])."""
+    """G(r) [B, R] (float64) for F(Q) rows [B, K] (or [K] -> [R]).
+
+    get_pdf_at_qmin (pyiid/experiments/elasticscatter/kernels/
+    master_kernel.py:39-105) as one linear map per grid.
+    """
     import ctypes
     squeeze = fq_t.dim() == 1
     f = fq_t.reshape(1, -1) if squeeze else fq_t
@@ -234,7 +247,8 @@ def pdf(fq_t, qstep, rstep, rgrid, qmin):
 
 
 def grad_pdf(grad_fq_t, qstep, rstep, rgrid, qmin):
-    """Transform of every row of a [N, 3, K] gradient -> [N, 3, R] float64."""
+    """Transform of every row of a [N, 3, K] gradient -> [N, 3, R] float64
+    (grad_pdf, kernels/master_kernel.py:272-290)."""
     import ctypes
     g = grad_fq_t.to(torch.float32).contiguous()
     n, _, k = g.shape
@@ -249,7 +263,8 @@ def grad_pdf(grad_fq_t, qstep, rstep, rgrid, qmin):
 
 
 def potential(gobs, gcalc, kind='rw'):
-    """(value, scale) rows [B, 2] for gcalc [B, R] (or [R] -> [2])."""
+    """(value, scale) rows [B, 2] for gcalc [B, R] (or [R] -> [2]): get_rw /
+    get_chi_sq with get_scale (kernels/master_kernel.py:206-266, 388-389)."""
     import ctypes
     squeeze = gcalc.dim() == 1
     gc = (gcalc.reshape(1, -1) if squeeze else gcalc).to(torch.float64)
@@ -264,7 +279,8 @@ def potential(gobs, gcalc, kind='rw'):
 
 
 def potential_grad(grad_pdf_t, gcalc, gobs, kind='rw'):
-    """sum_r c_r dG_r for each [a, c] row of grad_pdf [N, 3, R] -> [N, 3]."""
+    """sum_r c_r dG_r for each [a, c] row of grad_pdf [N, 3, R] -> [N, 3]:
+    get_grad_rw / get_grad_chi_sq (kernels/master_kernel.py:293-376)."""
     import ctypes
     gp = grad_pdf_t.to(torch.float64).contiguous()
     gc = gcalc.to(device=gp.device, dtype=torch.float64).contiguous()
@@ -283,7 +299,10 @@ def potential_grad(grad_pdf_t, gcalc, gobs, kind='rw'):
 def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
                          rgrid, qmin, gobs, kind='rw', want_grad=True,
                          out=None):
-    """Fused F -> G -> potential (+ adjoint gradient) for packed configs.
+    """Fused F -> G -> potential (+ adjoint gradient) for packed configs:
+    the energy and gradient chain of Calc1D (pyiid/calc/calc_1d.py:44-95,
+    wrap_rw / wrap_grad_rw in pyiid/calc/__init__.py:10-105) for many
+    configurations in one call.
 
     positions [sum N, 3] (CUDA), species [sum N] and offsets [B+1] (host).
     Returns dict(energy [B, 2] f64, grad [sum N, 3] f32 or None,
