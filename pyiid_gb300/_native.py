@@ -146,6 +146,9 @@ class Context:
             raise NativeError(f'pyiid_create failed ({rc}): {msg}')
         self.handle = h
         self.device = int(device)
+        # set_stream + call must not interleave between threads that share
+        # this context (each call runs on the stream its caller chose)
+        self._call_lock = threading.RLock()
 
     def close(self):
         if getattr(self, 'handle', None):
@@ -168,9 +171,10 @@ class Context:
         if stream is None:
             import torch
             stream = torch.cuda.current_stream(self.device).cuda_stream
-        self.check(self._lib.pyiid_set_stream(self.handle, _vp(stream)),
-                   'pyiid_set_stream')
-        self.check(getattr(self._lib, name)(self.handle, *args), name)
+        with self._call_lock:
+            self.check(self._lib.pyiid_set_stream(self.handle, _vp(stream)),
+                       'pyiid_set_stream')
+            self.check(getattr(self._lib, name)(self.handle, *args), name)
 
     def synchronize(self):
         self.check(self._lib.pyiid_synchronize(self.handle),

@@ -126,3 +126,46 @@ def test_binding_matches_every_prototype():
             ctype = re.sub(r'\b\w+$', '', c).strip() or c
             assert _kind_of_c(ctype) == _kind_of_ctypes(py), (name, i, c)
         assert _kind_of_c(ret) == _kind_of_ctypes(res), (name, ret)
+
+
+def test_context_call_keeps_stream_and_call_together():
+    """Threads sharing one context: every entry point runs on the stream its
+    own caller set (pyiid_set_stream and the call are not interleaved).
+    A fake library stands in for the device."""
+    import threading
+    import time
+    from pyiid_gb300 import _native
+
+    class FakeLib:
+        def __init__(self):
+            self.stream = None
+            self.mismatch = 0
+
+        def pyiid_set_stream(self, handle, stream):
+            self.stream = stream.value
+            return 0
+
+        def pyiid_fake(self, handle, want):
+            seen = self.stream
+            time.sleep(0)  # give the other thread a chance to interleave
+            if self.stream != want or seen != want:
+                self.mismatch += 1
+            return 0
+
+    ctx = _native.Context.__new__(_native.Context)
+    ctx._lib = FakeLib()
+    ctx.handle = ctypes.c_void_p(1)
+    ctx.device = 0
+    ctx._call_lock = threading.RLock()
+
+    def worker(s):
+        for _ in range(2000):
+            ctx.call('pyiid_fake', s, stream=s)
+
+    threads = [threading.Thread(target=worker, args=(s,)) for s in (11, 22, 33)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    ctx.handle = None  # nothing to destroy
+    assert ctx._lib.mismatch == 0
