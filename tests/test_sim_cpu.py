@@ -1,0 +1,129 @@
+"""The drop-in samplers (pyiid_gb300.sim) on the CPU with a plain-Python
+harmonic calculator: the reference's leapfrog checks
+(pyiid/tests/test_sim/test_leapfrog.py: no momentum, momentum,
+reversibility), dynamics lowering the energy both ways in time
+(test_sim/test_dynamics.py), energy conservation, and seeded
+reproducibility of HMC and NUTS
+(test_sim/test_nuts.py runs NUTS on the scattering calculator; that run is
+in tests/test_gpu_sampling.py)."""
+import numpy as np
+
+from pyiid_gb300.atoms import Atoms, Calculator
+from pyiid_gb300.sim import leapfrog
+from pyiid_gb300.sim.dynamics import classical_dynamics
+from pyiid_gb300.sim.hmc import run_hmc
+from pyiid_gb300.sim.nuts_hmc import NUTSCanonicalEnsemble
+
+
+class _Well(Calculator):
+    """E = k/2 sum |x - x0|^2, forces -k (x - x0)."""
+    implemented_properties = ['energy', 'forces']
+
+    def __init__(self, k=1.0, x0=None, **kw):
+        Calculator.__init__(self, **kw)
+        self.k = float(k)
+        self.x0 = None if x0 is None else np.array(x0, float)
+
+    def calculate(self, atoms=None, properties=['energy'],
+                  system_changes=()):
+        Calculator.calculate(self, atoms, properties, system_changes)
+        x = self.atoms.positions
+        d = x - (self.x0 if self.x0 is not None else 0.0)
+        self.results['energy'] = 0.5 * self.k * float((d * d).sum())
+        self.results['forces'] = -self.k * d
+
+
+def _square(k=1.0, x0=None):
+    a = Atoms('Au4', [[0, 0, 0], [3, 0, 0], [0, 3, 0], [3, 3, 0]])
+    a.set_calculator(_Well(k, x0))
+    return a
+
+
+def test_leapfrog_without_force_or_momentum_stays_put():
+    a = _square(k=0.0)
+    b = leapfrog(a, 1, False)
+    assert np.array_equal(a.positions, b.positions)
+
+
+def test_leapfrog_with_momentum_drifts_by_the_velocity():
+    a = _square(k=0.0)
+    a.set_momenta(np.ones((len(a), 3)))
+    b = leapfrog(a, 1, False)
+    assert np.allclose(b.positions - a.get_velocities(), a.positions,
+                       rtol=0, atol=1e-12)
+
+
+def test_leapfrog_is_reversible():
+    a = _square(k=0.7, x0=[[0.1, 0, 0], [3, 0.2, 0], [0, 3, 0.3], [3, 3, 0]])
+    a.set_momenta(np.ones((len(a), 3)))
+    b = leapfrog(a, 1, False)
+    c = leapfrog(b, -1, False)
+    assert np.allclose(c.positions, a.positions, rtol=0, atol=1e-10)
+    assert np.allclose(c.get_momenta(), a.get_momenta(), rtol=0, atol=1e-10)
+
+
+def test_dynamics_rolls_downhill_both_ways():
+    """test_sim/test_dynamics.py: from an expanded configuration at rest,
+    dynamics forward or backward in time lowers the potential energy."""
+    for step in (1.0, -1.0):
+        ideal = np.array([[-1.5, -1.5, 0], [1.5, -1.5, 0], [-1.5, 1.5, 0],
+                          [1.5, 1.5, 0]])
+        a = Atoms('Au4', ideal * 1.02)
+        a.set_calculator(_Well(k=2.0, x0=ideal))
+        a.set_velocities(np.zeros((4, 3)))
+        start = a.get_potential_energy()
+        traj = classical_dynamics(a, step, 5)
+        assert len(traj) == 6
+        assert min(t.get_potential_energy() for t in traj) < start
+
+
+def test_leapfrog_conserves_energy():
+    a = _square(k=1.0, x0=np.zeros((4, 3)))
+    a.set_momenta(np.full((len(a), 3), 5.0))
+    e0 = a.get_total_energy()
+    x = a
+    es = []
+    for _ in range(400):
+        x = leapfrog(x, 0.5, False)
+        es.append(x.get_total_energy())
+    # velocity Verlet on a harmonic well: bounded O((w h)^2) oscillation
+    assert np.max(np.abs(np.array(es) - e0)) <= 1e-3 * e0
+
+
+def test_hmc_is_reproducible_and_moves():
+    """The deprecated fixed-length HMC (unit-mass kicks, as the reference's
+    hmc.py): light atoms so that proposals are accepted."""
+    def run(seed):
+        a = Atoms('H4', [[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]])
+        a.set_calculator(_Well(k=0.2, x0=np.zeros((4, 3))))
+        rng = np.random.RandomState(seed)
+        traj, acc, acc_num = run_hmc(a, 30, 0.05, 5, 0.9, 0.0, 0.65, 1.02,
+                                     0.98, 0.001, 0.5, temp=1, rng=rng)
+        return traj, acc
+    t1, acc1 = run(3)
+    t2, acc2 = run(3)
+    assert len(t1) > 1 and any(acc1)
+    assert acc1 == acc2
+    assert np.array_equal(t1[-1].positions, t2[-1].positions)
+    assert not np.array_equal(t1[-1].positions, t1[0].positions)
+
+
+def test_nuts_is_reproducible_and_samples():
+    def run(seed):
+        a = _square(k=0.05, x0=np.zeros((4, 3)))
+        ens = NUTSCanonicalEnsemble(a, temperature=300, escape_level=6,
+                                    seed=seed)
+        traj, meta = ens.run(6)
+        return traj, meta, ens
+    t1, m1, e1 = run(11)
+    t2, m2, _ = run(11)
+    assert len(t1) >= 2 and m1['accepted_samples'] == len(t1) - 1
+    assert len(t1) == len(t2)
+    for x, y in zip(t1, t2):
+        assert np.array_equal(x.positions, y.positions)
+    assert np.all(np.isfinite(e1.pe)) and np.isfinite(e1.step_size)
+    assert e1.step_size > 0
+    # a different seed takes a different path
+    t3, _, _ = run(12)
+    assert not all(np.array_equal(x.positions, y.positions)
+                   for x, y in zip(t1[1:], t3[1:])) or len(t3) != len(t1)
