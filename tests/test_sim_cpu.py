@@ -127,3 +127,47 @@ def test_nuts_is_reproducible_and_samples():
     t3, _, _ = run(12)
     assert not all(np.array_equal(x.positions, y.positions)
                    for x, y in zip(t1[1:], t3[1:])) or len(t3) != len(t1)
+
+
+def _gcmc_run(mu, steps, seed, resolution=None):
+    from pyiid_gb300.sim.gcmc import GrandCanonicalEnsemble
+    np.random.seed(seed)  # the reference draws symbols and tests from it
+    a = Atoms('Au3', [[1, 1, 1], [2, 1, 1], [1, 2, 1]])
+    a.set_cell([6.0, 6.0, 6.0])
+    a.set_calculator(_Well(k=0.1))
+    ens = GrandCanonicalEnsemble(a, {'Au': mu}, temperature=1000, seed=seed,
+                                 resolution=resolution)
+    assert ens._engine is None  # a plain calculator: the reference path
+    ens.run(steps)
+    return ens
+
+
+def test_gcmc_reference_path_bookkeeping_and_reproducibility():
+    for resolution in (None, 0.5):
+        e1 = _gcmc_run(0.5, 60, 7, resolution)
+        e2 = _gcmc_run(0.5, 60, 7, resolution)
+        m = e1.metadata
+        assert sum(m[k] for k in ('accepted_additions', 'rejected_additions',
+                                  'accepted_removals',
+                                  'rejected_removals')) == 60
+        n_acc = m['accepted_additions'] + m['accepted_removals']
+        assert len(e1.traj) == 1 + n_acc
+        assert len(e1.traj[-1]) == 3 + m['accepted_additions'] - \
+            m['accepted_removals']
+        assert len(e1.traj) == len(e2.traj)
+        for x, y in zip(e1.traj, e2.traj):
+            assert np.array_equal(x.positions, y.positions)
+        # inserted atoms land inside the cell
+        assert np.all(e1.traj[-1].positions >= 0)
+        assert np.all(e1.traj[-1].positions <= 6.0 + 1e-12)
+
+
+def test_gcmc_chemical_potential_decides_the_extremes():
+    # mu >> any energy change: every insertion accepted; mu << : every
+    # removal accepted while more than one atom is left
+    e = _gcmc_run(1e6, 40, 3)
+    assert e.metadata['rejected_additions'] == 0
+    assert e.metadata['accepted_additions'] > 0
+    e = _gcmc_run(-1e6, 40, 3)
+    assert e.metadata['accepted_additions'] == 0
+    assert len(e.traj[-1]) == 1
