@@ -1,0 +1,135 @@
+"""The drop-in ElasticScatter's host logic on the CPU.
+
+The processor plug-in contract (pyiid/experiments/elasticscatter/
+__init__.py:206-292) is three callables; here they are test doubles backed
+by the FP64 oracle, and the F -> G transform is the oracle's FFT form.  What
+runs for real is the layer a pyIID user calls: the experiment grids, the
+per-atom scatter tables cached on the Atoms object (with the reference's
+quirks), the cache invalidation, the qmin slicing and zeroing of the
+getters, and the S(Q) / I(Q) post-processing.  Everything is compared with
+the reference's own recorded outputs at the reference tests' tolerances
+(pyiid/tests/test_scatter.py:9-10).  tests/test_gpu_compat.py runs the same
+getters on the GB300 processor.
+"""
+import numpy as np
+import pytest
+
+from oracle import debye_np as O
+from pyiid_gb300.atoms import Atom, Atoms
+
+RTOL, ATOL = 5e-4, 5e-5
+EXPS = {
+    'default': None,
+    'short': {'qmin': 0.6, 'qmax': 22.0, 'qbin': 0.13, 'rmin': 0.5,
+              'rmax': 12.0, 'rstep': 0.05, 'sampling': 'full'},
+    'ns': {'qmin': 1.1, 'qmax': 20.0, 'qbin': 0.1, 'rmin': 1.0,
+           'rmax': 15.0, 'rstep': 0.02, 'sampling': 'ns'},
+}
+
+
+@pytest.fixture
+def ES(monkeypatch):
+    """ElasticScatter with oracle-backed processor callables."""
+    from pyiid_gb300.experiments import elasticscatter as es_mod
+
+    def table(atoms, sum_type):
+        return atoms.get_array('F(Q) scatter' if sum_type == 'fq'
+                               else 'PDF scatter')
+
+    def fq(atoms, qbin, sum_type='fq'):
+        return O.fq(atoms.get_positions(), table(atoms, sum_type),
+                    qbin).astype(np.float32)
+
+    def grad(atoms, qbin, sum_type='fq'):
+        return O.grad_fq(atoms.get_positions(), table(atoms, sum_type),
+                         qbin).astype(np.float32)
+
+    def set_processor(self, processor=None, kernel_type='flat'):
+        self.fq, self.grad, self.grad_pdf = fq, grad, O.grad_pdf
+        self.processor, self.alg = 'oracle stand-in', kernel_type
+        return True
+
+    monkeypatch.setattr(es_mod.ElasticScatter, 'set_processor', set_processor)
+    monkeypatch.setattr(es_mod, 'get_pdf_at_qmin', O.pdf_fft)
+
+    def make(exp_name):
+        e = EXPS[exp_name]
+        return es_mod.ElasticScatter(exp_dict=None if e is None else dict(e))
+    return make
+
+
+def close(a, b, rtol=RTOL, atol=ATOL):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    assert a.shape == b.shape
+    np.testing.assert_allclose(np.nan_to_num(a), np.nan_to_num(b), rtol=rtol,
+                               atol=atol)
+
+
+@pytest.mark.parametrize('exp_name', ['default', 'short', 'ns'])
+@pytest.mark.parametrize('tag', ['au2', 'square', 'rand20', 'alloy16'])
+def test_getters_match_reference_outputs(golden, ES, tag, exp_name):
+    key = f'{tag}__{exp_name}'
+    s = ES(exp_name)
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    fq = s.get_fq(atoms)
+    close(fq, golden[key + '__fq'])
+    # the per-atom tables are built once and cached on the Atoms object
+    close(atoms.get_array('F(Q) scatter'), golden[key + '__fq_table'],
+          rtol=1e-6, atol=0)
+    close(atoms.get_array('PDF scatter'), golden[key + '__pdf_table'],
+          rtol=1e-6, atol=0)
+    fq2 = s.get_fq(atoms)
+    assert fq is not fq2 and np.array_equal(fq, fq2)
+    close(s.get_sq(atoms), golden[key + '__sq'])
+    close(s.get_iq(atoms), golden[key + '__iq'], atol=5e-3)
+    close(s.get_pdf(atoms), golden[key + '__pdf'])
+    g = s.get_grad_fq(atoms)
+    assert g.dtype == np.float32
+    close(g, golden[key + '__grad_fq'])
+    if key + '__grad_pdf' in golden.files:
+        close(s.get_grad_pdf(atoms), golden[key + '__grad_pdf'])
+    assert np.array_equal(s.get_r(), golden[key + '__r'])
+    assert np.allclose(s.get_scatter_vector(), golden[key + '__q'])
+    assert np.allclose(s.get_scatter_vector(pdf=True),
+                       golden[key + '__q_pdf'])
+
+
+def test_scatter_tables_are_rebuilt_when_the_atoms_change(golden, ES):
+    """test_scatter_state.py: adding or deleting an atom, or changing the
+    experiment, invalidates the cached tables."""
+    key = 'rand20__default'
+    s = ES('default')
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    s.get_fq(atoms)
+    assert atoms.get_array('F(Q) scatter').shape[0] == len(atoms)
+    atoms.append(Atom('Au', [0.5, 0.5, 0.5]))
+    fq = s.get_fq(atoms)
+    assert atoms.get_array('F(Q) scatter').shape[0] == len(atoms)
+    assert atoms.info['scatter_atoms'] == len(atoms)
+    del atoms[0]
+    fq2 = s.get_fq(atoms)
+    assert atoms.get_array('F(Q) scatter').shape[0] == len(atoms)
+    assert not np.array_equal(fq, fq2)
+    s.update_experiment({'qmax': 20.0})
+    s.get_fq(atoms)
+    assert atoms.info['exp'] == s.exp
+    assert atoms.get_array('F(Q) scatter').shape[1] == int(20.0 / 0.1)
+
+
+def test_experiment_grids():
+    """update_experiment (__init__.py:180-204): defaults, the 'ns' r step
+    pi / qmax and the PDF Q step pi / (rmax + 12 pi / qmax)."""
+    from pyiid_gb300.experiments.elasticscatter import ElasticScatter
+    s = ElasticScatter.__new__(ElasticScatter)
+    s.exp_dict_keys = ['qmin', 'qmax', 'qbin', 'rmin', 'rmax', 'rstep',
+                       'sampling']
+    s.default_values = [0.0, 25, .1, 0.0, 40.0, .01, 'full']
+    s.update_experiment(None)
+    assert s.exp == dict(zip(s.exp_dict_keys, s.default_values))
+    assert abs(s.pdf_qbin - 0.0756865) < 1e-7
+    s.update_experiment({'qmax': 20.0, 'sampling': 'ns'})
+    assert abs(s.exp['rstep'] - np.pi / 20.0) < 1e-15
+    assert abs(s.pdf_qbin - np.pi / (40.0 + 12 * np.pi / 20.0)) < 1e-15
+    assert len(s.get_r()) == len(np.arange(0.0, 40.0, np.pi / 20.0))
