@@ -118,17 +118,14 @@ def test_scatter_tables_are_rebuilt_when_the_atoms_change(golden, ES):
     assert atoms.get_array('F(Q) scatter').shape[1] == int(20.0 / 0.1)
 
 
-def test_experiment_grids():
-    """update_experiment (__init__.py:180-204): defaults, the 'ns' r step
-    pi / qmax and the PDF Q step pi / (rmax + 12 pi / qmax)."""
-    from pyiid_gb300.experiments.elasticscatter import ElasticScatter
-    s = ElasticScatter.__new__(ElasticScatter)
-    s.exp_dict_keys = ['qmin', 'qmax', 'qbin', 'rmin', 'rmax', 'rstep',
-                       'sampling']
-    s.default_values = [0.0, 25, .1, 0.0, 40.0, .01, 'full']
-    s.update_experiment(None)
-    assert s.exp == dict(zip(s.exp_dict_keys, s.default_values))
+def test_experiment_grids(ES):
+    """update_experiment (__init__.py:180-204): the reference's defaults, the
+    'ns' r step pi / qmax and the PDF Q step pi / (rmax + 12 pi / qmax)."""
+    s = ES('default')
+    assert s.exp == {'qmin': 0.0, 'qmax': 25, 'qbin': .1, 'rmin': 0.0,
+                     'rmax': 40.0, 'rstep': .01, 'sampling': 'full'}
     assert abs(s.pdf_qbin - 0.0756865) < 1e-7
+    assert len(s.get_r()) == 4000 and len(s.get_scatter_vector()) == 250
     s.update_experiment({'qmax': 20.0, 'sampling': 'ns'})
     assert abs(s.exp['rstep'] - np.pi / 20.0) < 1e-15
     assert abs(s.pdf_qbin - np.pi / (40.0 + 12 * np.pi / 20.0)) < 1e-15
