@@ -130,3 +130,61 @@ def test_experiment_grids(ES):
     assert abs(s.exp['rstep'] - np.pi / 20.0) < 1e-15
     assert abs(s.pdf_qbin - np.pi / (40.0 + 12 * np.pi / 20.0)) < 1e-15
     assert len(s.get_r()) == len(np.arange(0.0, 40.0, np.pi / 20.0))
+
+
+@pytest.fixture
+def oracle_potentials(monkeypatch):
+    """The potential functions behind wrap_rw / wrap_grad_rw (and chi^2) as
+    oracle doubles with the reference's signatures (master_kernel.py)."""
+    import pyiid_gb300.calc as calc_mod
+
+    def grad_rw(out, gpdf, gcalc, gobs, rw, scale):
+        out[:] = O.get_grad_rw(gpdf, gcalc, gobs, rw, scale)
+
+    def grad_chi(out, gpdf, gcalc, gobs, scale):
+        out[:] = O.get_grad_chi_sq(gpdf, gcalc, gobs, scale)
+
+    monkeypatch.setattr(calc_mod, 'get_rw',
+                        lambda gobs, gcalc, weight=None: O.get_rw(gobs, gcalc))
+    monkeypatch.setattr(calc_mod, 'get_chi_sq', O.get_chi_sq)
+    monkeypatch.setattr(calc_mod, 'get_grad_rw', grad_rw)
+    monkeypatch.setattr(calc_mod, 'get_grad_chi_sq', grad_chi)
+
+
+def _pot_keys(g):
+    return sorted({k.rsplit('__', 1)[0] for k in g.files
+                   if k.startswith('pot')})
+
+
+@pytest.mark.parametrize('idx', range(6))
+def test_calc1d_energy_and_forces_follow_the_reference(golden, ES,
+                                                       oracle_potentials,
+                                                       idx):
+    """Calc1D (pyiid/calc/calc_1d.py:9-95) on functions that are not the
+    GB300 getters takes the reference's path: energy = conv * Rw (or chi^2)
+    and forces = conv * the reference's gradient contraction (-1/2 of the
+    true -dE/dx; twice that with true_forces)."""
+    from pyiid_gb300.calc.calc_1d import Calc1D
+    key = _pot_keys(golden)[idx]
+    s = ES(key.split('__')[-1])
+    target = golden[key + '__target']
+    conv = 30.0
+    for pot in ('rw', 'chi_sq'):
+        for true_forces in (False, True):
+            atoms = Atoms(numbers=golden[key + '__numbers'],
+                          positions=golden[key + '__positions'])
+            calc = Calc1D(target_data=target,
+                          exp_function=lambda a: s.get_pdf(a),
+                          exp_grad_function=lambda a: s.get_grad_pdf(a),
+                          conv=conv, potential=pot, true_forces=true_forces)
+            assert calc._fused is None
+            atoms.set_calculator(calc)
+            want_e = conv * float(golden[key + '__' + pot][0])
+            e = atoms.get_potential_energy()
+            assert abs(e - want_e) <= 1e-5 * max(1.0, abs(want_e)), (pot, e)
+            want_f = conv * golden[key + '__grad_' + pot] * (
+                2.0 if true_forces else 1.0)
+            f = atoms.get_forces()
+            err = np.linalg.norm(f - want_f) / max(np.linalg.norm(want_f),
+                                                   1e-300)
+            assert err <= 1e-4, (pot, true_forces, err)
