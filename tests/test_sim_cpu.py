@@ -171,3 +171,91 @@ def test_gcmc_chemical_potential_decides_the_extremes():
     e = _gcmc_run(-1e6, 40, 3)
     assert e.metadata['accepted_additions'] == 0
     assert len(e.traj[-1]) == 1
+
+
+def _springs(x, k=0.3, r0=2.8):
+    """E = k/2 sum_{i<j} (r_ij - r0)^2 and its forces (translation
+    invariant, so the samplers' centring does not change it)."""
+    d = x[:, None, :] - x[None, :, :]
+    r = np.sqrt((d * d).sum(-1))
+    np.fill_diagonal(r, 1.0)
+    dr = r - r0
+    np.fill_diagonal(dr, 0.0)
+    e = 0.25 * k * float((dr * dr).sum())
+    f = -k * ((dr / r)[:, :, None] * d).sum(1)
+    return e, f
+
+
+class _Springs(Calculator):
+    implemented_properties = ['energy', 'forces']
+
+    def calculate(self, atoms=None, properties=['energy'],
+                  system_changes=()):
+        Calculator.calculate(self, atoms, properties, system_changes)
+        e, f = _springs(self.atoms.positions)
+        self.results['energy'] = e
+        self.results['forces'] = f
+
+
+def test_spring_forces_are_minus_the_gradient():
+    x = np.random.default_rng(0).normal(size=(5, 3)) * 2
+    e, f = _springs(x)
+    h = 1e-6
+    for i, c in ((0, 0), (3, 2), (4, 1)):
+        xp, xm = x.copy(), x.copy()
+        xp[i, c] += h
+        xm[i, c] -= h
+        assert abs((_springs(xp)[0] - _springs(xm)[0]) / (2 * h)
+                   + f[i, c]) < 1e-6
+
+
+def test_batched_nuts_scheduler_reproduces_sequential_chains():
+    """pyiid_gb300.nuts_batched drives every chain's reference NUTS as a
+    generator and evaluates the pending leapfrog end points of all chains
+    together; with the device evaluation replaced by the same Python
+    potential, chain c equals a sequential NUTSCanonicalEnsemble run with
+    seed c sample for sample."""
+    from pyiid_gb300.nuts_batched import BatchedNUTS
+
+    base = np.array([[0, 0, 0], [2.8, 0, 0], [0, 2.8, 0], [0, 0, 2.8],
+                     [2.0, 2.0, 2.0]], float)
+    rng = np.random.default_rng(4)
+    starts = [base + rng.normal(scale=0.1, size=base.shape) for _ in range(3)]
+    seeds = [5, 6, 7]
+    n_steps = 6  # the first iterations adapt the step size; later ones accept
+
+    seq = []
+    for x0, seed in zip(starts, seeds):
+        a = Atoms('Au5', x0)
+        a.set_calculator(_Springs())
+        ens = NUTSCanonicalEnsemble(a, temperature=300, escape_level=5,
+                                    seed=seed)
+        traj, meta = ens.run(n_steps)
+        seq.append((traj, meta, ens.step_size))
+
+    class _Pot:
+        n_configs = 3
+        offsets = np.array([0, 5, 10, 15])
+        masses = Atoms('Au5').get_masses()
+
+    class _CpuNUTS(BatchedNUTS):
+        def _evaluate(self, xs):
+            self.evaluations += 1
+            out = [_springs(np.asarray(x, float)) for x in xs]
+            return (np.array([e for e, _ in out]),
+                    np.stack([f for _, f in out]))
+
+    b = _CpuNUTS(_Pot(), np.stack(starts), temperature=300, seeds=seeds,
+                 escape_level=5)
+    b.step(n_steps)
+    for c, (traj, meta, step) in enumerate(seq):
+        ch = b.chains[c]
+        assert meta['accepted_samples'] > 0
+        assert ch.metadata['accepted_samples'] == meta['accepted_samples']
+        assert len(ch.samples) == len(traj) - 1
+        for x, t in zip(ch.samples, traj[1:]):
+            assert np.allclose(x, t.positions, rtol=0, atol=1e-9)
+        assert abs(ch.step_size - step) <= 1e-12 * step
+    # one batched evaluation per tree leaf of the deepest chain (twice with
+    # the centred re-evaluation), not one per leaf per chain
+    assert b.evaluations < sum(m['samples_total'] for _, m, _ in seq)
