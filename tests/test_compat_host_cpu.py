@@ -188,3 +188,30 @@ def test_calc1d_energy_and_forces_follow_the_reference(golden, ES,
             err = np.linalg.norm(f - want_f) / max(np.linalg.norm(want_f),
                                                    1e-300)
             assert err <= 1e-4, (pot, true_forces, err)
+
+
+@pytest.mark.parametrize('tag', ['au2', 'alloy16', 'rand20'])
+def test_species_tables_reproduce_the_per_atom_arrays(golden, ES, tag):
+    """The processor passes the kernels (species id per atom, one table row
+    per species) instead of the reference's [N, K] per-atom arrays; the two
+    must describe the same rows exactly, from the cached species column and
+    from the fallback that derives it from the distinct rows."""
+    from pyiid_gb300.experiments.elasticscatter.gb300_wrap import species_of
+    key = f'{tag}__short'
+    s = ES('short')
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    s.get_fq(atoms)
+    for sum_type, name in (('fq', 'F(Q) scatter'), ('PDF', 'PDF scatter')):
+        per_atom = atoms.get_array(name).astype(np.float32)
+        sp, tab = species_of(atoms, sum_type)
+        assert sp.dtype == np.int32 and tab.dtype == np.float32
+        assert np.array_equal(tab[sp], per_atom)
+        saved = atoms.arrays.pop('GB300 species', None)
+        try:
+            sp2, tab2 = species_of(atoms, sum_type)
+        finally:
+            if saved is not None:
+                atoms.arrays['GB300 species'] = saved
+        assert np.array_equal(tab2[sp2], per_atom)
+        assert len(tab2) == len(np.unique(per_atom, axis=0))
