@@ -35,9 +35,12 @@ def species_of(atoms, sum_type='fq'):
     tabs = atoms.info.get('GB300 tables')
     if sp is not None and tabs is not None and name in tabs and len(sp) == n:
         tab = tabs[name]
-        if tab.shape[1] == k and (n == 0 or (
-                np.array_equal(per_atom[0], tab[sp[0]]) and
-                np.array_equal(per_atom[-1], tab[sp[-1]]))):
+        # the cached column must still describe the per-atom array: compare
+        # up to 64 evenly spaced rows (the caller may have edited the array)
+        rows = np.unique(np.linspace(0, max(n - 1, 0), min(n, 64)).astype(int))
+        if tab.shape[1] == k and (n == 0 or np.array_equal(
+                np.asarray(per_atom[rows], np.float32),
+                np.asarray(tab, np.float32)[np.asarray(sp)[rows]])):
             return np.asarray(sp, np.int32), np.asarray(tab, np.float32)
     if n == 0:
         return np.zeros(0, np.int32), np.zeros((1, k), np.float32)

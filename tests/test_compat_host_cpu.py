@@ -215,3 +215,19 @@ def test_species_tables_reproduce_the_per_atom_arrays(golden, ES, tag):
                 atoms.arrays['GB300 species'] = saved
         assert np.array_equal(tab2[sp2], per_atom)
         assert len(tab2) == len(np.unique(per_atom, axis=0))
+
+
+def test_species_column_is_not_trusted_after_an_edit(golden, ES):
+    """An edited per-atom row (not the first or the last) makes the processor
+    derive the species from the array itself instead of the cached column."""
+    from pyiid_gb300.experiments.elasticscatter.gb300_wrap import species_of
+    key = 'alloy16__short'
+    s = ES('short')
+    atoms = Atoms(numbers=golden[key + '__numbers'],
+                  positions=golden[key + '__positions'])
+    s.get_fq(atoms)
+    arr = atoms.get_array('F(Q) scatter')    # a copy, as ASE returns
+    arr[len(atoms) // 2] *= 1.5
+    atoms.set_array('F(Q) scatter', arr)
+    sp, tab = species_of(atoms, 'fq')
+    assert np.array_equal(tab[sp], arr.astype(np.float32))
