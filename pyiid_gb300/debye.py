@@ -33,8 +33,40 @@ def _ptr(a, ctype):
 _cuda_seen = False
 
 
+def _positions_shape(x):
+    """Shape of positions given as a tensor, an array or nested lists; the
+    last axis must hold x, y, z (the kernels read 3 floats per atom)."""
+    shape = tuple(x.shape) if hasattr(x, 'shape') else np.shape(x)
+    if len(shape) == 0 or shape[-1] != 3:
+        raise NativeError(f'positions must be [N, 3] (got {list(shape)})')
+    return shape
+
+
+def _check_system(n, sp, tab):
+    """One configuration: species ids [n] and a form-factor table [S, K]
+    (the library reads n ids and S x K floats from these host arrays)."""
+    if tab.ndim != 2 or sp.ndim != 1 or sp.shape[0] != n:
+        raise NativeError(f'species must be [{n}] and scatter [S, K] (got '
+                          f'{list(sp.shape)} and {list(tab.shape)})')
+
+
+def _check_packed(n_rows, sp, off, tab):
+    """Packed configurations: offsets [B+1] and at least offsets' atoms of
+    positions (n_rows) and species ids (the library reads that many)."""
+    if off.ndim != 1 or off.shape[0] < 2:
+        raise NativeError('offsets must be [B + 1] with B >= 1')
+    total = int(off.max())
+    if tab.ndim != 2 or sp.ndim != 1 or sp.shape[0] < total or \
+            n_rows < total:
+        raise NativeError(f'offsets cover {total} atoms: positions has '
+                          f'{n_rows} rows, species {list(sp.shape)}, '
+                          f'scatter must be [S, K] (got {list(tab.shape)})')
+
+
 def as_positions(x, device=None):
-    """float32 contiguous CUDA tensor [N, 3] from an array or tensor."""
+    """float32 contiguous CUDA tensor [N, 3] from an array or tensor (any
+    leading shape with x, y, z last, e.g. [B, N, 3], is flattened)."""
+    _positions_shape(x)
     global _cuda_seen
     if not _cuda_seen:  # a device, once seen, stays (the check costs µs)
         if not torch.cuda.is_available():
@@ -45,8 +77,9 @@ def as_positions(x, device=None):
         t = x.detach()
         if not t.is_cuda:
             t = t.to('cuda' if device is None else device)
-        return t.to(torch.float32).contiguous()
-    return torch.as_tensor(_np(x, np.float32), device=device or 'cuda')
+        return t.to(torch.float32).contiguous().reshape(-1, 3)
+    return torch.as_tensor(_np(x, np.float32),
+                           device=device or 'cuda').reshape(-1, 3)
 
 
 def _check_dev(t, name, dtype):
@@ -78,8 +111,7 @@ def fq(positions, species, scatter, qbin, k_begin=0, out=None):
     n = pos.shape[0]
     sp = _np(species, np.int32)
     tab = _np(scatter, np.float32)
-    if tab.ndim != 2 or sp.shape != (n,):
-        raise NativeError('species must be [N] and scatter [S, K]')
+    _check_system(n, sp, tab)
     if out is None:
         out = torch.empty(tab.shape[1], dtype=torch.float32, device=pos.device)
     else:
@@ -100,6 +132,7 @@ def batch_fq(positions, species, offsets, scatter, qbin, k_begin=0,
     sp = _np(species, np.int32)
     off = _np(offsets, np.int32)
     tab = _np(scatter, np.float32)
+    _check_packed(pos.numel() // 3, sp, off, tab)
     b = len(off) - 1
     if out is None:
         out = torch.empty((b, tab.shape[1]), dtype=torch.float32,
@@ -126,6 +159,7 @@ def grad_fq(positions, species, scatter, qbin, k_begin=0, out=None):
     n = pos.shape[0]
     sp = _np(species, np.int32)
     tab = _np(scatter, np.float32)
+    _check_system(n, sp, tab)
     if out is None:
         out = torch.empty((n, 3, tab.shape[1]), dtype=torch.float32,
                           device=pos.device)
@@ -154,6 +188,7 @@ def fq_grad(positions, species, scatter, qbin, k_begin=0, out_fq=None,
     n = pos.shape[0]
     sp = _np(species, np.int32)
     tab = _np(scatter, np.float32)
+    _check_system(n, sp, tab)
     k = tab.shape[1]
     if out_fq is None:
         out_fq = torch.empty(k, dtype=torch.float32, device=pos.device)
@@ -188,6 +223,7 @@ def fq_grad_part(positions, species, scatter, qbin, k_begin, part, n_parts,
     n = pos.shape[0]
     sp = _np(species, np.int32)
     tab = _np(scatter, np.float32)
+    _check_system(n, sp, tab)
     k = tab.shape[1]
     if out_grad is None:
         out_grad = torch.zeros((n, 3, k), dtype=torch.float32,
@@ -314,6 +350,7 @@ def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
     sp = _np(species, np.int32)
     off = _np(offsets, np.int32)
     tab = _np(scatter, np.float32)
+    _check_packed(pos.numel() // 3, sp, off, tab)
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
     dev = pos.device
@@ -378,6 +415,7 @@ def mh_init(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
     sp = _np(species, np.int32)
     off = _np(offsets, np.int32)
     tab = _np(scatter, np.float32)
+    _check_packed(pos.numel() // 3, sp, off, tab)
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
     k = tab.shape[1]
@@ -418,9 +456,11 @@ def mh_steps(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
             pos.dtype == torch.float32 and pos.is_contiguous()):
         raise NativeError('positions must be a contiguous float32 CUDA tensor '
                           '(updated in place)')
+    _positions_shape(pos)
     sp = _np(species, np.int32)
     off = _np(offsets, np.int32)
     tab = _np(scatter, np.float32)
+    _check_packed(pos.numel() // 3, sp, off, tab)
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
     dev = pos.device
@@ -462,6 +502,7 @@ def mc_propose(positions, species, offsets, scatter, qstep, rstep, rgrid,
     sp = _np(species, np.int32)
     off = _np(offsets, np.int32)
     tab = _np(scatter, np.float32)
+    _check_packed(pos.numel() // 3, sp, off, tab)
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
     md = _np(mode, np.int32).reshape(b)

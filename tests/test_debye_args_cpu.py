@@ -1,0 +1,68 @@
+"""Argument checks of the device API that run before any library call.
+
+The C ABI receives bare pointers, so the Python layer checks what the
+library will read: 3 floats per atom, one species id per atom, a 2-D
+form-factor table, and for packed configurations at least as many position
+rows and species ids as the offsets cover.  A violation raises NativeError
+before any device work (here on the CPU, where no device exists)."""
+import numpy as np
+import pytest
+import torch
+
+from pyiid_gb300 import debye
+from pyiid_gb300._native import NativeError
+
+
+@pytest.mark.parametrize('shape', [(5, 3), (2, 4, 3), (3,), (0, 3)])
+def test_positions_with_xyz_last_are_accepted(shape):
+    assert debye._positions_shape(np.zeros(shape)) == shape
+    assert debye._positions_shape(torch.zeros(shape)) == shape
+
+
+@pytest.mark.parametrize('shape', [(5, 2), (15,), (3, 4), (), (0,)])
+def test_positions_without_xyz_last_are_refused(shape):
+    with pytest.raises(NativeError, match='positions must be'):
+        debye._positions_shape(np.zeros(shape))
+
+
+def test_shape_is_checked_before_the_device():
+    # on a machine without a device the shape error still comes first
+    with pytest.raises(NativeError, match='positions must be'):
+        debye.fq(np.zeros((4, 2), np.float32), np.zeros(4, np.int32),
+                 np.ones((1, 10), np.float32), 0.1)
+    with pytest.raises(NativeError, match='positions must be'):
+        debye.batch_fq(np.zeros(12, np.float32), np.zeros(4, np.int32),
+                       [0, 4], np.ones((1, 10), np.float32), 0.1)
+
+
+def test_single_configuration_species_and_table():
+    tab = np.ones((2, 10), np.float32)
+    debye._check_system(4, np.zeros(4, np.int32), tab)
+    debye._check_system(0, np.zeros(0, np.int32), tab)
+    for sp, t in ((np.zeros(3, np.int32), tab),      # too few ids
+                  (np.zeros(5, np.int32), tab),      # too many ids
+                  (np.zeros((4, 1), np.int32), tab),  # not 1-D
+                  (np.zeros(4, np.int32), np.ones(10, np.float32))):
+        with pytest.raises(NativeError, match='species must be'):
+            debye._check_system(4, sp, t)
+
+
+def test_packed_configurations_cover_their_buffers():
+    tab = np.ones((1, 10), np.float32)
+    off = np.array([0, 3, 3, 7], np.int32)
+    debye._check_packed(7, np.zeros(7, np.int32), off, tab)
+    # more rows than the offsets cover (capacity buffers) are fine
+    debye._check_packed(9, np.zeros(9, np.int32), off, tab)
+    with pytest.raises(NativeError, match='offsets cover 7 atoms'):
+        debye._check_packed(6, np.zeros(7, np.int32), off, tab)
+    with pytest.raises(NativeError, match='offsets cover 7 atoms'):
+        debye._check_packed(7, np.zeros(6, np.int32), off, tab)
+    with pytest.raises(NativeError, match='offsets cover'):
+        debye._check_packed(7, np.zeros(7, np.int32), off, tab[0])
+    # a decreasing last offset cannot hide a larger one
+    with pytest.raises(NativeError, match='offsets cover 9 atoms'):
+        debye._check_packed(7, np.zeros(7, np.int32),
+                            np.array([0, 9, 5], np.int32), tab)
+    with pytest.raises(NativeError, match='offsets must be'):
+        debye._check_packed(7, np.zeros(7, np.int32),
+                            np.array([0], np.int32), tab)
