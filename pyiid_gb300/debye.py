@@ -63,16 +63,38 @@ def _check_packed(n_rows, sp, off, tab):
                           f'scatter must be [S, K] (got {list(tab.shape)})')
 
 
-def as_positions(x, device=None):
-    """float32 contiguous CUDA tensor [N, 3] from an array or tensor (any
-    leading shape with x, y, z last, e.g. [B, N, 3], is flattened)."""
-    _positions_shape(x)
+def _require_cuda():
     global _cuda_seen
     if not _cuda_seen:  # a device, once seen, stays (the check costs µs)
         if not torch.cuda.is_available():
             raise NativeError('no CUDA device is visible; pyiid_gb300 runs '
                               'only on a GB300 (sm_103a) GPU')
         _cuda_seen = True
+
+
+def _dev_tensor(t, dtype, device=None):
+    """Contiguous CUDA tensor of ``dtype`` from a tensor or an array.  Host
+    data is copied to the device: the library dereferences device
+    pointers only."""
+    _require_cuda()
+    if not isinstance(t, torch.Tensor):
+        t = torch.as_tensor(np.asarray(t))
+    t = t.detach()
+    if device is None:
+        device = t.device if t.is_cuda else torch.device('cuda')
+    return t.to(device=device, dtype=dtype).contiguous()
+
+
+def _check_len(t, n, name):
+    if t.numel() != n:
+        raise NativeError(f'{name} has {t.numel()} values, expected {n}')
+
+
+def as_positions(x, device=None):
+    """float32 contiguous CUDA tensor [N, 3] from an array or tensor (any
+    leading shape with x, y, z last, e.g. [B, N, 3], is flattened)."""
+    _positions_shape(x)
+    _require_cuda()
     if isinstance(x, torch.Tensor):
         t = x.detach()
         if not t.is_cuda:
@@ -116,6 +138,7 @@ def fq(positions, species, scatter, qbin, k_begin=0, out=None):
         out = torch.empty(tab.shape[1], dtype=torch.float32, device=pos.device)
     else:
         _check_dev(out, 'out', torch.float32)
+        _check_len(out, tab.shape[1], 'out')
     ctx = context(pos.device.index)
     ctx.call('pyiid_fq', ctypes.c_void_p(pos.data_ptr()),
              _ptr(sp, ctypes.c_int32), n, _ptr(tab, ctypes.c_float),
@@ -139,6 +162,7 @@ def batch_fq(positions, species, offsets, scatter, qbin, k_begin=0,
                           device=pos.device)
     else:
         _check_dev(out, 'out', torch.float32)
+        _check_len(out, b * tab.shape[1], 'out')
     ctx = context(pos.device.index)
     ctx.call('pyiid_batch_fq', ctypes.c_void_p(pos.data_ptr()),
              _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
@@ -165,6 +189,7 @@ def grad_fq(positions, species, scatter, qbin, k_begin=0, out=None):
                           device=pos.device)
     else:
         _check_dev(out, 'out', torch.float32)
+        _check_len(out, n * 3 * tab.shape[1], 'out')
     if n == 0:
         return out
     ctx = context(pos.device.index)
@@ -267,9 +292,11 @@ def pdf(fq_t, qstep, rstep, rgrid, qmin):
     master_kernel.py:39-105) as one linear map per grid.
     """
     import ctypes
-    squeeze = fq_t.dim() == 1
-    f = fq_t.reshape(1, -1) if squeeze else fq_t
-    f = f.to(torch.float32).contiguous()
+    f = _dev_tensor(fq_t, torch.float32)
+    squeeze = f.dim() == 1
+    f = f.reshape(1, -1) if squeeze else f
+    if f.dim() != 2:
+        raise NativeError(f'F(Q) must be [B, K] or [K] (got {list(f.shape)})')
     rg = _np(rgrid, np.float64)
     out = torch.empty((f.shape[0], len(rg)), dtype=torch.float64,
                       device=f.device)
@@ -286,7 +313,10 @@ def grad_pdf(grad_fq_t, qstep, rstep, rgrid, qmin):
     """Transform of every row of a [N, 3, K] gradient -> [N, 3, R] float64
     (grad_pdf, kernels/master_kernel.py:272-290)."""
     import ctypes
-    g = grad_fq_t.to(torch.float32).contiguous()
+    g = _dev_tensor(grad_fq_t, torch.float32)
+    if g.dim() != 3 or g.shape[1] != 3:
+        raise NativeError(f'the gradient must be [N, 3, K] (got '
+                          f'{list(g.shape)})')
     n, _, k = g.shape
     rg = _np(rgrid, np.float64)
     out = torch.zeros((n, 3, len(rg)), dtype=torch.float64, device=g.device)
@@ -302,10 +332,14 @@ def potential(gobs, gcalc, kind='rw'):
     """(value, scale) rows [B, 2] for gcalc [B, R] (or [R] -> [2]): get_rw /
     get_chi_sq with get_scale (kernels/master_kernel.py:206-266, 388-389)."""
     import ctypes
-    squeeze = gcalc.dim() == 1
-    gc = (gcalc.reshape(1, -1) if squeeze else gcalc).to(torch.float64)
-    gc = gc.contiguous()
-    go = gobs.to(device=gc.device, dtype=torch.float64).contiguous()
+    gc = _dev_tensor(gcalc, torch.float64)
+    squeeze = gc.dim() == 1
+    gc = gc.reshape(1, -1) if squeeze else gc
+    if gc.dim() != 2:
+        raise NativeError(f'gcalc must be [B, R] or [R] (got '
+                          f'{list(gc.shape)})')
+    go = _dev_tensor(gobs, torch.float64, gc.device)
+    _check_len(go, gc.shape[1], 'gobs')
     out = torch.empty((gc.shape[0], 2), dtype=torch.float64, device=gc.device)
     ctx = context(gc.device.index)
     ctx.call('pyiid_potential', ctypes.c_void_p(go.data_ptr()),
@@ -318,9 +352,14 @@ def potential_grad(grad_pdf_t, gcalc, gobs, kind='rw'):
     """sum_r c_r dG_r for each [a, c] row of grad_pdf [N, 3, R] -> [N, 3]:
     get_grad_rw / get_grad_chi_sq (kernels/master_kernel.py:293-376)."""
     import ctypes
-    gp = grad_pdf_t.to(torch.float64).contiguous()
-    gc = gcalc.to(device=gp.device, dtype=torch.float64).contiguous()
-    go = gobs.to(device=gp.device, dtype=torch.float64).contiguous()
+    gp = _dev_tensor(grad_pdf_t, torch.float64)
+    if gp.dim() != 3 or gp.shape[1] != 3:
+        raise NativeError(f'grad_pdf must be [N, 3, R] (got '
+                          f'{list(gp.shape)})')
+    gc = _dev_tensor(gcalc, torch.float64, gp.device)
+    go = _dev_tensor(gobs, torch.float64, gp.device)
+    _check_len(gc, gp.shape[2], 'gcalc')
+    _check_len(go, gp.shape[2], 'gobs')
     n = gp.shape[0]
     out = torch.zeros((n, 3), dtype=torch.float64, device=gp.device)
     if n:
@@ -354,7 +393,8 @@ def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
     rg = _np(rgrid, np.float64)
     b = len(off) - 1
     dev = pos.device
-    go = gobs.to(device=dev, dtype=torch.float64).contiguous()
+    go = _dev_tensor(gobs, torch.float64, dev)
+    _check_len(go, len(rg), 'gobs')
     if out is None:
         out = {
             'energy': torch.empty((b, 2), dtype=torch.float64, device=dev),
@@ -365,8 +405,19 @@ def batch_potential_grad(positions, species, offsets, scatter, qstep, rstep,
             'fq': torch.empty((b, tab.shape[1]), dtype=torch.float32,
                               device=dev),
         }
+    else:
+        for key, dt, size in (('energy', torch.float64, 2 * b),
+                              ('gcalc', torch.float64, b * len(rg)),
+                              ('fq', torch.float32, b * tab.shape[1])):
+            _check_dev(out[key], key, dt)
+            _check_len(out[key], size, key)
+        if want_grad and out.get('grad') is not None:
+            _check_dev(out['grad'], 'grad', torch.float32)
+            if out['grad'].numel() < 3 * int(off.max()):
+                raise NativeError(f'grad has {out["grad"].numel()} values, '
+                                  f'the offsets cover {int(off.max())} atoms')
     ctx = context(dev.index)
-    g = out.get('grad')
+    g = out.get('grad') if want_grad else None
     ctx.call('pyiid_batch_potential_grad', ctypes.c_void_p(pos.data_ptr()),
              _ptr(sp, ctypes.c_int32), _ptr(off, ctypes.c_int32), b,
              _ptr(tab, ctypes.c_float), tab.shape[0], tab.shape[1],
@@ -420,7 +471,8 @@ def mh_init(positions, species, offsets, scatter, qstep, rstep, rgrid, qmin,
     b = len(off) - 1
     k = tab.shape[1]
     dev = pos.device
-    go = gobs.to(device=dev, dtype=torch.float64).contiguous()
+    go = _dev_tensor(gobs, torch.float64, dev)
+    _check_len(go, len(rg), 'gobs')
     if state is None:
         state = {}
     if state.get('buf') is None or state.get('n_configs') != b or \

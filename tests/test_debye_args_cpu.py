@@ -2,8 +2,10 @@
 
 The C ABI receives bare pointers, so the Python layer checks what the
 library will read: 3 floats per atom, one species id per atom, a 2-D
-form-factor table, and for packed configurations at least as many position
-rows and species ids as the offsets cover.  A violation raises NativeError
+form-factor table, for packed configurations at least as many position
+rows and species ids as the offsets cover, [.., 3, ..] gradients, and
+gobs / gcalc as long as the r grid; host data for the transforms and
+potentials is copied to the device first.  A violation raises NativeError
 before any device work (here on the CPU, where no device exists)."""
 import numpy as np
 import pytest
@@ -66,3 +68,57 @@ def test_packed_configurations_cover_their_buffers():
     with pytest.raises(NativeError, match='offsets must be'):
         debye._check_packed(7, np.zeros(7, np.int32),
                             np.array([0], np.int32), tab)
+
+
+@pytest.fixture
+def host_tensors(monkeypatch):
+    """Runs the checks of the transform and potential calls on the CPU: the
+    copy to the device is replaced by a host copy, so a call with valid
+    shapes gets as far as the device context, which does not exist here."""
+    def host_tensor(t, dtype, device=None):
+        if not isinstance(t, torch.Tensor):
+            t = torch.as_tensor(np.asarray(t))
+        return t.detach().to(dtype=dtype).contiguous()
+    monkeypatch.setattr(debye, '_dev_tensor', host_tensor)
+
+
+def test_transform_shapes(host_tensors):
+    rg = np.arange(0.0, 4.0, 0.1)
+    with pytest.raises(NativeError, match='F\\(Q\\) must be'):
+        debye.pdf(torch.zeros(2, 3, 4), 0.1, 0.1, rg, 0.0)
+    with pytest.raises(NativeError, match='no CUDA'):
+        debye.pdf(torch.zeros(2, 50), 0.1, 0.1, rg, 0.0)
+    with pytest.raises(NativeError, match='gradient must be'):
+        debye.grad_pdf(torch.zeros(5, 2, 50), 0.1, 0.1, rg, 0.0)
+    with pytest.raises(NativeError, match='gradient must be'):
+        debye.grad_pdf(torch.zeros(5, 50), 0.1, 0.1, rg, 0.0)
+    with pytest.raises(NativeError, match='no CUDA'):
+        debye.grad_pdf(torch.zeros(5, 3, 50), 0.1, 0.1, rg, 0.0)
+
+
+def test_potential_lengths_follow_the_r_grid(host_tensors):
+    r = 40
+    with pytest.raises(NativeError, match='gcalc must be'):
+        debye.potential(torch.zeros(r), torch.zeros(2, 2, r))
+    with pytest.raises(NativeError, match=f'gobs has {r - 1} values'):
+        debye.potential(torch.zeros(r - 1), torch.zeros(2, r))
+    with pytest.raises(NativeError, match='no CUDA'):
+        debye.potential(torch.zeros(r), torch.zeros(2, r))
+    with pytest.raises(NativeError, match='grad_pdf must be'):
+        debye.potential_grad(torch.zeros(5, r), torch.zeros(r),
+                             torch.zeros(r))
+    with pytest.raises(NativeError, match=f'gcalc has {r - 1} values'):
+        debye.potential_grad(torch.zeros(5, 3, r), torch.zeros(r - 1),
+                             torch.zeros(r))
+    with pytest.raises(NativeError, match=f'gobs has {r + 1} values'):
+        debye.potential_grad(torch.zeros(5, 3, r), torch.zeros(r),
+                             torch.zeros(r + 1))
+    with pytest.raises(NativeError, match='no CUDA'):
+        debye.potential_grad(torch.zeros(5, 3, r), torch.zeros(r),
+                             torch.zeros(r))
+
+
+def test_without_a_device_host_data_is_refused_cleanly():
+    # the real copy to the device raises NativeError, not a torch error
+    with pytest.raises(NativeError, match='no CUDA'):
+        debye.pdf(np.zeros(50, np.float32), 0.1, 0.1, np.arange(0, 4, .1), 0)
