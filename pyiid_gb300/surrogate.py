@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import debye
-from ._native import context
+from ._native import NativeError, context
 from .atoms import kB
 
 __all__ = ['RBFMLPSurrogate', 'DelayedAcceptanceMH', 'ExactSingleAtomMH',
@@ -91,6 +91,10 @@ class RBFMLPSurrogate:
         pos = debye.as_positions(positions)
         off, offp = _i32(offsets)
         n = int(off[-1])
+        if off.ndim != 1 or len(off) < 2 or pos.shape[0] < int(off.max()):
+            raise NativeError(f'offsets {list(off.shape)} must be [B + 1] '
+                              f'and cover at most the {pos.shape[0]} '
+                              'positions')
         fb = torch.empty((n, self.C), dtype=torch.bfloat16, device=self.dev)
         ff = (torch.empty((n, self.C), dtype=torch.float32, device=self.dev)
               if want_f32 else None)
@@ -112,9 +116,16 @@ class RBFMLPSurrogate:
     def forward(self, feat_bf16, offsets):
         """Rw estimates [B] (FP64) for descriptor rows of packed configs."""
         off, offp = _i32(offsets)
+        if not (isinstance(feat_bf16, torch.Tensor) and feat_bf16.is_cuda and
+                feat_bf16.dtype == torch.bfloat16 and
+                feat_bf16.is_contiguous() and
+                feat_bf16.numel() == int(off[-1]) * self.C):
+            raise NativeError(f'descriptors must be a contiguous bfloat16 '
+                              f'CUDA tensor [{int(off[-1])}, {self.C}]')
         w1b, b1, w2b = self._effective()
         self._last = (w1b, b1, w2b)  # keep alive for backward
         e = torch.empty(len(off) - 1, dtype=torch.float64, device=self.dev)
+        self._last_b = len(off) - 1
         p = self.params
         self.ctx.call('pyiid_mlp_forward', _vp(feat_bf16), int(off[-1]),
                       self.C, offp, len(off) - 1, _vp(w1b), _vp(b1),
@@ -126,7 +137,12 @@ class RBFMLPSurrogate:
         """Parameter gradients (in the standardised parametrisation) of the
         last forward for dL/dE = d_energy [B]."""
         g = {k: torch.empty_like(v) for k, v in self.params.items()}
-        self.ctx.call('pyiid_mlp_backward', _vp(d_energy.double().contiguous()),
+        de = torch.as_tensor(d_energy).to(device=self.dev,
+                                          dtype=torch.float64).contiguous()
+        if de.numel() != getattr(self, '_last_b', -1):
+            raise NativeError('d_energy must hold one value per configuration '
+                              'of the last forward')
+        self.ctx.call('pyiid_mlp_backward', _vp(de),
                       _vp(g['w1']), _vp(g['b1']), _vp(g['w2']), _vp(g['b2']),
                       _vp(g['w3']), _vp(g['b3']))
         if self.mu is not None:

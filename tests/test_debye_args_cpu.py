@@ -122,3 +122,31 @@ def test_without_a_device_host_data_is_refused_cleanly():
     # the real copy to the device raises NativeError, not a torch error
     with pytest.raises(NativeError, match='no CUDA'):
         debye.pdf(np.zeros(50, np.float32), 0.1, 0.1, np.arange(0, 4, .1), 0)
+
+
+def test_surrogate_checks_its_device_buffers(monkeypatch):
+    """The surrogate's kernels read descriptors [N, C] in bfloat16 on the
+    device and one dL/dE per configuration of the last forward; anything
+    else is refused before the library is called (a recording fake stands in
+    for the device context)."""
+    from pyiid_gb300 import surrogate
+
+    calls = []
+
+    class FakeCtx:
+        def call(self, name, *args, **kw):
+            calls.append(name)
+
+    monkeypatch.setattr(surrogate, 'context', lambda index=None: FakeCtx())
+    sur = surrogate.RBFMLPSurrogate(n_centres=8, n_hidden=16, device='cpu')
+    off = np.array([0, 5, 9])
+    with pytest.raises(NativeError, match='descriptors must be'):
+        sur.forward(torch.zeros((9, 8), dtype=torch.bfloat16), off)
+    with pytest.raises(NativeError, match='d_energy'):
+        sur.backward(torch.zeros(2, dtype=torch.float64))  # no forward yet
+    sur._last_b = 2
+    with pytest.raises(NativeError, match='d_energy'):
+        sur.backward(torch.zeros(3, dtype=torch.float64))
+    assert calls == []
+    g = sur.backward(np.array([0.5, -1.0]))   # host values are accepted
+    assert calls == ['pyiid_mlp_backward'] and set(g) == set(sur.params)
