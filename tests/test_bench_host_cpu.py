@@ -1,0 +1,68 @@
+"""bench.py's host-side helpers, which fill fields of its JSON line: the
+clock summary of the nvidia-smi samples (median SM clock under load,
+throttle reasons), the DRAM traffic read from the committed ncu summary,
+the workload and its config block."""
+import os
+
+import numpy as np
+
+from conftest import REPO
+
+
+def _sampler(tmp_lines):
+    import bench
+    s = bench.ClockSampler(0)
+    os.makedirs(os.path.join(REPO, 'tests', '_build'), exist_ok=True)
+    s.path = os.path.join(REPO, 'tests', '_build', 'clocks_sample.csv')
+    with open(s.path, 'w') as f:
+        f.write('\n'.join(tmp_lines) + '\n')
+    s.proc = object()  # as if nvidia-smi had been started
+    return s
+
+
+def test_clock_summary_under_load_and_reasons():
+    idle = '1980, 2070, 150.0, 0x0, Not Active, Not Active, Not Active, ' \
+           'Not Active'
+    busy = '2070, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, ' \
+           'Not Active'
+    capped = '1950, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, ' \
+             'Active'
+    s = _sampler([idle, busy, busy, capped, 'garbage line', '1, 2, x, 4'])
+    out = s.summary()
+    # samples below half the peak power are not "under load"
+    assert out['sm_mhz'] == 2070.0
+    assert out['sm_max_mhz'] == 2070.0
+    assert out['power_w_max'] == 1390.0
+    assert out['samples'] == 4
+    assert out['reasons'] == ['sw_power_cap']
+    hot = '1500, 2070, 1000.0, 0x40, Not Active, Active, Not Active, ' \
+          'Not Active'
+    assert _sampler([hot]).summary()['reasons'] == ['hw_thermal_slowdown']
+
+
+def test_clock_summary_without_samples():
+    import bench
+    s = bench.ClockSampler(0)
+    assert s.summary()['reasons'] == ['unavailable']
+    assert _sampler(['nothing useful']).summary()['reasons'] == ['no samples']
+
+
+def test_traffic_comes_from_the_committed_profile():
+    import bench
+    t = bench.traffic_from_profile('fqgrad2_kernel')
+    assert t is not None and 3.0e8 < t < 4.0e8   # ~332 MB per launch
+    assert bench.traffic_from_profile('gradfq2_kernel') is not None
+    assert bench.traffic_from_profile('no_such_kernel') is None
+
+
+def test_workload_and_config_block():
+    import bench
+    pos, sp, tab, n_bins, k_begin = bench.workload(2000)
+    assert pos.shape == (2000, 3) and pos.dtype == np.float32
+    assert n_bins == 1500 and k_begin == 25          # Q 0.5-30 step 0.02
+    assert sp.shape == (2000,) and tab.shape == (1, 1500)
+    c = bench.config_dict(1500, 25, {'path': 'x'})
+    assert c['n_atoms'] == 20000 and c['bins_returned'] == 1475
+    assert c['pairs'] == 20000 * 19999 // 2 and c['path'] == 'x'
+    assert 'flushed' in c['l2']
+    assert bench.measured_hbm_gbs() is None or bench.measured_hbm_gbs() > 1000
