@@ -1,7 +1,8 @@
 """bench.py's host-side helpers, which fill fields of its JSON line: the
 clock summary of the nvidia-smi samples (median SM clock under load,
 throttle reasons), the DRAM traffic read from the committed ncu summary,
-the workload and its config block."""
+the workload and its config block, the bounded CPU sample and the line of
+the reference arm (--impl reference)."""
 import os
 
 import numpy as np
@@ -66,3 +67,36 @@ def test_workload_and_config_block():
     assert c['pairs'] == 20000 * 19999 // 2 and c['path'] == 'x'
     assert 'flushed' in c['l2']
     assert bench.measured_hbm_gbs() is None or bench.measured_hbm_gbs() > 1000
+
+
+def test_cpu_sample_reports_a_bounded_port_measurement():
+    import bench
+    out = bench.cpu_sample(target_s=0.2, threads=2, n_atoms=300)
+    assert out['kind'] == 'port' and out['unit'] == 'evals/s'
+    assert out['cores'] == 2 and out['value'] > 0
+    assert 'of 44850 pairs' in out['sample'] and out['seconds'] > 0
+
+
+def test_reference_arm_line_follows_the_contract(monkeypatch):
+    """--impl reference: the reference's CPU path (the port here) on the
+    same metric, config and units, with a cpu_baseline and an e2e block
+    that moves no bytes; rank > 0 prints nothing."""
+    import types
+    import bench
+    samples = iter([0.5, 0.7])
+
+    def fake_sample(target_s=15.0, threads=0, n_atoms=None):
+        return {'value': next(samples), 'unit': 'evals/s', 'cores': 8,
+                'kind': 'port', 'sample': 'stub', 'seconds': 1.0}
+    monkeypatch.setattr(bench, 'cpu_sample', fake_sample)
+    args = types.SimpleNamespace(steps=2, warmup=0)
+    assert bench.run_reference(args, 1, 2) is None
+    line = bench.run_reference(args, 0, 1)
+    assert line['impl'] == 'reference' and line['metric'] == bench.METRIC
+    assert abs(line['value'] - 0.6) < 1e-12
+    assert line['unit'] == 'evals/s' and line['higher_is_better'] is True
+    assert line['cpu_baseline']['value'] == line['value']
+    assert line['cpu_baseline']['kind'] == 'port'
+    assert line['e2e'] == {'value': line['value'], 'unit': 'evals/s',
+                           'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
+    assert line['config']['bins_returned'] == 1475
