@@ -259,3 +259,50 @@ def test_batched_nuts_scheduler_reproduces_sequential_chains():
     # one batched evaluation per tree leaf of the deepest chain (twice with
     # the centred re-evaluation), not one per leaf per chain
     assert b.evaluations < sum(m['samples_total'] for _, m, _ in seq)
+
+
+class _Voxelled(_Well):
+    """A well that also reports voxel and atomwise energies (as the spring
+    calculators do), to check MultiCalc's sums of them."""
+
+    def calculate_voxel_energy(self, atoms, resolution):
+        c = np.diagonal(atoms.get_cell())
+        return np.full(tuple(int(x / resolution) for x in c), self.k)
+
+    def calculate_atomwise_energy(self, atoms):
+        return np.full(len(atoms), 2.0 * self.k)
+
+
+def test_multicalc_sums_energies_forces_and_maps():
+    """pyiid/calc/multi_calc.py:8-125: the composite calculator's energy,
+    forces, voxel and atomwise energies are the sums over its calculators
+    (those without voxel / atomwise methods contribute nothing), and the
+    atoms keep the composite calculator attached."""
+    from pyiid_gb300.calc.multi_calc import MultiCalc
+    x0 = [[0.2, 0, 0], [3, 0.1, 0], [0, 3, 0.3], [3, 3, 0]]
+    parts = [_Well(k=0.7, x0=x0), _Well(k=0.2), _Voxelled(k=0.5)]
+    a = _square()
+    a.set_cell([4.0, 4.0, 4.0])
+    want_e, want_f = 0.0, np.zeros((4, 3))
+    for c in parts:
+        b = _square()
+        b.set_calculator(c)
+        want_e += b.get_potential_energy()
+        want_f += b.get_forces()
+    mc = MultiCalc(calc_list=parts)
+    a.set_calculator(mc)
+    assert abs(a.get_potential_energy() - want_e) <= 1e-12 * abs(want_e)
+    assert np.allclose(a.get_forces(), want_f, rtol=0, atol=1e-12)
+    assert a.calc is mc
+    vox = mc.calculate_voxel_energy(a, 0.5)
+    assert vox.shape == (8, 8, 8) and np.all(vox == 0.5)
+    assert np.all(mc.calculate_atomwise_energy(a) == 1.0)
+    # energies follow the positions (the sub-calculators' caches too)
+    a.positions[0, 0] += 0.5
+    b = _square()
+    b.positions[0, 0] += 0.5
+    e2 = 0.0
+    for c in parts:
+        b.set_calculator(c)
+        e2 += b.get_potential_energy()
+    assert abs(a.get_potential_energy() - e2) <= 1e-12 * abs(e2)
