@@ -98,3 +98,56 @@ def test_no_cpu_fallback_without_gpu():
     with pytest.raises(NativeError):
         debye.fq(np.zeros((2, 3), np.float32), np.zeros(2, np.int32),
                  np.ones((1, 10), np.float32), 0.1)
+
+
+def test_atoms_formulas_indexing_and_arrays():
+    """ASE semantics a drop-in user relies on: formulas, atom views that
+    write through, slices and boolean masks as new Atoms, deletion keeping
+    every per-atom array aligned, concatenation filling missing arrays."""
+    a = Atoms('Au2PtPd', [[0, 0, 0], [1, 0, 0], [2, 0, 0], [3, 0, 0]])
+    assert list(a.numbers) == [79, 79, 78, 46]
+    a.set_array('tag', np.arange(4) * 10)
+    a.set_momenta(np.arange(12.0).reshape(4, 3))
+    a[2].position = [5.0, 5.0, 5.0]                 # view writes through
+    assert np.array_equal(a.positions[2], [5, 5, 5])
+    assert a[-1].symbol == 'Pd'
+    with pytest.raises(IndexError):
+        a[4]
+    b = a[1:3]
+    assert len(b) == 2 and list(b.get_array('tag')) == [10, 20]
+    c = a[a.numbers == 79]
+    assert list(c.numbers) == [79, 79]
+    del a[[0, 2]]
+    assert list(a.numbers) == [79, 46]
+    assert list(a.get_array('tag')) == [10, 30]
+    assert np.array_equal(a.get_momenta()[1], [9, 10, 11])
+    d = a + Atoms('Pt', [[7, 7, 7]])
+    assert list(d.numbers) == [79, 46, 78]
+    assert d.get_array('tag')[-1] == 0 and np.all(d.get_momenta()[-1] == 0)
+    with pytest.raises(ValueError):
+        d.set_array('tag', np.arange(5))
+    d.set_array('tag', None)
+    assert not d.has('tag')
+    # get_array copies unless asked not to
+    arr = d.get_array('numbers')
+    arr[0] = 1
+    assert d.numbers[0] == 79
+    d.get_array('numbers', copy=False)[0] = 1
+    assert d.numbers[0] == 1
+
+
+def test_atoms_mechanics():
+    a = Atoms('H2Au', [[0, 0, 0], [2, 0, 0], [0, 0, 4]])
+    m = a.get_masses()
+    com = (m[:, None] * a.positions).sum(0) / m.sum()
+    assert np.allclose(a.get_center_of_mass(), com)
+    a.set_velocities(np.ones((3, 3)))
+    assert np.allclose(a.get_momenta(), m[:, None])
+    ke = 0.5 * 3 * m.sum()
+    assert abs(a.get_kinetic_energy() - ke) < 1e-12
+    assert abs(a.get_temperature() - 2 * ke / (9 * kB)) < 1e-9
+    a.center(about=[1.0, 1.0, 1.0])
+    p = a.positions
+    assert np.allclose(0.5 * (p.min(0) + p.max(0)), [1, 1, 1])
+    e = Atoms()
+    assert len(e) == 0 and e.get_temperature() == 0.0
