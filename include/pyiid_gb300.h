@@ -207,6 +207,17 @@ int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
 int pyiid_potential(pyiid_ctx *ctx, const double *gobs, const double *gcalc,
                     int n_configs, int n_r, int potential, double *out);
 
+/* Rw with per-point weights, get_rw(gobs, gcalc, weight) of
+ * kernels/master_kernel.py:206-236:
+ *   a = (gcalc.gobs)/(gcalc.gcalc) (unweighted, get_scale :388-389);
+ *   a <= 0 -> (Rw, scale) = (1, 1);
+ *   else Rw = sqrt(sum_i w_i (gobs_i - a gcalc_i)^2 / sum_i w_i gobs_i^2).
+ *   weight : device double [n_r]; other arguments as pyiid_potential
+ *            (out[2 b] = Rw, out[2 b + 1] = scale). */
+int pyiid_potential_weighted(pyiid_ctx *ctx, const double *gobs,
+                             const double *gcalc, const double *weight,
+                             int n_configs, int n_r, double *out);
+
 /* Gradient of the potential from an explicit G(r) gradient:
  *   grad[a][c] = sum_r c_r * grad_pdf[a][c][r]  with the reference's c_r.
  *   grad_pdf : device double [n_atoms][3][n_r]

@@ -5,8 +5,10 @@ gcc -O3 -fopenmp -shared -fPIC oracle/debye_ref.c -> oracle/_lib/libdebye_ref.so
 The reference itself is pure Python (numba), so there is no reference C/C++
 source to compile into oracle/_ref; its Python code is exercised by
 tests/golden/make_golden.py instead.  No -march flags: the same source is
-built on x86_64 here and on aarch64 GPU hosts.
+built on x86_64 here and on aarch64 GPU hosts.  The library is rebuilt unless
+the stamp beside it equals the SHA-256 of the source and the command line.
 """
+import hashlib
 import os
 import shutil
 import subprocess
@@ -18,15 +20,22 @@ SRC = os.path.join(HERE, 'debye_ref.c')
 
 
 def build(force=False):
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
-        return LIB
-    os.makedirs(LIBDIR, exist_ok=True)
     cc = os.environ.get('CC') or shutil.which('gcc') or 'cc'
+    flags = ['-O3', '-fopenmp', '-shared', '-fPIC']
+    h = hashlib.sha256(' '.join([cc, *flags]).encode())
+    with open(SRC, 'rb') as f:
+        h.update(f.read())
+    digest, stamp = h.hexdigest(), LIB + '.sha256'
+    if not force and os.path.exists(LIB) and os.path.exists(stamp):
+        with open(stamp) as f:
+            if f.read().strip() == digest:
+                return LIB
+    os.makedirs(LIBDIR, exist_ok=True)
     tmp = LIB + '.tmp'
-    subprocess.run([cc, '-O3', '-fopenmp', '-shared', '-fPIC', '-o', tmp, SRC,
-                    '-lm'], check=True)
+    subprocess.run([cc, *flags, '-o', tmp, SRC, '-lm'], check=True)
     os.replace(tmp, LIB)
+    with open(stamp, 'w') as f:
+        f.write(digest + '\n')
     return LIB
 
 

@@ -50,6 +50,8 @@ _SIGNATURES = {
     'pyiid_grad_pdf': (_c_int, [_vp, _vp, _c_int, _c_int, _c_dbl, _c_dbl,
                                 _f64p, _c_int, _c_dbl, _vp]),
     'pyiid_potential': (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _vp]),
+    'pyiid_potential_weighted': (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int,
+                                          _vp]),
     'pyiid_potential_grad': (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int,
                                       _c_int, _vp]),
     'pyiid_batch_potential_grad': (_c_int, [
@@ -107,10 +109,13 @@ def load():
         if _lib is not None:
             return _lib
         path = _build.lib_path()
-        if not os.path.exists(path):
-            try:
-                _build.build()
-            except Exception as e:  # noqa: BLE001
+        # rebuild when the stamp does not match the sources (a copied or
+        # checked-out library next to edited sources is never loaded); a
+        # machine without nvcc loads what is there
+        try:
+            _build.build()
+        except Exception as e:  # noqa: BLE001
+            if not os.path.exists(path):
                 raise NativeError(f'native library {path} is missing and '
                                   f'could not be built: {e}') from e
         try:

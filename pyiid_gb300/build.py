@@ -3,7 +3,13 @@
 One translation unit (``csrc/capi.cu``) compiled with nvcc for
 ``-gencode arch=compute_103a,code=sm_103a``; the CUDA runtime is linked
 statically so the library has no path dependence on the toolkit.
+
+The library is rebuilt unless its stamp (``libpyiid_gb300.so.sha256`` beside
+it) equals the SHA-256 of every source under ``csrc/``, the public header,
+the nvcc command line and the nvcc version, so a library copied or checked
+out next to edited sources is never reused.
 """
+import hashlib
 import os
 import shutil
 import subprocess
@@ -36,18 +42,53 @@ def lib_path():
     return os.path.join(LIBDIR, LIBNAME)
 
 
+def _flags():
+    return [*ARCH, '-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC',
+            '-shared', '-cudart', 'static']
+
+
+def source_hash(nvcc=None):
+    """SHA-256 over the sources (names and bytes), the nvcc flags and the
+    nvcc version string."""
+    h = hashlib.sha256()
+    for d in _sources():
+        h.update(os.path.relpath(d, REPO).encode() + b'\0')
+        with open(d, 'rb') as f:
+            h.update(f.read())
+        h.update(b'\0')
+    h.update(' '.join(_flags()).encode())
+    nvcc = nvcc or _nvcc()
+    res = subprocess.run([nvcc, '--version'], capture_output=True, text=True)
+    h.update(res.stdout.encode())
+    return h.hexdigest()
+
+
+def stamp_path():
+    return lib_path() + '.sha256'
+
+
+def is_current(nvcc=None):
+    """True when the built library's stamp matches the current sources."""
+    out, st = lib_path(), stamp_path()
+    if not (os.path.exists(out) and os.path.exists(st)):
+        return False
+    with open(st) as f:
+        return f.read().strip() == source_hash(nvcc)
+
+
 def build(force=False, verbose=False):
-    """Compile the library if any source is newer than it; return its path."""
+    """Compile the library unless its stamp matches the sources; return its
+    path."""
     out = lib_path()
-    deps = _sources()
-    if (not force and os.path.exists(out) and
-            os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps)):
-        return out
+    nvcc = _nvcc()
+    digest = source_hash(nvcc)
+    if not force and os.path.exists(out) and os.path.exists(stamp_path()):
+        with open(stamp_path()) as f:
+            if f.read().strip() == digest:
+                return out
     os.makedirs(LIBDIR, exist_ok=True)
     tmp = out + '.tmp'
-    cmd = [_nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17',
-           '-Xcompiler', '-fPIC', '-shared', '-cudart', 'static',
-           '-o', tmp, os.path.join(CSRC, 'capi.cu')]
+    cmd = [nvcc, *_flags(), '-o', tmp, os.path.join(CSRC, 'capi.cu')]
     if verbose:
         cmd.insert(1, '-Xptxas=-v')
         print(' '.join(cmd))
@@ -57,6 +98,9 @@ def build(force=False, verbose=False):
     if verbose:
         print(res.stderr)
     os.replace(tmp, out)
+    with open(stamp_path() + '.tmp', 'w') as f:
+        f.write(digest + '\n')
+    os.replace(stamp_path() + '.tmp', stamp_path())
     return out
 
 

@@ -1205,6 +1205,20 @@ int pyiid_potential(pyiid_ctx *ctx, const double *gobs, const double *gcalc,
   return PYIID_OK;
 }
 
+int pyiid_potential_weighted(pyiid_ctx *ctx, const double *gobs,
+                             const double *gcalc, const double *weight,
+                             int n_configs, int n_r, double *out) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  if (n_configs < 1 || n_r < 1)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  if (!weight) return fail(ctx, PYIID_ERR_INVALID_ARG, "null weight");
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  potential_kernel<<<n_configs, 256, 0, ctx->stream>>>(
+      gobs, gcalc, n_r, PYIID_POTENTIAL_RW, out, nullptr, weight);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
 int pyiid_potential_grad(pyiid_ctx *ctx, const double *grad_pdf,
                          const double *gcalc, const double *gobs, int n_atoms,
                          int n_r, int potential, double *grad) {

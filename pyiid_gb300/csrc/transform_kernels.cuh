@@ -77,37 +77,46 @@ struct PotentialValue {
 };
 
 // The potential of one configuration, computed by the whole CTA (every
-// thread returns the same values).  scratch: 32 * 3 doubles of shared memory.
+// thread returns the same values).  scratch: 32 * 4 doubles of shared memory.
+// weight (Rw only, may be null): per-point weights of get_rw
+// (master_kernel.py:226-235): Rw = sqrt(sum w (go - a gc)^2 / sum w go^2)
+// with the unweighted scale a; ee and gce (used by the gradients, which the
+// reference never weights) stay unweighted.
 __device__ __forceinline__ PotentialValue potential_value(
     const double *__restrict__ gobs, const double *__restrict__ gc, int n_r,
-    int potential, double *scratch) {
-  double v3[3] = {0.0, 0.0, 0.0};
+    int potential, double *scratch,
+    const double *__restrict__ weight = nullptr) {
+  double v3[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < n_r; i += blockDim.x) {
     const double c = gc[i], o = gobs[i];
     v3[0] += c * o;
     v3[1] += c * c;
     v3[2] += o * o;
+    if (weight) v3[3] += weight[i] * o * o;
   }
-  block_sum<3>(v3, scratch);
-  const double gco = v3[0], gcc = v3[1], goo = v3[2];
+  block_sum<4>(v3, scratch);
+  const double gco = v3[0], gcc = v3[1];
+  const double goo = weight ? v3[3] : v3[2];
   const double a = gco / gcc;
   // the reference replaces a non-positive scale by 1; a NaN scale stays NaN
   const double s = (a <= 0.0) ? 1.0 : a;
-  double v2[2] = {0.0, 0.0};
+  double v2[3] = {0.0, 0.0, 0.0};
   for (int i = threadIdx.x; i < n_r; i += blockDim.x) {
     const double e = gobs[i] - s * gc[i];
     v2[0] += e * e;
     v2[1] += gc[i] * e;
+    if (weight) v2[2] += weight[i] * e * e;
   }
-  block_sum<2>(v2, scratch);
+  block_sum<3>(v2, scratch);
   PotentialValue r;
   r.ee = v2[0];
   r.gce = v2[1];
   r.a = a;
   r.gcc = gcc;
   r.scale = s;
+  const double top = weight ? v2[2] : v2[0];
   if (potential == 0)
-    r.value = (a <= 0.0) ? 1.0 : sqrt(r.ee / goo);
+    r.value = (a <= 0.0) ? 1.0 : sqrt(top / goo);
   else
     r.value = r.ee;
   return r;
@@ -116,11 +125,13 @@ __device__ __forceinline__ PotentialValue potential_value(
 __global__ void potential_kernel(const double *__restrict__ gobs,
                                  const double *__restrict__ gcalc, int n_r,
                                  int potential, double *__restrict__ out,
-                                 float *__restrict__ cvec) {
-  __shared__ double scratch[32 * 3];
+                                 float *__restrict__ cvec,
+                                 const double *__restrict__ weight = nullptr) {
+  __shared__ double scratch[32 * 4];
   const int b = blockIdx.x;
   const double *gc = gcalc + (size_t)b * n_r;
-  const PotentialValue pv = potential_value(gobs, gc, n_r, potential, scratch);
+  const PotentialValue pv =
+      potential_value(gobs, gc, n_r, potential, scratch, weight);
   const double value = pv.value, s = pv.scale, a = pv.a, gcc = pv.gcc;
   const double ee = pv.ee, gce = pv.gce;
   const double pre = (potential == 0) ? -value / ee : -2.0;

@@ -328,9 +328,11 @@ def grad_pdf(grad_fq_t, qstep, rstep, rgrid, qmin):
     return out
 
 
-def potential(gobs, gcalc, kind='rw'):
+def potential(gobs, gcalc, kind='rw', weight=None):
     """(value, scale) rows [B, 2] for gcalc [B, R] (or [R] -> [2]): get_rw /
-    get_chi_sq with get_scale (kernels/master_kernel.py:206-266, 388-389)."""
+    get_chi_sq with get_scale (kernels/master_kernel.py:206-266, 388-389).
+    ``weight`` ([R], Rw only): get_rw's per-point weights (the scale stays
+    unweighted, as in the reference)."""
     import ctypes
     gc = _dev_tensor(gcalc, torch.float64)
     squeeze = gc.dim() == 1
@@ -342,9 +344,19 @@ def potential(gobs, gcalc, kind='rw'):
     _check_len(go, gc.shape[1], 'gobs')
     out = torch.empty((gc.shape[0], 2), dtype=torch.float64, device=gc.device)
     ctx = context(gc.device.index)
-    ctx.call('pyiid_potential', ctypes.c_void_p(go.data_ptr()),
-             ctypes.c_void_p(gc.data_ptr()), gc.shape[0], gc.shape[1],
-             POTENTIALS[kind], ctypes.c_void_p(out.data_ptr()))
+    if weight is not None:
+        if kind != 'rw':
+            raise NativeError('weights apply to Rw only (the reference\'s '
+                              'get_chi_sq takes none)')
+        w = _dev_tensor(weight, torch.float64, gc.device)
+        _check_len(w, gc.shape[1], 'weight')
+        ctx.call('pyiid_potential_weighted', ctypes.c_void_p(go.data_ptr()),
+                 ctypes.c_void_p(gc.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                 gc.shape[0], gc.shape[1], ctypes.c_void_p(out.data_ptr()))
+    else:
+        ctx.call('pyiid_potential', ctypes.c_void_p(go.data_ptr()),
+                 ctypes.c_void_p(gc.data_ptr()), gc.shape[0], gc.shape[1],
+                 POTENTIALS[kind], ctypes.c_void_p(out.data_ptr()))
     return out[0] if squeeze else out
 
 

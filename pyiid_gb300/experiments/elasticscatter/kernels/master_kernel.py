@@ -46,18 +46,21 @@ def grad_pdf(grad_fq, rstep, qstep, rgrid, qmin):
     return debye.grad_pdf(g, qstep, rstep, rgrid, qmin).cpu().numpy()
 
 
-def _pot(gobs, gcalc, kind):
+def _pot(gobs, gcalc, kind, weight=None):
+    w = None if weight is None else _dev(weight, np.float64)
     out = debye.potential(_dev(gobs, np.float64), _dev(gcalc, np.float64),
-                          kind).cpu().numpy()
+                          kind, weight=w).cpu().numpy()
     return out
 
 
 def get_rw(gobs, gcalc, weight=None):
     """(Rw, scale); (1, 1) for a non-positive scale (master_kernel.py:206-236).
-    Only the unit weight the reference's callers use is supported."""
-    if weight is not None and not np.all(np.asarray(weight) == 1):
-        raise NotImplementedError('only unit weights are supported')
-    v, s = _pot(gobs, gcalc, 'rw')
+    ``weight`` weighs the residual and the normalisation point by point; the
+    scale is the unweighted one, as in the reference."""
+    if weight is not None:
+        weight = np.broadcast_to(np.asarray(weight, dtype=np.float64),
+                                 np.shape(gcalc))
+    v, s = _pot(gobs, gcalc, 'rw', weight)
     if s == 1.0 and v == 1.0:
         return 1, 1
     return v, s

@@ -1,7 +1,10 @@
 """Generate golden vectors by running the reference pyIID code itself.
 
-Run from the repository root:  python tests/golden/make_golden.py [REF_ROOT]
-(REF_ROOT defaults to /root/reference).  Writes tests/golden/reference_*.npz.
+Run from the repository root:
+    python tests/golden/make_golden.py REF_ROOT
+or with PYIID_REFERENCE_ROOT=REF_ROOT in the environment, where REF_ROOT is the
+root of a pyIID source checkout (the directory holding ``pyiid/``).
+Writes tests/golden/reference_*.npz.
 
 The reference is pure Python with numba-JIT'd loops.  numba, xraylib, mkl and
 ASE are not installed, so this script registers small stand-in modules:
@@ -200,6 +203,11 @@ def main(ref_root):
         out[key + '__positions'] = pb
         out[key + '__numbers'] = np.asarray(nb)
         out[key + '__rw'] = np.array(wrap_rw(gcalc, target))
+        # get_rw's optional per-point weights (no reference caller passes
+        # them; the function accepts them): seeded weights in [0.2, 2)
+        w = np.random.default_rng(17).uniform(0.2, 2.0, len(target))
+        out[key + '__weight'] = w
+        out[key + '__rw_weighted'] = np.array(get_rw(target, gcalc, weight=w))
         out[key + '__grad_rw'] = wrap_grad_rw(gpdf, gcalc, target)
         out[key + '__chi_sq'] = np.array(wrap_chi_sq(gcalc, target))
         out[key + '__grad_chi_sq'] = wrap_grad_chi_sq(gpdf, gcalc, target)
@@ -222,5 +230,18 @@ def main(ref_root):
           os.path.getsize(path) // 1024, 'KiB')
 
 
+def reference_root(argv):
+    """The pyIID checkout to run: the first argument, else
+    $PYIID_REFERENCE_ROOT; fails with a message when neither names a
+    directory holding the pyiid package."""
+    root = argv[1] if len(argv) > 1 else os.environ.get('PYIID_REFERENCE_ROOT')
+    if not root:
+        sys.exit('usage: make_golden.py REF_ROOT (or set PYIID_REFERENCE_ROOT)'
+                 ' -- the root of a pyIID source checkout')
+    if not os.path.isdir(os.path.join(root, 'pyiid')):
+        sys.exit(f'make_golden.py: {root!r} holds no pyiid/ package')
+    return root
+
+
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    main(reference_root(sys.argv))

@@ -199,3 +199,34 @@ def test_set_processor_contract():
     assert s.set_processor('CPU') is None       # not provided: no CPU fallback
     assert s.set_processor('Multi-GPU') is None
     assert s.processor == 'GB300' and s.alg == 'flat'
+
+
+def test_weighted_rw_matches_reference(golden):
+    """master_kernel.get_rw(gobs, gcalc, weight) on the GPU
+    (pyiid_potential_weighted) against the reference's weighted Rw of the
+    recorded potential cases (kernels/master_kernel.py:206-236), and the
+    oracle with random weights on the same G(r)."""
+    from oracle import debye_np as O
+    from pyiid_gb300.experiments.elasticscatter.kernels import master_kernel
+    keys = sorted({k.rsplit('__', 1)[0] for k in golden.files
+                   if k.startswith('pot') and k.endswith('__rw_weighted')})
+    assert len(keys) == 6
+    for key in keys:
+        s = ES(key.split('__')[-1])
+        atoms = Atoms(numbers=golden[key + '__numbers'],
+                      positions=golden[key + '__positions'])
+        gcalc = s.get_pdf(atoms)
+        target = golden[key + '__target']
+        w = golden[key + '__weight']
+        rw, scale = master_kernel.get_rw(target, gcalc, weight=w)
+        ref = golden[key + '__rw_weighted']
+        assert abs(rw - ref[0]) <= 1e-5 * abs(ref[0]), key
+        assert abs(scale - ref[1]) <= 1e-5 * abs(ref[1]), key
+        # exactly the oracle's weighted value on the same gcalc
+        w2 = np.random.default_rng(3).uniform(0.0, 3.0, len(target))
+        got = master_kernel.get_rw(target, gcalc, weight=w2)
+        want = O.get_rw(target, np.asarray(gcalc, np.float64), w2)
+        assert abs(got[0] - want[0]) <= 1e-12 * max(1.0, abs(want[0])), key
+        # unit weights give the unweighted value
+        assert abs(master_kernel.get_rw(target, gcalc, weight=np.ones_like(w))[0]
+                   - master_kernel.get_rw(target, gcalc)[0]) <= 1e-14

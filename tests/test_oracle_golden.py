@@ -131,6 +131,27 @@ def test_oracle_potentials_match_reference(golden, idx):
     assert rel(gp @ c, golden[key + '__grad_rw']) < 2 * TOL
 
 
+@pytest.mark.parametrize('idx', range(6))
+def test_oracle_weighted_rw_matches_reference(golden, idx):
+    """get_rw(gobs, gcalc, weight) of kernels/master_kernel.py:206-236 with
+    seeded per-point weights, against the reference's own output."""
+    key = pot_keys(golden)[idx]
+    exp = O.update_experiment(EXPS[key.split('__')[-1]])
+    target = golden[key + '__target']
+    pos = golden[key + '__positions']
+    _, pt = O.wrap_atoms_tables(golden[key + '__numbers'], exp, form_factor)
+    qb = O.pdf_qbin(exp)
+    gcalc = O.pdf_fft(O.fq(pos, pt, qb), exp['rstep'], qb, O.r_grid(exp),
+                      exp['qmin'])
+    w = golden[key + '__weight']
+    rw, scale = O.get_rw(target, gcalc, w)
+    ref = golden[key + '__rw_weighted']
+    assert abs(rw - ref[0]) < 1e-5 and abs(scale - ref[1]) < 1e-5 * abs(ref[1])
+    if ref[0] != 1:
+        # the weights change the value (the scale stays unweighted)
+        assert abs(rw - O.get_rw(target, gcalc)[0]) > 1e-4
+
+
 def test_known_answers_of_reference_tests(golden):
     """pyiid/tests/test_master/test_master_kernel.py:19-48."""
     x = np.arange(0, 2 * np.pi, .1)
