@@ -55,15 +55,17 @@ def workload(n_atoms=None):
     return pos, sp, tab, n_bins, k_begin
 
 
-def config_dict(n_bins, k_begin, extra=None, n_atoms=N_ATOMS):
-    d = {'workload': 'single fcc Pt nanoparticle, exact F(Q) + full dF/dx',
-         'n_atoms': n_atoms, 'lattice_a': A_PT, 'sigma': SIGMA,
-         'q_grid': [QMIN, QMAX, QBIN], 'bins_returned': n_bins - k_begin,
-         'pairs': n_atoms * (n_atoms - 1) // 2,
-         'l2': 'flushed between timed steps (256 MiB write)'}
-    if extra:
-        d.update(extra)
-    return d
+def config_dict(n_bins, k_begin, n_atoms=N_ATOMS):
+    """The workload block shared by both arms (identical dicts, so a reader
+    can compare the GPU line with the reference line key by key); what
+    differs between the arms (launch shapes, parallelism, the sampling of
+    the CPU arm) goes in the line's ``arm`` block."""
+    return {'workload': 'single fcc Pt nanoparticle, exact F(Q) + full dF/dx',
+            'n_atoms': n_atoms, 'lattice_a': A_PT, 'sigma': SIGMA,
+            'q_grid': f'{QMIN}-{QMAX} step {QBIN}',
+            'bins_returned': n_bins - k_begin,
+            'pairs': n_atoms * (n_atoms - 1) // 2,
+            'l2': 'flushed between timed steps (256 MiB write)'}
 
 
 def dist_env():
@@ -328,12 +330,11 @@ def run_gpu(args, rank, world, local):
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_step,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'fp32 (FP64 final reductions)', 'data': 'synthetic (seeded fcc Pt)',
-        'config': config_dict(n_bins, k_begin,
-                              {'parallelism': f'replica x{world}',
-                               'launch_shapes': tuned or 'defaults',
-                               'path': ('one pass (pyiid_fq_grad)' if one_pass
-                                        else 'two passes (pyiid_fq, '
-                                             'pyiid_grad_fq)')}, n),
+        'config': config_dict(n_bins, k_begin, n),
+        'arm': {'parallelism': f'replica x{world}',
+                'launch_shapes': tuned or 'defaults',
+                'path': ('one pass (pyiid_fq_grad)' if one_pass
+                         else 'two passes (pyiid_fq, pyiid_grad_fq)')},
         'kernel_ms': kernel_ms,
         'pair_bin_terms_per_s': 2 * pairs * k_ret / (ms_step * 1e-3),
         'wall_s_timed_region': wall,
@@ -463,10 +464,10 @@ def run_gpu_sharded(args, rank, world, local):
         'scaling': 'strong', 'vs_baseline': None,
         'dtype': 'fp32 (FP64 final reductions)',
         'data': 'synthetic (seeded fcc Pt)',
-        'config': config_dict(n_bins, k_begin, {
-            'parallelism': f'one particle split over {world} ranks '
-                           '(tile ranges; all-reduce of the K raw sums)',
-            'path': 'pyiid_fq_grad_part + pyiid_fq_from_sums'}, n),
+        'config': config_dict(n_bins, k_begin, n),
+        'arm': {'parallelism': f'one particle split over {world} ranks '
+                               '(tile ranges; all-reduce of the K raw sums)',
+                'path': 'pyiid_fq_grad_part + pyiid_fq_from_sums'},
         'pair_bin_terms_per_s': 2 * pairs * k_ret / (ms_step * 1e-3),
         'wall_s_timed_region': wall,
         'gpu_launches': int(launches),
@@ -727,7 +728,24 @@ def single_config_au1000(torch, reps=50):
     return {'potential_and_gradient_ms':
                 time_ms(torch, lambda: pot.evaluate(x), reps),
             'fq_ms': time_ms(torch, lambda: debye.fq(x, sp2, tab2, 0.05, 2,
-                                                     out=fo), reps)}
+                                                     out=fo), reps),
+            'fq_noalloc_ms': time_ms(torch, lambda: fq_noalloc(
+                x, sp2, tab2, 0.05, 2, fo), reps)}
+
+
+def fq_noalloc(pos_t, sp, tab, qbin, kb, out):
+    """One pyiid_fq_noalloc call through the C ABI (it synchronizes)."""
+    import ctypes
+    import torch
+    from pyiid_gb300 import _native
+    ctx = _native.context(pos_t.device.index)
+    sp = np.ascontiguousarray(sp, np.int32)
+    tab = np.ascontiguousarray(tab, np.float32)
+    ctx.call('pyiid_fq_noalloc', ctypes.c_void_p(pos_t.data_ptr()),
+             sp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(sp),
+             tab.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), tab.shape[0],
+             tab.shape[1], float(qbin), int(kb), ctypes.c_void_p(out.data_ptr()))
+    return out
 
 
 def measured_hbm_gbs():
@@ -970,7 +988,9 @@ def cpu_sample(target_s=15.0, threads=0, n_atoms=None):
     pairs (F and dF/dx tasks) and extrapolate to all pairs:
       t(eval) = t_fixed + P * (t(2 rounds) - t(1 round)) / (pairs per round)
     where t_fixed (per-thread [n,3,K] buffers and their one final sum) is
-    the 1-round time minus its marginal part; a full evaluation pays it once."""
+    the 1-round time minus its marginal part; a full evaluation pays it once.
+    The returned value is therefore EXTRAPOLATED (``extrapolated`` True,
+    ``pairs_timed`` of ``pairs_per_evaluation``)."""
     from oracle import debye_c
     pos, sp, tab, n_bins, k_begin = workload(n_atoms)
     per_atom = tab[sp]
@@ -992,13 +1012,39 @@ def cpu_sample(target_s=15.0, threads=0, n_atoms=None):
     per_pair = (t2 - t1) / (chunk * nthreads * (rounds - 1))
     fixed = max(0.0, t1 - per_pair * chunk * nthreads)
     t_eval = fixed + per_pair * pairs
+    timed = chunk * nthreads * (rounds + 1)
     return {'value': 1.0 / t_eval, 'unit': 'evals/s', 'cores': int(used),
             'kind': 'port',
-            'sample': (f'{chunk * nthreads * rounds} of {pairs} pairs (all '
-                       f'{n_bins} bins, F and dF/dx tasks of {chunk} pairs), '
-                       f'{t1 + t2:.1f} s; marginal {per_pair * 1e6:.1f} us/pair '
+            'extrapolated': True,
+            'pairs_timed': timed, 'pairs_per_evaluation': pairs,
+            'sample': (f'{timed} of {pairs} pairs (all {n_bins} bins, F and '
+                       f'dF/dx tasks of {chunk} pairs) timed in '
+                       f'{t1 + t2:.1f} s; marginal {per_pair * 1e6:.2f} us/pair '
                        f'+ fixed {fixed:.2f} s, extrapolated to all pairs'),
             'seconds': t1 + t2}
+
+
+def cpu_full_evaluations(sizes=(1000, 2000), threads=0):
+    """Complete evaluations of the FP32 reference-path port (every pair,
+    F(Q) and dF/dx, all bins of the workload's Q grid) on the first N sites
+    of the same particle, timed without extrapolation; each also scaled by
+    pairs to the workload's size for comparison with the sampled estimate."""
+    from oracle import debye_c
+    out = {}
+    for n in sizes:
+        pos, sp, tab, n_bins, k_begin = workload(n)
+        pairs = n * (n - 1) // 2
+        t0 = time.perf_counter()
+        _, _, used = debye_c.port_tasks(pos, tab[sp], QBIN, 2048, pairs, True,
+                                        True, threads)
+        dt = time.perf_counter() - t0
+        full = N_ATOMS * (N_ATOMS - 1) // 2
+        out[f'n{n}'] = {'n_atoms': n, 'pairs': pairs, 'bins': n_bins,
+                        'seconds_per_eval': dt, 'evals_per_s': 1.0 / dt,
+                        'cores': int(used), 'extrapolated': False,
+                        'scaled_by_pairs_to_workload_evals_per_s':
+                            pairs / (dt * full)}
+    return out
 
 
 def run_reference(args, rank, world):
@@ -1016,13 +1062,31 @@ def run_reference(args, rank, world):
     v = float(np.mean([x['value'] for x in vals]))
     base = dict(vals[-1])
     base['value'] = v
+    full = cpu_full_evaluations() if getattr(args, 'full_cpu', True) else {}
+    step_s = float(np.mean([x['seconds'] for x in vals]))
     return {
         'metric': METRIC, 'value': v, 'unit': 'evals/s', 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': 1e3 / v, 'higher_is_better': True, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'fp32 (FP64 sums)',
+        # a step is one bounded sample of the workload's pairs: its measured
+        # wall time; the value is the full evaluation rate extrapolated
+        # from the samples
+        'ms_per_step': 1e3 * step_s, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'fp32 (FP64 sums)',
         'data': 'synthetic (seeded fcc Pt)', 'impl': 'reference',
-        'config': config_dict(n_bins, k_begin, {'parallelism': 'host cores'}),
+        'config': config_dict(n_bins, k_begin),
+        'arm': {'parallelism': 'host cores (OpenMP threads)',
+                'path': 'FP32 loop-for-loop port of the reference numba CPU '
+                        'path (cpu_flat.py + flat_multi_cpu_wrap.py)'},
+        'extrapolated': True,
+        'timed': {'pairs_per_step': int(np.mean([x['pairs_timed']
+                                                 for x in vals])),
+                  'pairs_per_evaluation': base['pairs_per_evaluation'],
+                  'seconds_per_step': step_s,
+                  'note': 'value = full-evaluation rate extrapolated from the '
+                          'timed pairs by the marginal per-pair cost; see '
+                          'measured_full_evaluations for complete, '
+                          'unextrapolated evaluations of smaller particles'},
+        'measured_full_evaluations': full,
         'cpu_baseline': base,
         'e2e': {'value': v, 'unit': 'evals/s', 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},

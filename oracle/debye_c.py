@@ -88,3 +88,70 @@ def port_fq(pos, per_atom_scatter, qbin, chunk=4096, n_threads=0):
     na = np.mean(scat[i] * scat[j], axis=0, dtype=np.float32) * np.float32(n)
     with np.errstate(all='ignore'):
         return 2 * np.nan_to_num(final / na)
+
+
+# ------------------------------------------------- compositions (FP64 chain)
+def fq_all_bins(pos, species, ftab, qbin):
+    """F(Q) [K] from Q = 0: 2 nan_to_num(S / na) with S from the C pair
+    sums on every bin and na = N mean f_a f_b (flat_multi_cpu_wrap.py:44-60)."""
+    from . import debye_np
+    tab = np.asarray(ftab, np.float32)
+    s = pair_sums(pos, species, tab, qbin, np.arange(tab.shape[1]))
+    na = debye_np.normalization(tab[np.asarray(species)])
+    with np.errstate(all='ignore'):
+        return 2 * np.nan_to_num(s / na)
+
+
+def potential_chain(pos, species, ftab, exp, qbin, gobs, kind='rw'):
+    """(value, scale, gcalc, F, T) of one configuration on the PDF grid:
+    F from fq_all_bins, G = F T (the FFT transform as its exact linear map,
+    master_kernel.py:39-203), then get_rw / get_chi_sq
+    (master_kernel.py:206-266)."""
+    from . import debye_np
+    f = fq_all_bins(pos, species, ftab, qbin)
+    T = debye_np.tmatrix(len(f), exp['rstep'], qbin, debye_np.r_grid(exp),
+                         exp['qmin'])
+    gcalc = f @ T
+    gobs = np.asarray(gobs, np.float64)
+    fn = debye_np.get_rw if kind == 'rw' else debye_np.get_chi_sq
+    val, scale = fn(gobs, gcalc)
+    return val, scale, gcalc, f, T
+
+
+def true_grad_rows(pos, species, ftab, exp, qbin, gobs, atoms, kind='rw',
+                   with_chain=False):
+    """Exact d(potential)/dx of the given atoms, [len(atoms), 3] (FP64):
+    sum_k w_k dF_k/dx_a with w = T c, c the adjoint vector of the potential
+    (the derivative get_grad_rw / get_grad_chi_sq contract,
+    master_kernel.py:293-376) and dF = 2 dS / na from oracle_grad_rows."""
+    from . import debye_np
+    val, scale, gcalc, f, T = potential_chain(pos, species, ftab, exp, qbin,
+                                              gobs, kind)
+    c = debye_np.potential_adjoint_vector(np.asarray(gobs, np.float64),
+                                          gcalc, kind)
+    w = T @ c
+    tab = np.asarray(ftab, np.float32)
+    ds = grad_rows(pos, species, tab, qbin, atoms)
+    na = debye_np.normalization(tab[np.asarray(species)])
+    with np.errstate(all='ignore'):
+        df = np.nan_to_num(2 * ds / na)
+    if with_chain:
+        return df @ w, (val, scale, gcalc, f, T)
+    return df @ w
+
+
+def moved_atom_sums(pos, species, ftab, qbin, atom, new_xyz):
+    """S(x') - S(x) in FP64 when ``atom`` moves to ``new_xyz`` (float64,
+    not rounded to float32): the atom's N - 1 pair terms before and after."""
+    x = np.asarray(pos, np.float32).astype(np.float64)
+    tab = np.asarray(ftab, np.float64)
+    sp = np.asarray(species)
+    k = tab.shape[1]
+    q = np.arange(k) * float(qbin)
+    others = np.arange(len(x)) != atom
+    fb = tab[sp[others]] * tab[sp[atom]][None]
+
+    def terms(xa):
+        r = np.linalg.norm(x[others] - xa[None], axis=1)
+        return (fb * np.sin(np.outer(r, q)) / r[:, None]).sum(0)
+    return terms(np.asarray(new_xyz, np.float64)) - terms(x[atom])

@@ -1854,12 +1854,18 @@ extern "C" int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
     for (int a = 0; a < count[s]; a += kTile)
       tiles.push_back(make_int4(start[s] + a, std::min(kTile, count[s] - a), 0, s));
   std::vector<int4> items;
+  // runs of J tiles as get_layout cuts them: shorter than kJMax when that
+  // would leave fewer than about four work items per SM
+  const double n_t = (double)tiles.size();
+  const int jmax = std::max(
+      1, std::min(kJMax, (int)std::floor(n_t * (n_t + 1) / 2 /
+                                         (4.0 * std::max(1, ctx->n_sms)))));
   for (int I = 0; I < (int)tiles.size(); ++I) {
     int J = 0;
     while (J <= I) {
       const int sJ = tiles[J].w;
       int Je = J;
-      while (Je <= I && tiles[Je].w == sJ && Je - J < kJMax) ++Je;
+      while (Je <= I && tiles[Je].w == sJ && Je - J < jmax) ++Je;
       const int sI = tiles[I].w;
       items.push_back(make_int4(I, J, Je, sI * (sI + 1) / 2 + sJ));
       J = Je;

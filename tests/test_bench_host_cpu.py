@@ -62,9 +62,10 @@ def test_workload_and_config_block():
     assert pos.shape == (2000, 3) and pos.dtype == np.float32
     assert n_bins == 1500 and k_begin == 25          # Q 0.5-30 step 0.02
     assert sp.shape == (2000,) and tab.shape == (1, 1500)
-    c = bench.config_dict(1500, 25, {'path': 'x'})
+    c = bench.config_dict(1500, 25)
     assert c['n_atoms'] == 20000 and c['bins_returned'] == 1475
-    assert c['pairs'] == 20000 * 19999 // 2 and c['path'] == 'x'
+    assert c['pairs'] == 20000 * 19999 // 2
+    assert c == bench.config_dict(1500, 25, 20000)
     assert 'flushed' in c['l2']
     assert bench.measured_hbm_gbs() is None or bench.measured_hbm_gbs() > 1000
 
@@ -75,6 +76,15 @@ def test_cpu_sample_reports_a_bounded_port_measurement():
     assert out['kind'] == 'port' and out['unit'] == 'evals/s'
     assert out['cores'] == 2 and out['value'] > 0
     assert 'of 44850 pairs' in out['sample'] and out['seconds'] > 0
+    assert out['extrapolated'] is True and out['pairs_per_evaluation'] == 44850
+
+
+def test_full_cpu_evaluations_are_measured_not_scaled():
+    import bench
+    out = bench.cpu_full_evaluations(sizes=(120,), threads=2)['n120']
+    assert out['extrapolated'] is False and out['pairs'] == 120 * 119 // 2
+    assert out['seconds_per_eval'] > 0 and out['cores'] == 2
+    assert out['scaled_by_pairs_to_workload_evals_per_s'] < out['evals_per_s']
 
 
 def test_reference_arm_line_follows_the_contract(monkeypatch):
@@ -87,8 +97,12 @@ def test_reference_arm_line_follows_the_contract(monkeypatch):
 
     def fake_sample(target_s=15.0, threads=0, n_atoms=None):
         return {'value': next(samples), 'unit': 'evals/s', 'cores': 8,
-                'kind': 'port', 'sample': 'stub', 'seconds': 1.0}
+                'kind': 'port', 'sample': 'stub', 'seconds': 1.0,
+                'extrapolated': True, 'pairs_timed': 1000,
+                'pairs_per_evaluation': 199990000}
     monkeypatch.setattr(bench, 'cpu_sample', fake_sample)
+    monkeypatch.setattr(bench, 'cpu_full_evaluations',
+                        lambda: {'n1000': {'extrapolated': False}})
     args = types.SimpleNamespace(steps=2, warmup=0)
     assert bench.run_reference(args, 1, 2) is None
     line = bench.run_reference(args, 0, 1)
@@ -100,3 +114,10 @@ def test_reference_arm_line_follows_the_contract(monkeypatch):
     assert line['e2e'] == {'value': line['value'], 'unit': 'evals/s',
                            'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
     assert line['config']['bins_returned'] == 1475
+    # the reader sees what was timed and what was scaled
+    assert line['extrapolated'] is True
+    assert line['timed']['pairs_per_step'] == 1000
+    assert line['ms_per_step'] == 1000.0
+    assert line['measured_full_evaluations']['n1000']['extrapolated'] is False
+    # both arms share one config block
+    assert line['config'] == bench.config_dict(1500, 25)

@@ -88,3 +88,37 @@ def test_port_task_split_does_not_change_the_sums(chunk):
     s_ref, _, _ = C.port_tasks(pos, per_atom, 0.1, 435, 435, True, False)
     s, _, _ = C.port_tasks(pos, per_atom, 0.1, chunk, 435, True, False)
     assert np.abs(s - s_ref).max() <= 1e-12 * np.abs(s_ref).max()
+
+
+@pytest.mark.parametrize('exp_name', ['default', 'short'])
+def test_fp64_chain_compositions_match_the_numpy_oracle(exp_name):
+    """The compositions the large-size GPU tests use (C pair sums -> F ->
+    G -> potential, gradient rows through the adjoint vector, one moved
+    atom's sum change) equal the NumPy oracle's full chain on a 50-atom
+    alloy."""
+    from oracle import mh_np
+    exp = O.update_experiment(EXPS[exp_name])
+    qb = O.pdf_qbin(exp)
+    nb = int(np.floor(exp['qmax'] / qb))
+    ref = S.fcc_nearest(4.08, 50)
+    pos = S.displaced(ref, 0.05, 9)
+    nums = list(np.random.default_rng(9).choice([78, 79], 50))
+    sp, tab, _ = species_tables(nums, qb, nb)
+    rg = O.r_grid(exp)
+    gobs = O.pdf_tmatrix(O.fq(ref, tab[sp], qb), exp['rstep'], qb, rg,
+                         exp['qmin'])
+    f = C.fq_all_bins(pos, sp, tab, qb)
+    assert rel(f, O.fq(pos, tab[sp], qb)) < 1e-12
+    for kind in ('rw', 'chi_sq'):
+        val, scale, gcalc, _, _ = C.potential_chain(pos, sp, tab, exp, qb,
+                                                    gobs, kind)
+        assert abs(val - O.potential_value(pos, tab[sp], exp, gobs, kind)) \
+            <= 1e-12 * abs(val)
+        atoms = np.array([0, 13, 49], np.int32)
+        rows = C.true_grad_rows(pos, sp, tab, exp, qb, gobs, atoms, kind)
+        _, tg = O.true_grad_potential(pos, tab[sp], exp, gobs, kind)
+        assert rel(rows, tg[atoms]) < 1e-10
+    new = pos[13].astype(np.float64) + np.array([1e-3, -2e-3, 5e-4])
+    ds = C.moved_atom_sums(pos, sp, tab, qb, 13, new)
+    want = mh_np.exact_delta_s(pos, sp, tab.astype(np.float64), qb, 13, new)
+    assert np.abs(ds - want).max() <= 1e-9 * np.abs(want).max()

@@ -43,6 +43,10 @@ def test_noalloc_matches_fq_two_calls_in_a_row():
         (structures.random_cube(150, 12.0, 4),
          list(np.random.default_rng(4).choice([78, 79], 150)), 0.0756865, 330,
          7),
+        # one 1,000-atom particle: its 32 tiles are cut into short J runs
+        # (one tile pair per work item) so that the launch fills the GPU
+        (structures.displaced(structures.fcc_nearest(4.08, 1000), 0.05, 4),
+         None, 0.05, 500, 2),
     ]
     for pos, nums, qbin, nb, kb in cases:
         nums = nums if nums is not None else [79] * len(pos)
