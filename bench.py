@@ -366,6 +366,15 @@ def run_gpu(args, rank, world, local):
             'achieved': gbs, 'peak': hbm, 'unit': 'GB/s', 'frac': gbs / hbm,
             'peak_source': 'MEASURED_PEAKS.json hbm_gbs (measured copy)'}
     if workloads:
+        hmc, nuts = (workloads.get('hmc_64_chains_au1000'),
+                     workloads.get('nuts_64_chains_au1000'))
+        try:
+            hmc_lf = hmc['hmc_iterations_per_s'] * 64 * 10
+            nuts['batched']['hmc_leapfrog_steps_per_s'] = hmc_lf
+            nuts['batched']['over_hmc_leapfrog_rate'] = (
+                nuts['batched']['leapfrog_steps_per_s'] / hmc_lf)
+        except (KeyError, TypeError):
+            pass
         line['workloads'] = workloads
     return line
 
@@ -1143,15 +1152,18 @@ def run_nuts(torch, iters=2):
 
 
 def _run_nuts(torch, iters):
-    """NUTS (the reference's algorithm) on 64 chains of the 1,000-atom Au
-    particle (300 K, E = 100 Rw, escape depth 6): all chains batched into
-    one exact evaluation per tree leaf, against one chain of the sequential
-    NUTSCanonicalEnsemble (the reference's per-chain loop) on the same GPU."""
+    """NUTS on 64 chains of the 1,000-atom Au particle (300 K, E = 100 Rw,
+    escape depth 6): the tree of every chain grown on the device in lock
+    step, one batched exact evaluation per leapfrog step of all chains
+    (pyiid_gb300.nuts.BatchedNUTS; the Debye potential is translation
+    invariant, so the re-centred end point is not re-evaluated), against
+    one chain of the sequential NUTSCanonicalEnsemble (the drop-in sampler
+    on a Calc1D) on the same GPU."""
     from pyiid_gb300.atoms import Atoms
     from pyiid_gb300.calc.calc_1d import Calc1D
     from pyiid_gb300.experiments.elasticscatter import ElasticScatter
     from pyiid_gb300.experiments.elasticscatter.gb300_wrap import species_of
-    from pyiid_gb300.nuts_batched import BatchedNUTS
+    from pyiid_gb300.nuts import BatchedNUTS
     from pyiid_gb300.sampling import PDFPotential
     from pyiid_gb300.sim.nuts_hmc import NUTSCanonicalEnsemble
     from pyiid_gb300 import structures
@@ -1173,16 +1185,27 @@ def _run_nuts(torch, iters):
                        'E = 100 Rw, escape depth 6'}
     t = time.perf_counter()
     bn = BatchedNUTS(pot, starts, temperature=300, seeds=range(64),
-                     escape_level=6)
-    ev0 = bn.evaluations
+                     escape_level=6, exact=False)
+    bn.step(1)  # warm-up iteration
+    torch.cuda.synchronize()
+    e = bn.engine
+    lf0, ev0, acc0 = int(e.leapfrogs.sum()), e.evaluations, int(
+        e.accepted.sum())
     t1 = time.perf_counter()
-    bn.step(iters)
+    ticks = bn.step(iters)
+    torch.cuda.synchronize()
     dt = time.perf_counter() - t1
-    leaves = sum(ch.metadata['samples_total'] for ch in bn.chains)
+    leaves = int(e.leapfrogs.sum()) - lf0
     out['batched'] = {'chain_iterations_per_s': 64 * iters / dt,
                       'leapfrog_steps_per_s': leaves / dt,
-                      'batched_evaluations': bn.evaluations - ev0,
-                      'setup_s': t1 - t}
+                      'accepted_samples_per_s':
+                          (int(e.accepted.sum()) - acc0) / dt,
+                      'ticks': ticks, 'ms_per_tick': 1e3 * dt / max(ticks, 1),
+                      'chain_utilisation': leaves / max(64 * ticks, 1),
+                      'batched_evaluations': e.evaluations - ev0,
+                      'setup_s': t1 - t,
+                      'tree': 'on the device (lock step, masks), '
+                              'no per-leaf host exchange'}
     atoms = Atoms(numbers=[79] * 1000, positions=starts[0])
     atoms.set_calculator(Calc1D(target_data=target, exp_function=s.get_pdf,
                                 exp_grad_function=s.get_grad_pdf, conv=100.))
@@ -1193,7 +1216,7 @@ def _run_nuts(torch, iters):
     dt = time.perf_counter() - t1
     out['sequential_one_chain'] = {
         'chain_iterations_per_s': 1 / dt,
-        'leapfrog_steps_per_s': ens.metadata['samples_total'] / dt}
+        'leapfrog_steps_per_s': ens.metadata['leapfrog_steps'] / dt}
     return out
 
 

@@ -58,8 +58,8 @@ def get_rw(gobs, gcalc, weight=None):
     ``weight`` weighs the residual and the normalisation point by point; the
     scale is the unweighted one, as in the reference."""
     if weight is not None:
-        weight = np.broadcast_to(np.asarray(weight, dtype=np.float64),
-                                 np.shape(gcalc))
+        weight = np.array(np.broadcast_to(np.asarray(weight, np.float64),
+                                          np.shape(gcalc)))
     v, s = _pot(gobs, gcalc, 'rw', weight)
     if s == 1.0 and v == 1.0:
         return 1, 1

@@ -1,61 +1,29 @@
-"""No-U-Turn sampler with dual-averaging step size (pyiid/sim/nuts_hmc.py).
+"""No-U-Turn sampler over ASE-style Atoms (the reference's
+``pyiid.sim.nuts_hmc.NUTSCanonicalEnsemble``, pyiid/sim/nuts_hmc.py:91-232).
 
-Same algorithm and conventions as the reference: slice variable in
-post-exponential units (u in [0, 1] compared with exp(E0 - E)), the tree
-built by recursive doubling with leapfrog steps, the U-turn criterion on the
-span between the outermost states, the Emax = 200 slack, the emergency
-escape depth, and the dual-averaging update of the step size
-(nuts_hmc.py:160-232).  The temperature enters through the Maxwell-Boltzmann
-momenta only, as in the reference (``beta`` is accepted but unused,
-nuts_hmc.py:15-60).
+One chain of :class:`pyiid_gb300.nuts.NUTSEngine` (Hoffman and Gelman's
+efficient NUTS with dual averaging, grown leaf by leaf with keyed random
+draws) driven by the calculator attached to the atoms: energies and forces
+come from ``get_potential_energy`` / ``get_forces`` at every leapfrog point
+and at the re-centred end point, as an ASE calculator recomputes them
+when positions change.  The constructor arguments, ``step``/``run``, the
+trajectory of accepted configurations, ``pe``, the observers and the
+metadata counters keep the reference's meaning; the engine's module
+docstring lists the conventions kept (post-exponential slice variable,
+Emax = 200, escape depth, Maxwell-Boltzmann momenta, dual-averaging
+constants).  A BatchedNUTS chain with the same seed and potential makes the
+same decisions (the random draws are keyed by iteration and tree slot).
 """
 from copy import deepcopy as dc
 from time import time
 
 import numpy as np
+import torch
 
-from ..atoms import MaxwellBoltzmannDistribution, fs, kB
-from . import Ensemble, leapfrog
+from ..nuts import NUTSEngine, Emax
+from . import Ensemble
 
-__all__ = ['buildtree', 'NUTSCanonicalEnsemble', 'Emax']
-
-Emax = 200
-
-
-def buildtree(input_atoms, u, v, j, e, e0, rs, beta=1):
-    """One subtree of depth j in direction v (nuts_hmc.py:15-88).  Returns
-    (minus, plus, proposal, n, s, alpha_sum, n_alpha)."""
-    if j == 0:
-        atoms_prime = leapfrog(input_atoms, v * e)
-        neg_delta_energy = e0 - atoms_prime.get_total_energy()
-        with np.errstate(over='ignore'):
-            exp1 = np.exp(neg_delta_energy)
-            exp2 = np.exp(Emax + neg_delta_energy)
-        n_prime = int(u <= exp1)
-        s_prime = int(u < exp2)
-        with np.errstate(over='ignore'):
-            a = min(1, np.exp(-atoms_prime.get_total_energy() +
-                              input_atoms.get_total_energy()))
-        return atoms_prime, atoms_prime, atoms_prime, n_prime, s_prime, a, 1
-    (neg_atoms, pos_atoms, atoms_prime, n_prime, s_prime, a_prime,
-     na_prime) = buildtree(input_atoms, u, v, j - 1, e, e0, rs, beta)
-    if s_prime == 1:
-        if v == -1:
-            (neg_atoms, _, atoms_pp, n_pp, s_pp, app, napp) = buildtree(
-                neg_atoms, u, v, j - 1, e, e0, rs, beta)
-        else:
-            (_, pos_atoms, atoms_pp, n_pp, s_pp, app, napp) = buildtree(
-                pos_atoms, u, v, j - 1, e, e0, rs, beta)
-        if rs.uniform() < float(n_pp / (max(n_prime + n_pp, 1))):
-            atoms_prime = atoms_pp
-        a_prime = a_prime + app
-        na_prime = na_prime + napp
-        span = (pos_atoms.positions - neg_atoms.positions).flatten()
-        s_prime = s_pp * (span.dot(neg_atoms.get_velocities().flatten()) >= 0
-                          ) * (span.dot(pos_atoms.get_velocities().flatten()) >= 0)
-        n_prime = n_prime + n_pp
-    return (neg_atoms, pos_atoms, atoms_prime, n_prime, s_prime, a_prime,
-            na_prime)
+__all__ = ['NUTSCanonicalEnsemble', 'Emax']
 
 
 class NUTSCanonicalEnsemble(Ensemble):
@@ -68,98 +36,62 @@ class NUTSCanonicalEnsemble(Ensemble):
                           verbose)
         self.accept_target = accept_target
         self.temp = temperature
-        self.thermal_nrg = self.temp * kB
-        self.momentum = momentum
-        self.step_size = self._find_step_size(atoms, self.thermal_nrg)
-        self.mu = np.log(10 * self.step_size)
-        self.sim_hbar = 0
-        self.gamma = 0.05
-        self.t0 = 10
-        self.metadata.update({'samples_total': 0, 'accepted_samples': 0})
         self.escape_level = escape_level
-        self.m = 0
+        self.momentum = momentum
+        self._work = dc(atoms)
+        self._work.set_calculator(atoms.get_calculator())
+        x0 = np.asarray(atoms.get_positions(), np.float64)[None]
+        self._engine = NUTSEngine(
+            self._evaluate, x0, atoms.get_masses(), temperature,
+            [self.metadata['seed']], escape_level=escape_level,
+            accept_target=accept_target, momentum=momentum,
+            reevaluate_centred=True, dtype=torch.float64, device='cpu')
+        self.metadata.update({'samples_total': 0, 'accepted_samples': 0})
+        if verbose:
+            print('initial step size', self.step_size)
 
-    def _mb(self, atoms, thermal_nrg):
-        MaxwellBoltzmannDistribution(atoms, thermal_nrg, force_temp=True,
-                                     rng=self.random_state)
+    def _evaluate(self, x):
+        a = self._work
+        a.set_positions(x[0].numpy())
+        u = float(a.get_potential_energy())
+        f = np.asarray(a.get_forces(), np.float64)
+        return (torch.tensor([u], dtype=torch.float64),
+                torch.as_tensor(f)[None])
 
-    def _find_step_size(self, input_atoms, thermal_nrg=None, momentum=None):
-        """Doubling / halving search for a reasonable first step size
-        (nuts_hmc.py:116-158)."""
-        atoms = dc(input_atoms)
-        step_size = .5
-        if thermal_nrg:
-            self._mb(atoms, thermal_nrg)
-        elif momentum:
-            atoms.set_momenta(self.random_state.normal(0, 1, (len(atoms), 3)))
-        atoms_prime = leapfrog(atoms, step_size)
-        with np.errstate(over='ignore'):
-            # a = +1 (grow) or -1 (shrink), kept a Python float so that the
-            # threshold 2^-a is well defined for both signs
-            a = 1.0 if np.exp(-1 * atoms_prime.get_total_energy() +
-                              atoms.get_total_energy()) > 0.5 else -1.0
-            while (np.exp(-1 * atoms_prime.get_total_energy() +
-                          atoms.get_total_energy())) ** a > 2.0 ** -a:
-                step_size *= 2 ** a
-                if self.verbose:
-                    print('trying step size', step_size)
-                atoms_prime = leapfrog(atoms, step_size)
-                if step_size < 1e-7 or step_size > 1e7:
-                    step_size = 1.
-                    break
-        return step_size
+    @property
+    def step_size(self):
+        return float(self._engine.step[0])
+
+    @property
+    def mu(self):
+        return float(self._engine.mu[0])
 
     def step(self):
-        new_configurations = []
+        """One NUTS iteration; returns the configurations it accepted (or
+        None), each appended to the trajectory with observers called."""
+        e = self._engine
+        n0 = len(e.samples[0])
+        e.run(1)
+        new = []
+        for x in e.samples[0][n0:]:
+            a = dc(self.traj[-1])
+            a.set_calculator(self._work.get_calculator())
+            a.set_positions(x.numpy())
+            self.traj.append(a)
+            new.append(a)
+            a.get_forces()
+            self.pe.append(a.get_potential_energy())
+            self.call_observers()
+        self.metadata['accepted_samples'] = int(e.accepted[0])
+        self.metadata['samples_total'] = int(e.samples_total[0])
+        self.metadata['leapfrog_steps'] = int(e.leapfrogs[0])
         if self.verbose:
-            print('\ttime step size', self.step_size / fs, 'fs')
-        if self.momentum is None:
-            self._mb(self.traj[-1], self.thermal_nrg)
-        else:
-            self.traj[-1].set_momenta(self.random_state.normal(
-                0, 1, (len(self.traj[-1]), 3)))
-        u = self.random_state.uniform(0, 1)
-        e0 = self.traj[-1].get_total_energy()
-        e = self.step_size
-        n, s, j = 1, 1, 0
-        neg_atoms = dc(self.traj[-1])
-        pos_atoms = dc(self.traj[-1])
-        a, na = 0.0, 1
-        while s == 1:
-            v = self.random_state.choice([-1, 1])
-            if v == -1:
-                (neg_atoms, _, atoms_prime, n_prime, s_prime, a, na) = \
-                    buildtree(neg_atoms, u, v, j, e, e0, self.random_state,
-                              1 / self.thermal_nrg)
-            else:
-                (_, pos_atoms, atoms_prime, n_prime, s_prime, a, na) = \
-                    buildtree(pos_atoms, u, v, j, e, e0, self.random_state,
-                              1 / self.thermal_nrg)
-            if s_prime == 1 and self.random_state.uniform() < min(
-                    1, n_prime * 1. / n):
-                self.traj += [atoms_prime]
-                self.metadata['accepted_samples'] += 1
-                new_configurations.append(atoms_prime)
-                atoms_prime.get_forces()
-                self.pe.append(atoms_prime.get_potential_energy())
-                self.call_observers()
-            n = n + n_prime
-            span = (pos_atoms.positions - neg_atoms.positions).flatten()
-            s = s_prime * (span.dot(neg_atoms.get_velocities().flatten()) >= 0
-                           ) * (span.dot(pos_atoms.get_velocities().flatten()) >= 0)
-            j += 1
-            self.metadata['samples_total'] += 2 ** j
-            if j >= self.escape_level:
-                s = 0
-        w = 1. / (self.m + self.t0)
-        self.sim_hbar = (1 - w) * self.sim_hbar + w * (self.accept_target -
-                                                       a / na)
-        self.step_size = np.exp(self.mu - (self.m ** .5 / self.gamma) *
-                                self.sim_hbar)
-        self.m += 1
-        return new_configurations or None
+            print('\tstep size', self.step_size, 'accepted', len(new))
+        return new or None
 
     def estimate_simulation_duration(self, atoms, iterations):
+        """Upper bound of the run time: every iteration at the escape depth
+        (2^escape_level leapfrog steps of two force calls each)."""
         t0 = time()
         atoms.get_forces()
         tf = time() - t0

@@ -245,7 +245,7 @@ def test_single_atom_mh_at_1000_atoms_every_proposal(au1000):
     # the energy changes the decisions rest on, in units of kT
     print(f'1,000-atom MH: {n_acc}/{n_steps} accepted, max energy-change '
           f'error {conv * dv_err / mc.kT:.2e} kT')
-    assert conv * dv_err / mc.kT <= 1e-2, conv * dv_err / mc.kT
+    assert conv * dv_err / mc.kT <= 1e-3, conv * dv_err / mc.kT
     assert np.array_equal(mc.positions().cpu().numpy(), x)
     e = float(mc.state['energy'][0, 0].item())
     assert abs(e - v) <= TOL_F * abs(v)

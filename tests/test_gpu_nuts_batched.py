@@ -1,6 +1,8 @@
-"""Batched NUTS: every chain of a BatchedNUTS batch reproduces a sequential
-NUTSCanonicalEnsemble run (the reference's algorithm, pyiid/sim/nuts_hmc.py)
-with the same seed and the same potential, sample for sample."""
+"""Batched NUTS on the GPU: every chain of a BatchedNUTS batch (the tree
+grown on the device for all chains in lock step) reproduces a sequential
+NUTSCanonicalEnsemble run on a Calc1D of the same potential (pyiid/sim/
+nuts_hmc.py's sampler through the drop-in calculator) with the same seed,
+sample for sample."""
 import numpy as np
 import pytest
 
@@ -33,7 +35,7 @@ def setup(n=22, chains=3):
 
 def test_batched_chains_reproduce_sequential_nuts():
     from pyiid_gb300.atoms import Atoms
-    from pyiid_gb300.nuts_batched import BatchedNUTS
+    from pyiid_gb300.nuts import BatchedNUTS
     from pyiid_gb300.sampling import PDFPotential
     from pyiid_gb300.sim.nuts_hmc import NUTSCanonicalEnsemble
     s, target, starts, tab, calc = setup()
@@ -63,7 +65,7 @@ def test_batched_chains_reproduce_sequential_nuts():
 
 
 def test_single_evaluation_mode_runs_and_samples():
-    from pyiid_gb300.nuts_batched import BatchedNUTS
+    from pyiid_gb300.nuts import BatchedNUTS
     from pyiid_gb300.sampling import PDFPotential
     s, target, starts, tab, calc = setup(chains=4)
     pot = PDFPotential([79] * len(starts[0]), target, dict(EXP), conv=50.,

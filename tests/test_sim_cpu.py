@@ -209,21 +209,61 @@ def test_spring_forces_are_minus_the_gradient():
                    + f[i, c]) < 1e-6
 
 
-def test_batched_nuts_scheduler_reproduces_sequential_chains():
-    """pyiid_gb300.nuts_batched drives every chain's reference NUTS as a
-    generator and evaluates the pending leapfrog end points of all chains
-    together; with the device evaluation replaced by the same Python
-    potential, chain c equals a sequential NUTSCanonicalEnsemble run with
-    seed c sample for sample."""
-    from pyiid_gb300.nuts_batched import BatchedNUTS
+def _spring_batch(x):
+    """(U [B], F [B, N, 3]) of _springs for a torch batch of positions."""
+    import torch
+    out = [_springs(xi.numpy()) for xi in x]
+    return (torch.tensor([e for e, _ in out], dtype=torch.float64),
+            torch.as_tensor(np.stack([f for _, f in out])))
 
+
+def _spring_starts(n_chains):
     base = np.array([[0, 0, 0], [2.8, 0, 0], [0, 2.8, 0], [0, 0, 2.8],
                      [2.0, 2.0, 2.0]], float)
     rng = np.random.default_rng(4)
-    starts = [base + rng.normal(scale=0.1, size=base.shape) for _ in range(3)]
-    seeds = [5, 6, 7]
-    n_steps = 6  # the first iterations adapt the step size; later ones accept
+    return [base + rng.normal(scale=0.1, size=base.shape)
+            for _ in range(n_chains)]
 
+
+def test_nuts_engine_grows_the_tree_as_the_recursive_algorithm():
+    """The engine's leaf-by-leaf tree (one batch of chains, lock step, under
+    masks) against an independent recursive NUTS (oracle/nuts_np.py,
+    Hoffman and Gelman's BuildTree) reading the same keyed random tables:
+    every chain's samples, acceptance count, leapfrog count and adapted
+    step size agree."""
+    import torch
+    from oracle.nuts_np import RecursiveNUTS
+    from pyiid_gb300.nuts import NUTSEngine
+    starts = _spring_starts(4)
+    seeds = [5, 6, 7, 8]
+    masses = Atoms('Au5').get_masses()
+    iters = 7
+    eng = NUTSEngine(_spring_batch, np.stack(starts), masses, 300.0, seeds,
+                     escape_level=5, device='cpu')
+    eng.run(iters)
+    for c, (x0, seed) in enumerate(zip(starts, seeds)):
+        ref = RecursiveNUTS(_springs, x0, masses, 300.0, seed, 5)
+        # the first-step searches agree
+        assert abs(float(eng.mu[c]) - ref.mu) <= 1e-12 * abs(ref.mu)
+        for _ in range(iters):
+            ref.iterate()
+        assert int(eng.accepted[c]) == ref.accepted > 0
+        assert int(eng.leapfrogs[c]) == ref.leapfrogs
+        assert len(eng.samples[c]) == len(ref.samples)
+        for a, b in zip(eng.samples[c], ref.samples):
+            assert np.allclose(a.numpy(), b, rtol=0, atol=1e-12)
+        assert abs(float(eng.step[c]) - ref.eps) <= 1e-12 * ref.eps
+
+
+def test_sequential_nuts_equals_a_chain_of_a_batch():
+    """The drop-in NUTSCanonicalEnsemble (one chain, the attached
+    calculator) and chain c of a batched engine with seed c make the same
+    decisions sample for sample; the batch evaluates all chains together
+    (one evaluation per tick, twice with the re-centred point)."""
+    from pyiid_gb300.nuts import NUTSEngine
+    starts = _spring_starts(3)
+    seeds = [5, 6, 7]
+    n_steps = 6
     seq = []
     for x0, seed in zip(starts, seeds):
         a = Atoms('Au5', x0)
@@ -232,33 +272,20 @@ def test_batched_nuts_scheduler_reproduces_sequential_chains():
                                     seed=seed)
         traj, meta = ens.run(n_steps)
         seq.append((traj, meta, ens.step_size))
-
-    class _Pot:
-        n_configs = 3
-        offsets = np.array([0, 5, 10, 15])
-        masses = Atoms('Au5').get_masses()
-
-    class _CpuNUTS(BatchedNUTS):
-        def _evaluate(self, xs):
-            self.evaluations += 1
-            out = [_springs(np.asarray(x, float)) for x in xs]
-            return (np.array([e for e, _ in out]),
-                    np.stack([f for _, f in out]))
-
-    b = _CpuNUTS(_Pot(), np.stack(starts), temperature=300, seeds=seeds,
-                 escape_level=5)
-    b.step(n_steps)
+    eng = NUTSEngine(_spring_batch, np.stack(starts),
+                     Atoms('Au5').get_masses(), 300.0, seeds,
+                     escape_level=5, device='cpu')
+    eng.run(n_steps)
     for c, (traj, meta, step) in enumerate(seq):
-        ch = b.chains[c]
         assert meta['accepted_samples'] > 0
-        assert ch.metadata['accepted_samples'] == meta['accepted_samples']
-        assert len(ch.samples) == len(traj) - 1
-        for x, t in zip(ch.samples, traj[1:]):
-            assert np.allclose(x, t.positions, rtol=0, atol=1e-9)
-        assert abs(ch.step_size - step) <= 1e-12 * step
-    # one batched evaluation per tree leaf of the deepest chain (twice with
-    # the centred re-evaluation), not one per leaf per chain
-    assert b.evaluations < sum(m['samples_total'] for _, m, _ in seq)
+        assert int(eng.accepted[c]) == meta['accepted_samples']
+        assert int(eng.samples_total[c]) == meta['samples_total']
+        assert len(eng.samples[c]) == len(traj) - 1
+        for x, t in zip(eng.samples[c], traj[1:]):
+            assert np.allclose(x.numpy(), t.positions, rtol=0, atol=1e-9)
+        assert abs(float(eng.step[c]) - step) <= 1e-12 * step
+    total = sum(int(v) for v in eng.leapfrogs)
+    assert eng.evaluations < 2 * total + 64
 
 
 class _Voxelled(_Well):
