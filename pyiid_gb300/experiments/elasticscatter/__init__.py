@@ -113,20 +113,12 @@ class ElasticScatter(object):
         atoms.info['scatter_atoms'] = n
 
     def _check_wrap_atoms_state(self, atoms):
-        t_value = True
-        if self.wrap_atoms_state is None:
-            t_value = False
-        elif 'F(Q) scatter' not in atoms.arrays.keys():
-            t_value = False
-        elif atoms.info['exp'] != self.exp or atoms.info[
-                'scatter_atoms'] != len(atoms):
-            t_value = False
-        if not t_value:
-            if self.verbose:
-                print('calculating new scatter factors')
-            self._wrap_atoms(atoms)
-            self.wrap_atoms_state = atoms
-        return t_value
+        """Refresh the atoms' scatter tables when they are stale; returns
+        whether they were current (__init__.py:153-178)."""
+        current = self.check_wrap_atoms_state(atoms)
+        if not current:
+            self._ensure(atoms, known_stale=True)
+        return current
 
     def update_experiment(self, exp_dict):
         """__init__.py:180-204."""
@@ -161,55 +153,64 @@ class ElasticScatter(object):
         return None
 
     def check_wrap_atoms_state(self, atoms):
-        if self.wrap_atoms_state is None:
-            return False
-        if 'F(Q) scatter' not in atoms.arrays.keys():
-            return False
-        if atoms.info['exp'] != self.exp or \
-                atoms.info['scatter_atoms'] != len(atoms):
-            return False
-        return True
+        """True when the atoms carry scatter tables made for this experiment
+        and this number of atoms (__init__.py:294-302)."""
+        info = atoms.info
+        return bool(self.wrap_atoms_state is not None
+                    and 'F(Q) scatter' in atoms.arrays
+                    and info.get('exp') == self.exp
+                    and info.get('scatter_atoms') == len(atoms))
 
-    def _ensure(self, atoms):
-        if self.check_wrap_atoms_state(atoms) is False:
+    def _ensure(self, atoms, known_stale=False):
+        if known_stale or not self.check_wrap_atoms_state(atoms):
             if self.verbose:
                 print('calculating new scatter factors')
             self._wrap_atoms(atoms)
             self.wrap_atoms_state = atoms
 
+    def _noisy(self, fq, iq_std, q, f_sq):
+        """F(Q) plus Gaussian noise propagated from an I(Q) standard
+        deviation: sigma_F = iq_std |Q| / |f^2| (__init__.py:332-341,
+        :376-383), with a 1e-9 floor on a zero first point; one
+        ``self.rs.normal`` draw of the whole vector."""
+        sigma = iq_std * np.abs(q) / np.abs(f_sq)
+        if sigma[0] == 0.0:
+            sigma[0] = sigma[0] + 1e-9
+        return fq + self.rs.normal(0, sigma)
+
     # ------------------------------------------------------------ getters
     def get_fq(self, atoms, iq_std=None, noise_distribution=None):
-        """Reduced structure factor F(Q) (__init__.py:304-341)."""
+        """Reduced structure factor F(Q) (__init__.py:304-341): bins from
+        qmin up; with ``iq_std`` the I(Q) noise carried through
+        (avg f)^2."""
         self._ensure(atoms)
-        fq = self.fq(atoms, self.exp['qbin'])
-        fq = fq[int(np.floor(self.exp['qmin'] / self.exp['qbin'])):]
-        if iq_std is not None:
-            fq_std = iq_std * np.abs(self.get_scatter_vector()) / np.abs(
-                np.average(atoms.get_array('F(Q) scatter'), axis=0) ** 2)[int(
-                    np.floor(self.exp['qmin'] / self.exp['qbin'])):]
-            if fq_std[0] == 0.0:
-                fq_std[0] += 1e-9
-            fq += self.rs.normal(0, fq_std)
-        return fq
+        k0 = int(np.floor(self.exp['qmin'] / self.exp['qbin']))
+        fq = self.fq(atoms, self.exp['qbin'])[k0:]
+        if iq_std is None:
+            return fq
+        f_avg = np.average(atoms.get_array('F(Q) scatter'), axis=0)
+        return self._noisy(fq, iq_std, self.get_scatter_vector(),
+                           (f_avg ** 2)[k0:])
 
     def get_pdf(self, atoms, iq_std=None, noise_distribution=np.random.normal):
-        """Pair distribution function G(r) (__init__.py:343-391)."""
+        """Pair distribution function G(r) (__init__.py:343-391); with
+        ``iq_std`` the I(Q) noise carried through avg(f^2) on the PDF grid.
+        An ``iq_std`` array of another length is resampled linearly by
+        index onto the grid's points (NaN beyond its last point); the
+        reference's resampling line raises on current numpy."""
         self._ensure(atoms)
         fq = self.fq(atoms, self.pdf_qbin, 'PDF')
         if iq_std is not None:
-            from scipy.interpolate import griddata
-            a = np.abs(self.get_scatter_vector(pdf=True))
-            b = np.abs(np.average(atoms.get_array('PDF scatter') ** 2, axis=0))
-            if hasattr(iq_std, 'shape') and iq_std.shape != a.shape:
-                iq_std = griddata(np.arange(0, iq_std.shape), iq_std,
-                                  np.arange(a.shape))
-            fq_noise = iq_std * a / b
-            if fq_noise[0] == 0.0:
-                fq_noise[0] += 1e-9
-            fq += self.rs.normal(0, fq_noise)
-        r = self.get_r()
-        return get_pdf_at_qmin(fq, self.exp['rstep'], self.pdf_qbin, r,
-                               self.exp['qmin'])
+            q = self.get_scatter_vector(pdf=True)
+            f_sq = np.average(atoms.get_array('PDF scatter') ** 2, axis=0)
+            if hasattr(iq_std, 'shape') and iq_std.shape != q.shape:
+                src = np.asarray(iq_std, np.float64).ravel()
+                at = np.arange(len(q), dtype=np.float64)
+                iq_std = np.interp(at, np.arange(len(src)), src)
+                iq_std[at > len(src) - 1] = np.nan
+            fq = self._noisy(fq, iq_std, q, f_sq)
+        return get_pdf_at_qmin(fq, self.exp['rstep'], self.pdf_qbin,
+                               self.get_r(), self.exp['qmin'])
 
     def get_sq(self, atoms, iq_std=None, noise_distribution=np.random.normal):
         """Structure factor S(Q) (__init__.py:393-420)."""
@@ -228,18 +229,30 @@ class ElasticScatter(object):
         return sq * f2[int(np.floor(self.exp['qmin'] / self.exp['qbin'])):]
 
     def get_2d_scatter(self, atoms, pixel_array):
-        """I(Q) projected onto a detector map of Q values (__init__.py:448-475)."""
+        """I(Q) projected onto a detector (__init__.py:448-475): a pixel of
+        momentum transfer q takes the intensity of the bin Q_k with
+        |q - Q_k| < qbin/2 (strictly; the higher bin where two qualify,
+        0 where none does)."""
         iq = self.get_iq(atoms)
-        s = self.get_scatter_vector()
-        qb = self.exp['qbin']
-        final_shape = pixel_array.shape
-        fp = pixel_array.ravel()
-        img = np.zeros(fp.shape)
-        for sub_s, i in zip(s, iq):
-            c = np.intersect1d(np.where(sub_s - qb / 2. < fp)[0],
-                               np.where(sub_s + qb / 2. > fp)[0])
-            img[c] = i
-        return img.reshape(final_shape)
+        qk = self.get_scatter_vector()
+        nk = min(len(qk), len(iq))
+        half = self.exp['qbin'] / 2.
+        q = np.asarray(pixel_array, dtype=np.float64).ravel()
+        img = np.zeros(q.shape)
+        if nk == 0:
+            return img.reshape(np.shape(pixel_array))
+        with np.errstate(invalid='ignore'):
+            near = np.floor((q - qk[0]) / self.exp['qbin'] + 0.5)
+        near = np.nan_to_num(near, nan=-2.0, posinf=-2.0, neginf=-2.0)
+        # the qualifying bins are among the nearest three; ascending order
+        # lets the higher one win
+        for dk in (-1, 0, 1):
+            k = near.astype(np.int64) + dk
+            kc = np.clip(k, 0, nk - 1)
+            hit = ((k >= 0) & (k < nk) & (qk[kc] - half < q) &
+                   (qk[kc] + half > q))
+            img[hit] = iq[kc[hit]]
+        return img.reshape(np.shape(pixel_array))
 
     def get_grad_fq(self, atoms):
         """Gradient of F(Q) in the reference convention (-1/2 dF/dx),

@@ -184,6 +184,32 @@ def main(ref_root):
     numbers, pos = cases['rand40']
     run('rand40', 'default', numbers, pos, False)
 
+    # noisy getters (seeded RandomState of the ElasticScatter) and the
+    # detector projection of I(Q)
+    for exp_name in ('default', 'short'):
+        numbers, pos = cases['alloy16']
+        key = f'noise__alloy16__{exp_name}'
+        e = EXPS[exp_name]
+        scat = ElasticScatter(exp_dict=None if e is None else dict(e),
+                              seed=1234)
+        atoms = MiniAtoms(numbers, pos)
+        out[key + '__fq_iq_std_scalar'] = scat.get_fq(atoms, iq_std=0.01)
+        n_q = len(scat.get_scatter_vector())
+        std = np.linspace(0.005, 0.02, n_q)
+        out[key + '__iq_std_array'] = std
+        out[key + '__fq_iq_std_array'] = scat.get_fq(atoms, iq_std=std)
+        out[key + '__pdf_iq_std_scalar'] = scat.get_pdf(atoms, iq_std=0.01)
+        n_qp = len(scat.get_scatter_vector(pdf=True))
+        stdp = np.linspace(0.005, 0.02, n_qp)
+        out[key + '__pdf_iq_std_array'] = scat.get_pdf(atoms, iq_std=stdp)
+        prng = np.random.default_rng(77)
+        q = scat.get_scatter_vector()
+        pix = prng.uniform(q[0] - 1.0, q[-1] + 1.0, (40, 30))
+        pix[0, :8] = q[:8]  # exactly on bin centres
+        pix[1, :8] = q[:8] + scat.exp['qbin'] / 2.  # on bin edges
+        out[key + '__pixels'] = pix
+        out[key + '__2d'] = scat.get_2d_scatter(atoms, pix)
+
     # potentials through the calc wrappers (Calc1D's energy/forces path)
     for exp_name, (ta, tb) in [('short', ('square', 'square75')),
                                ('short', ('rand20', 'rand20b')),

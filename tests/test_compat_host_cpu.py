@@ -52,9 +52,10 @@ def ES(monkeypatch):
     monkeypatch.setattr(es_mod.ElasticScatter, 'set_processor', set_processor)
     monkeypatch.setattr(es_mod, 'get_pdf_at_qmin', O.pdf_fft)
 
-    def make(exp_name):
+    def make(exp_name, **kw):
         e = EXPS[exp_name]
-        return es_mod.ElasticScatter(exp_dict=None if e is None else dict(e))
+        return es_mod.ElasticScatter(exp_dict=None if e is None else dict(e),
+                                     **kw)
     return make
 
 
@@ -231,3 +232,49 @@ def test_species_column_is_not_trusted_after_an_edit(golden, ES):
     atoms.set_array('F(Q) scatter', arr)
     sp, tab = species_of(atoms, 'fq')
     assert np.array_equal(tab[sp], arr.astype(np.float32))
+
+
+@pytest.mark.parametrize('exp_name', ['default', 'short'])
+def test_noisy_getters_and_detector_map_match_reference(golden, ES, exp_name):
+    """get_fq / get_pdf with an I(Q) standard deviation (scalar and per
+    point) draw the same noise from the seeded ElasticScatter as the
+    reference does (__init__.py:332-341, 376-383), and get_2d_scatter
+    (__init__.py:448-475) maps the same pixels to the same bins, bin
+    centres and bin edges included."""
+    key = f'noise__alloy16__{exp_name}'
+    s = ES(exp_name, seed=1234)
+    base = 'alloy16__default'
+    atoms = Atoms(numbers=golden[base + '__numbers'],
+                  positions=golden[base + '__positions'])
+    close(s.get_fq(atoms, iq_std=0.01), golden[key + '__fq_iq_std_scalar'])
+    close(s.get_fq(atoms, iq_std=golden[key + '__iq_std_array']),
+          golden[key + '__fq_iq_std_array'])
+    close(s.get_pdf(atoms, iq_std=0.01), golden[key + '__pdf_iq_std_scalar'])
+    n_qp = len(s.get_scatter_vector(pdf=True))
+    close(s.get_pdf(atoms, iq_std=np.linspace(0.005, 0.02, n_qp)),
+          golden[key + '__pdf_iq_std_array'])
+    img = s.get_2d_scatter(atoms, golden[key + '__pixels'])
+    ref = golden[key + '__2d']
+    assert img.shape == ref.shape
+    # the same pixels are lit (bin membership is exact) ...
+    assert np.array_equal(img == 0, ref == 0)
+    # ... with the same intensities
+    close(img, ref)
+
+
+def test_detector_map_is_the_bin_rule():
+    """Pixel q lit by the bin Q_k with |q - Q_k| < qbin/2 (the later bin
+    where two qualify, none at exact half-bin edges), NaN pixels dark."""
+    from pyiid_gb300.experiments import elasticscatter as es_mod
+    s = es_mod.ElasticScatter.__new__(es_mod.ElasticScatter)
+    s.exp = {'qmin': 0.0, 'qmax': 1.0, 'qbin': 0.1}
+    iq = np.arange(1.0, 11.0)
+    s.get_iq = lambda atoms: iq
+    q = s.exp['qbin'] * np.arange(10)
+    s.get_scatter_vector = lambda pdf=False: q
+    pix = np.array([[0.0, 0.04, 0.05, 0.06, 0.949, 0.95, 1.2, np.nan]])
+    img = s.get_2d_scatter(None, pix)
+    want = np.zeros(pix.size)
+    for qk, ik in zip(q, iq):
+        want[(qk - 0.05 < pix.ravel()) & (qk + 0.05 > pix.ravel())] = ik
+    assert np.array_equal(img.ravel(), want)

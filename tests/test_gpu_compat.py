@@ -230,3 +230,25 @@ def test_weighted_rw_matches_reference(golden):
         # unit weights give the unweighted value
         assert abs(master_kernel.get_rw(target, gcalc, weight=np.ones_like(w))[0]
                    - master_kernel.get_rw(target, gcalc)[0]) <= 1e-14
+
+
+@pytest.mark.parametrize('exp_name', ['default', 'short'])
+def test_noisy_getters_and_detector_map_match_reference(golden, exp_name):
+    """The seeded noise of get_fq / get_pdf and get_2d_scatter on the GB300
+    processor against the reference's recorded outputs."""
+    from pyiid_gb300.experiments.elasticscatter import ElasticScatter
+    key = f'noise__alloy16__{exp_name}'
+    e = EXPS[exp_name]
+    s = ElasticScatter(exp_dict=None if e is None else dict(e), seed=1234)
+    atoms = Atoms(numbers=golden['alloy16__default__numbers'],
+                  positions=golden['alloy16__default__positions'])
+    close(s.get_fq(atoms, iq_std=0.01), golden[key + '__fq_iq_std_scalar'])
+    close(s.get_fq(atoms, iq_std=golden[key + '__iq_std_array']),
+          golden[key + '__fq_iq_std_array'])
+    close(s.get_pdf(atoms, iq_std=0.01), golden[key + '__pdf_iq_std_scalar'])
+    n_qp = len(s.get_scatter_vector(pdf=True))
+    close(s.get_pdf(atoms, iq_std=np.linspace(0.005, 0.02, n_qp)),
+          golden[key + '__pdf_iq_std_array'])
+    img = s.get_2d_scatter(atoms, golden[key + '__pixels'])
+    assert np.array_equal(img == 0, golden[key + '__2d'] == 0)
+    close(img, golden[key + '__2d'])
