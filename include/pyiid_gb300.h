@@ -456,6 +456,43 @@ int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy, float *g_w1,
                        float *g_b1, float *g_w2, float *g_b2, float *g_w3,
                        float *g_b3);
 
+/* Neighbour lists for the surrogate: for every atom a of a packed batch,
+ * the atoms b != a of its configuration with |x_a - x_b| < r_list, in
+ * increasing b.
+ *   nbr_idx : device int32 [total][max_nb] (indices into the packed arrays)
+ *   nbr_cnt : device int32 [total], the number of neighbours found; a count
+ *             above max_nb means the list overflowed (only max_nb stored)
+ * No counterpart in the reference. */
+int pyiid_neighbor_list(pyiid_ctx *ctx, const float *positions,
+                        const int32_t *offsets, int n_configs, float r_list,
+                        int max_nb, int32_t *nbr_idx, int32_t *nbr_cnt);
+
+/* Energy and forces of the surrogate for trajectories driven by it (the
+ * cheap first stage of delayed-acceptance HMC).  From neighbour lists
+ * (pyiid_neighbor_list with r_list >= r_cut) the descriptors of
+ * pyiid_rbf_features, the MLP of pyiid_mlp_forward and its gradient with
+ * respect to the descriptors (the same BF16 tensor-core GEMMs, transposed),
+ * then per atom
+ *   dE/dx_a = sum_{b in list(a), r_ab < r_cut} sum_c (dE/dfeat[a][c] +
+ *             dE/dfeat[b][c]) dphi_c/dr (x_a - x_b) / r_ab.
+ *   energy    : device double [n_configs], E = sum_a y_a (unscaled)
+ *   forces    : device float [total][3] = -scale dE/dx, or NULL (energy only)
+ *   feat_bf16 : device bfloat16 [total][n_centres] for the descriptors, or
+ *               NULL (context workspace)
+ * Other arguments as pyiid_rbf_features / pyiid_mlp_forward.  Uses its own
+ * workspace (training calls on the same context do not disturb it); after a
+ * first call with the same sizes the call allocates nothing and can be
+ * captured in a CUDA graph.  No counterpart in the reference. */
+int pyiid_surrogate_forces(pyiid_ctx *ctx, const float *positions,
+                           const int32_t *offsets, int n_configs,
+                           const int32_t *nbr_idx, const int32_t *nbr_cnt,
+                           int max_nb, int n_centres, float r_cut,
+                           float sigma, const void *w1_bf16, const float *b1,
+                           const void *w2_bf16, const float *b2,
+                           const float *w3, const float *b3, int n_hidden,
+                           float scale, double *energy, float *forces,
+                           void *feat_bf16);
+
 /* ------------------------------------------------------------------------ *
  * Launch-shape variants (autotuning).
  *

@@ -85,6 +85,12 @@ _SIGNATURES = {
                                    _vp]),
     'pyiid_mlp_backward': (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                     _vp]),
+    'pyiid_neighbor_list': (_c_int, [_vp, _vp, _i32p, _c_int, ctypes.c_float,
+                                     _c_int, _vp, _vp]),
+    'pyiid_surrogate_forces': (_c_int, [
+        _vp, _vp, _i32p, _c_int, _vp, _vp, _c_int, _c_int, ctypes.c_float,
+        ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, ctypes.c_float,
+        _vp, _vp, _vp]),
     'pyiid_variant_count': (_c_int, [_c_int]),
     'pyiid_variant_info': (_c_int, [_c_int, _c_int, _i32p, _c_int]),
     'pyiid_set_variant': (_c_int, [_vp, _c_int, _c_int]),

@@ -2207,3 +2207,149 @@ extern "C" int pyiid_mlp_backward(pyiid_ctx *ctx, const double *d_energy,
   LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }
+
+// ======================================================= surrogate forces
+// The surrogate's energy and forces for trajectories driven by it (the
+// first stage of delayed-acceptance HMC): descriptors from neighbour lists,
+// the MLP forward, its gradient with respect to the descriptors (the same
+// BF16 tensor-core GEMMs transposed) and the per-atom forces.  Workspace and
+// the atom -> configuration map use their own buffers ("sf_*"), so training
+// calls on the same context never move what a captured graph of this path
+// reads.
+namespace {
+
+std::mutex g_sf_mu;
+std::unordered_map<const pyiid_ctx *, uint64_t> g_sf_key;
+
+int sf_config_map(pyiid_ctx *ctx, const int32_t *offsets, int n_configs,
+                  int **d_cfg, int **d_off) {
+  const int total = offsets[n_configs];
+  const uint64_t key = fnv1a(offsets, sizeof(int32_t) * (n_configs + 1));
+  void *p;
+  TRY(ensure(ctx, "sf_cfg", sizeof(int) * std::max(total, 1), &p));
+  *d_cfg = static_cast<int *>(p);
+  TRY(ensure(ctx, "sf_off", sizeof(int) * (n_configs + 1), &p));
+  *d_off = static_cast<int *>(p);
+  std::lock_guard<std::mutex> lk(g_sf_mu);
+  auto it = g_sf_key.find(ctx);
+  // the key mixes the buffer address so a reallocated buffer is refilled
+  const uint64_t full = fnv1a(d_cfg, sizeof(*d_cfg), key);
+  if (it == g_sf_key.end() || it->second != full) {
+    std::vector<int> cfg(std::max(total, 1), 0);
+    for (int c = 0; c < n_configs; ++c)
+      for (int a = offsets[c]; a < offsets[c + 1]; ++a) cfg[a] = c;
+    CUDA_TRY(ctx, cudaMemcpy(*d_cfg, cfg.data(), sizeof(int) * cfg.size(),
+                             cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMemcpy(*d_off, offsets, sizeof(int) * (n_configs + 1),
+                             cudaMemcpyHostToDevice));
+    g_sf_key[ctx] = full;
+  }
+  return PYIID_OK;
+}
+
+}  // namespace
+
+extern "C" int pyiid_neighbor_list(pyiid_ctx *ctx, const float *positions,
+                                   const int32_t *offsets, int n_configs,
+                                   float r_list, int max_nb, int32_t *nbr_idx,
+                                   int32_t *nbr_cnt) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  TRY(check_offsets(ctx, offsets, n_configs));
+  if (!(r_list > 0)) return fail(ctx, PYIID_ERR_INVALID_ARG, "r_list <= 0");
+  if (max_nb < 1) return fail(ctx, PYIID_ERR_INVALID_ARG, "max_nb < 1");
+  const int total = offsets[n_configs];
+  if (total == 0) return PYIID_OK;
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  int *d_cfg, *d_off;
+  TRY(sf_config_map(ctx, offsets, n_configs, &d_cfg, &d_off));
+  const int warps = 8;
+  neighbor_list_kernel<<<(total + warps - 1) / warps, 32 * warps, 0,
+                         ctx->stream>>>(positions, d_cfg, d_off, total,
+                                        r_list * r_list, max_nb, nbr_idx,
+                                        nbr_cnt);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}
+
+extern "C" int pyiid_surrogate_forces(
+    pyiid_ctx *ctx, const float *positions, const int32_t *offsets,
+    int n_configs, const int32_t *nbr_idx, const int32_t *nbr_cnt, int max_nb,
+    int n_centres, float r_cut, float sigma, const void *w1_bf16,
+    const float *b1, const void *w2_bf16, const float *b2, const float *w3,
+    const float *b3, int n_hidden, float scale, double *energy,
+    float *forces, void *feat_bf16) {
+  if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
+  TRY(check_offsets(ctx, offsets, n_configs));
+  if (n_centres < 2 || n_centres > 64)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "n_centres must be in [2, 64]");
+  if (!(r_cut > 0) || !(sigma > 0))
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "r_cut and sigma must be > 0");
+  if (n_hidden < 1 || max_nb < 1)
+    return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  const int n = offsets[n_configs];
+  CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  int *d_cfg, *d_off;
+  TRY(sf_config_map(ctx, offsets, n_configs, &d_cfg, &d_off));
+  const int H = n_hidden, C = n_centres;
+  const size_t nh = (size_t)std::max(n, 1) * H;
+  void *p;
+  __nv_bfloat16 *X = static_cast<__nv_bfloat16 *>(feat_bf16);
+  if (!X) {
+    TRY(ensure(ctx, "sf_x", (size_t)std::max(n, 1) * C * sizeof(__nv_bfloat16),
+               &p));
+    X = static_cast<__nv_bfloat16 *>(p);
+  }
+  TRY(ensure(ctx, "sf_h1", nh * sizeof(float), &p));
+  float *h1 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sf_pre1", nh * sizeof(float), &p));
+  float *pre1 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sf_h1b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *h1b = static_cast<__nv_bfloat16 *>(p);
+  TRY(ensure(ctx, "sf_h2", nh * sizeof(float), &p));
+  float *h2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sf_pre2", nh * sizeof(float), &p));
+  float *pre2 = static_cast<float *>(p);
+  TRY(ensure(ctx, "sf_h2b", nh * sizeof(__nv_bfloat16), &p));
+  __nv_bfloat16 *h2b = static_cast<__nv_bfloat16 *>(p);
+  TRY(ensure(ctx, "sf_y", sizeof(float) * std::max(n, 1), &p));
+  float *y = static_cast<float *>(p);
+  TRY(ensure(ctx, "sf_gx", (size_t)std::max(n, 1) * C * sizeof(float), &p));
+  float *gx = static_cast<float *>(p);
+  const __nv_bfloat16 *W1 = static_cast<const __nv_bfloat16 *>(w1_bf16);
+  const __nv_bfloat16 *W2 = static_cast<const __nv_bfloat16 *>(w2_bf16);
+  const int warps = 8;
+  const int wgrid = (std::max(n, 1) + warps - 1) / warps;
+  if (n > 0) {
+    rbf_features_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
+        positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, X, nullptr);
+    LAUNCH_CHECK(ctx);
+    TRY((gemm<false, false>(ctx, X, C, W1, H, h1, H, n, H, C, 0)));
+    bias_silu_kernel<<<512, 256, 0, ctx->stream>>>(h1, b1, n, H, h1b, pre1);
+    LAUNCH_CHECK(ctx);
+    TRY((gemm<false, false>(ctx, h1b, H, W2, H, h2, H, n, H, H, 0)));
+    bias_silu_kernel<<<512, 256, 0, ctx->stream>>>(h2, b2, n, H, h2b, pre2);
+    LAUNCH_CHECK(ctx);
+    head_kernel<<<(n * 32 + 255) / 256, 256, 0, ctx->stream>>>(h2, w3, b3, n,
+                                                                H, y);
+    LAUNCH_CHECK(ctx);
+  }
+  reduce_by_config_kernel<<<n_configs, 256, 0, ctx->stream>>>(y, d_off,
+                                                              n_configs, energy);
+  LAUNCH_CHECK(ctx);
+  if (!forces || n == 0) return PYIID_OK;
+  // dE/dh2 = w3 for every atom; back through both layers to dE/dfeat.
+  // h1/h2 and their BF16 copies are dead now: reuse them as gradients.
+  broadcast_rows_kernel<<<512, 256, 0, ctx->stream>>>(w3, n, H, h2, h2b);
+  LAUNCH_CHECK(ctx);
+  silu_backward_kernel<<<512, 256, 0, ctx->stream>>>(h2, pre2, nh, h2b, h2);
+  LAUNCH_CHECK(ctx);
+  TRY((gemm<false, true>(ctx, h2b, H, W2, H, h1, H, n, H, H, 0)));
+  silu_backward_kernel<<<512, 256, 0, ctx->stream>>>(h1, pre1, nh, h1b, h1);
+  LAUNCH_CHECK(ctx);
+  TRY((gemm<false, true>(ctx, h1b, H, W1, H, gx, C, n, C, H, 0)));
+  rbf_forces_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
+      positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, gx, scale,
+      forces);
+  LAUNCH_CHECK(ctx);
+  return PYIID_OK;
+}

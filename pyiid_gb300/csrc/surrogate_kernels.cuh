@@ -266,6 +266,165 @@ __global__ void column_sum_kernel(const float *__restrict__ Mx, int rows,
   if (threadIdx.x == 0) out[j] = (float)sm[0];
 }
 
+// ------------------------------------------------ neighbour-list variants
+// Neighbour lists: for every atom a, the atoms b != a of its configuration
+// with |x_a - x_b|^2 < r_list2, in increasing b.  count[a] is the number
+// found; entries beyond max_nb are not stored, so count[a] > max_nb flags an
+// overflow.  One warp per atom: lanes test b = b0 + lane + 32 t and a ballot
+// compacts the hits in b order.
+__global__ void neighbor_list_kernel(const float *__restrict__ pos,
+                                     const int *__restrict__ atom_cfg,
+                                     const int *__restrict__ offsets,
+                                     int n_atoms, float r_list2, int max_nb,
+                                     int *__restrict__ nbr,
+                                     int *__restrict__ count) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (a >= n_atoms) return;  // whole warps leave together
+  const int cfg = atom_cfg[a];
+  const int b0 = offsets[cfg], b1 = offsets[cfg + 1];
+  const float ax = pos[3 * a], ay = pos[3 * a + 1], az = pos[3 * a + 2];
+  int n = 0;
+  for (int base = b0; base < b1; base += 32) {
+    const int b = base + lane;
+    bool hit = false;
+    if (b < b1 && b != a) {
+      const float dx = pos[3 * b] - ax, dy = pos[3 * b + 1] - ay,
+                  dz = pos[3 * b + 2] - az;
+      hit = dx * dx + dy * dy + dz * dz < r_list2;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (hit) {
+      const int slot = n + __popc(m & ((1u << lane) - 1u));
+      if (slot < max_nb) nbr[(size_t)a * max_nb + slot] = b;
+    }
+    n += __popc(m);
+  }
+  if (lane == 0) count[a] = n;
+}
+
+// rbf_features_kernel over a neighbour list instead of every atom of the
+// configuration: the same terms added in the same (increasing b) order, so
+// the descriptors are bitwise those of the all-pairs kernel whenever the
+// list holds every atom within rc.
+__global__ void rbf_features_nl_kernel(const float *__restrict__ pos,
+                                       const int *__restrict__ nbr,
+                                       const int *__restrict__ count,
+                                       int max_nb, int n_atoms, int n_centres,
+                                       float rc, float sigma,
+                                       __nv_bfloat16 *__restrict__ fb,
+                                       float *__restrict__ ff) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (a >= n_atoms) return;
+  const int n = min(count[a], max_nb);
+  const int *nb = nbr + (size_t)a * max_nb;
+  const float ax = pos[3 * a], ay = pos[3 * a + 1], az = pos[3 * a + 2];
+  const float step = rc / (float)(n_centres - 1);
+  const float inv2s2 = 0.5f / (sigma * sigma);
+  const float mu0 = lane * step, mu1 = (lane + 32) * step;
+  const float rc2 = rc * rc;
+  float acc0 = 0.f, acc1 = 0.f;
+  for (int i = 0; i < n; ++i) {
+    const int b = nb[i];
+    const float dx = pos[3 * b] - ax, dy = pos[3 * b + 1] - ay,
+                dz = pos[3 * b + 2] - az;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 >= rc2) continue;
+    const float r = sqrtf(r2);
+    const float fc = 0.5f * (1.f + cospif(r / rc));
+    const float d0 = r - mu0, d1 = r - mu1;
+    acc0 = fmaf(fc, __expf(-d0 * d0 * inv2s2), acc0);
+    acc1 = fmaf(fc, __expf(-d1 * d1 * inv2s2), acc1);
+  }
+  if (lane < n_centres) {
+    fb[(size_t)a * n_centres + lane] = __float2bfloat16_rn(acc0);
+    if (ff) ff[(size_t)a * n_centres + lane] = acc0;
+  }
+  if (lane + 32 < n_centres) {
+    fb[(size_t)a * n_centres + lane + 32] = __float2bfloat16_rn(acc1);
+    if (ff) ff[(size_t)a * n_centres + lane + 32] = acc1;
+  }
+}
+
+// out[a][j] = v[j] for every row a (FP32 and BF16): dE/dh2 when
+// E = sum_a y_a.
+__global__ void broadcast_rows_kernel(const float *__restrict__ v, int rows,
+                                      int n, float *__restrict__ out,
+                                      __nv_bfloat16 *__restrict__ outb) {
+  const size_t total = (size_t)rows * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const float x = v[i % n];
+    out[i] = x;
+    outb[i] = __float2bfloat16_rn(x);
+  }
+}
+
+// Forces of the surrogate energy E = sum_a y_a from g[a][c] = dE/dfeat[a][c]:
+//   dE/dx_a = sum_{b in list(a), r_ab < rc} sum_c (g[a][c] + g[b][c])
+//             phi_c'(r_ab) (x_a - x_b) / r_ab,
+//   phi_c(r) = exp(-(r - mu_c)^2 / (2 s^2)) fc(r),
+//   phi_c'(r) = exp(-(r - mu_c)^2 / (2 s^2)) (fc'(r) - fc(r) (r - mu_c)/s^2),
+//   fc'(r) = -(pi / (2 rc)) sin(pi r / rc),
+// (the descriptor of b holds the pair too), forces[a] = -scale dE/dx_a.  One
+// warp per atom, lane = centre (and centre + 32); the x, y, z partial sums
+// are reduced over the warp once per atom.
+__global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
+                                     const int *__restrict__ nbr,
+                                     const int *__restrict__ count,
+                                     int max_nb, int n_atoms, int n_centres,
+                                     float rc, float sigma,
+                                     const float *__restrict__ g, float scale,
+                                     float *__restrict__ forces) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (a >= n_atoms) return;
+  const int n = min(count[a], max_nb);
+  const int *nb = nbr + (size_t)a * max_nb;
+  const float ax = pos[3 * a], ay = pos[3 * a + 1], az = pos[3 * a + 2];
+  const float step = rc / (float)(n_centres - 1);
+  const float inv_s2 = 1.f / (sigma * sigma);
+  const float inv2s2 = 0.5f * inv_s2;
+  const float mu0 = lane * step, mu1 = (lane + 32) * step;
+  const bool c0 = lane < n_centres, c1 = lane + 32 < n_centres;
+  const float ga0 = c0 ? g[(size_t)a * n_centres + lane] : 0.f;
+  const float ga1 = c1 ? g[(size_t)a * n_centres + lane + 32] : 0.f;
+  const float rc2 = rc * rc;
+  const float kfc = -0.5f * 3.14159265358979f / rc;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  for (int i = 0; i < n; ++i) {
+    const int b = nb[i];
+    const float dx = ax - pos[3 * b], dy = ay - pos[3 * b + 1],
+                dz = az - pos[3 * b + 2];
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 >= rc2) continue;
+    const float r = sqrtf(r2);
+    float sn, cs;
+    sincospif(r / rc, &sn, &cs);
+    const float fc = 0.5f * (1.f + cs), dfc = kfc * sn;
+    const float gb0 = c0 ? g[(size_t)b * n_centres + lane] : 0.f;
+    const float gb1 = c1 ? g[(size_t)b * n_centres + lane + 32] : 0.f;
+    const float d0 = r - mu0, d1 = r - mu1;
+    const float p0 = __expf(-d0 * d0 * inv2s2) * (dfc - fc * d0 * inv_s2);
+    const float p1 = __expf(-d1 * d1 * inv2s2) * (dfc - fc * d1 * inv_s2);
+    const float s = ((ga0 + gb0) * p0 + (ga1 + gb1) * p1) / r;
+    fx = fmaf(s, dx, fx);
+    fy = fmaf(s, dy, fy);
+    fz = fmaf(s, dz, fz);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+  }
+  if (lane == 0) {
+    forces[3 * (size_t)a] = -scale * fx;
+    forces[3 * (size_t)a + 1] = -scale * fy;
+    forces[3 * (size_t)a + 2] = -scale * fz;
+  }
+}
+
 __global__ void to_bf16_kernel(const float *__restrict__ x, size_t n,
                                __nv_bfloat16 *__restrict__ y) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;

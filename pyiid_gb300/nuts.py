@@ -499,9 +499,14 @@ class BatchedNUTS:
         masses = np.asarray(pot.masses, np.float64).reshape(B, -1)
         out = pot.buffers()
 
+        k = -0.5 * float(pot.conv)
+
         def evaluate(x):
-            e, g = pot.evaluate(x.reshape(-1, 3).to(torch.float32), out=out)
-            return e, (-0.5 * g).reshape(x.shape).to(x.dtype)
+            # as Calc1D: conv * Rw in FP64, forces (-1/2 conv) times the
+            # float32 gradient of Rw, scaled in FP64
+            e, _ = pot.evaluate(x.reshape(-1, 3).to(torch.float32), out=out)
+            g = out['grad'].to(x.dtype)
+            return e, (k * g).reshape(x.shape)
 
         seeds = list(range(B)) if seeds is None else list(seeds)
         self.engine = NUTSEngine(evaluate, torch.as_tensor(starts,

@@ -325,3 +325,243 @@ class DelayedAcceptanceMH(ExactSingleAtomMH):
             self._subpots = getattr(self, '_subpots', {})
             self._subpots[k] = sub
         return sub.evaluate(xs.reshape(-1, 3), want_grad=False)[0]
+
+
+class DelayedAcceptanceHMC:
+    """Hamiltonian Monte Carlo whose trajectories follow the surrogate, with
+    delayed acceptance (Christen & Fox 2005) on top.
+
+    Every iteration of every chain draws Maxwell-Boltzmann momenta and runs
+    ``n_steps`` leapfrog steps of size ``dt`` (BatchedHMC's integrator) with
+    the SURROGATE's forces -conv dRw~/dx (``pyiid_surrogate_forces``:
+    neighbour-list descriptors, BF16 tensor-core MLP forward and input
+    gradient).  Leapfrog on any smooth potential is reversible and volume
+    preserving, so the move is a valid Metropolis proposal for the exact
+    target exp(-H/kT); it is accepted in two stages:
+        stage 1: log u1 < -(H~' - H~)/kT,  H~ = conv Rw~ + K   (surrogate)
+        stage 2: log u2 < -[(H' - H) - (H~' - H~)]/kT,  H = conv Rw + K
+    with the exact Debye potential (energy only, ``pyiid_batch_potential_grad``
+    without gradient) in stage 2, so the chain's target is the exact one
+    whatever the surrogate's quality; a poor surrogate costs acceptance, not
+    correctness.  The exact potential is evaluated once per iteration (at
+    the trajectory's end), against once per leapfrog step in BatchedHMC.
+
+    The neighbour lists are built at the start of every trajectory with
+    radius r_cut + ``skin``; the largest displacement within a trajectory
+    and the largest list length are tracked on the device, and
+    :meth:`check` raises when either invalidates the lists.  Exact
+    (configuration, Rw) pairs of every stage 2 enter a ring buffer;
+    :meth:`train` takes Adam steps on it and copies the new weights into the
+    buffers the captured iteration reads.  With ``graph=True`` one iteration
+    of all chains is one CUDA graph replay.
+    """
+
+    def __init__(self, pot, surrogate, positions, temperature=300.0, dt=1e-3,
+                 n_steps=10, seed=0, graph=False, skin=1.0, max_nb=256,
+                 buffer_size=2048):
+        d = pot.device
+        self.pot, self.sur = pot, surrogate
+        self.kT = kB * float(temperature)
+        self.dt, self.n_steps = float(dt), int(n_steps)
+        self.B = pot.n_configs
+        self.off, self._offp = _i32(pot.offsets)
+        self.N = int(pot.n_total)
+        sizes = np.diff(self.off)
+        self.n_per = int(sizes[0]) if len(sizes) and np.all(
+            sizes == sizes[0]) else None
+        self.x = torch.as_tensor(np.asarray(positions, np.float32),
+                                 device=d).reshape(-1, 3).clone()
+        self.m = torch.as_tensor(pot.masses, dtype=torch.float32,
+                                 device=d)[:, None]
+        self.cfg = pot.config_index()
+        self.gen = torch.Generator(device=d)
+        self.gen.manual_seed(int(seed))
+        self.max_nb = int(max_nb)
+        self.r_list = float(surrogate.rc + skin)
+        self.skin = float(skin)
+        self.nbr = torch.zeros((self.N, self.max_nb), dtype=torch.int32,
+                               device=d)
+        self.cnt = torch.zeros(self.N, dtype=torch.int32, device=d)
+        self.feat = torch.empty((self.N, surrogate.C), dtype=torch.bfloat16,
+                                device=d)
+        self.es = torch.empty(self.B, dtype=torch.float64, device=d)
+        self.fs = torch.empty((self.N, 3), dtype=torch.float32, device=d)
+        C, H = surrogate.C, surrogate.H
+        self.w = {'w1b': torch.empty((C, H), dtype=torch.bfloat16, device=d),
+                  'b1': torch.empty(H, device=d),
+                  'w2b': torch.empty((H, H), dtype=torch.bfloat16, device=d),
+                  'b2': torch.empty(H, device=d),
+                  'w3': torch.empty(H, device=d),
+                  'b3': torch.empty(1, device=d)}
+        self.refresh_weights()
+        self.E = pot.evaluate(self.x, want_grad=False)[0].clone()
+        self.accepted = torch.zeros(self.B, dtype=torch.int64, device=d)
+        self.stage1 = torch.zeros(self.B, dtype=torch.int64, device=d)
+        self.max_disp = torch.zeros((), dtype=torch.float32, device=d)
+        self.max_cnt = torch.zeros((), dtype=torch.int32, device=d)
+        self.sum_dhs_err = torch.zeros((), dtype=torch.float64, device=d)
+        self.proposed = 0
+        # replay buffer of exact (configuration, Rw) pairs (equal-size chains)
+        self.buf_size = int(buffer_size) if self.n_per else 0
+        if self.buf_size:
+            self.buf_x = torch.zeros((self.buf_size, self.n_per, 3),
+                                     dtype=torch.float32, device=d)
+            self.buf_e = torch.zeros(self.buf_size, dtype=torch.float64,
+                                     device=d)
+        self.buf_ptr = torch.zeros((), dtype=torch.int64, device=d)
+        self.buf_n = 0
+        self.graph = None
+        if graph:
+            self._capture()
+
+    # -------------------------------------------------------------- pieces
+    def refresh_weights(self):
+        """Copy the surrogate's current (standardisation-folded) weights into
+        the buffers the iteration reads."""
+        w1b, b1, w2b = self.sur._effective()
+        p = self.sur.params
+        self.w['w1b'].copy_(w1b)
+        self.w['b1'].copy_(b1)
+        self.w['w2b'].copy_(w2b)
+        self.w['b2'].copy_(p['b2'])
+        self.w['w3'].copy_(p['w3'])
+        self.w['b3'].copy_(p['b3'])
+
+    def _neighbours(self, x):
+        self.sur.ctx.call('pyiid_neighbor_list', _vp(x), self._offp, self.B,
+                          ctypes.c_float(self.r_list), self.max_nb,
+                          _vp(self.nbr), _vp(self.cnt))
+
+    def surrogate(self, x):
+        """(conv Rw~ [B] FP64, forces -conv dRw~/dx [N, 3]) at x, with the
+        current neighbour lists."""
+        s, w = self.sur, self.w
+        conv = float(self.pot.conv)
+        s.ctx.call('pyiid_surrogate_forces', _vp(x), self._offp, self.B,
+                   _vp(self.nbr), _vp(self.cnt), self.max_nb, s.C,
+                   ctypes.c_float(s.rc), ctypes.c_float(s.sigma),
+                   _vp(w['w1b']), _vp(w['b1']), _vp(w['w2b']), _vp(w['b2']),
+                   _vp(w['w3']), _vp(w['b3']), s.H, ctypes.c_float(conv),
+                   _vp(self.es), _vp(self.fs), _vp(self.feat))
+        return conv * self.es, self.fs
+
+    def _kinetic(self, p):
+        ke_atom = 0.5 * (p.double() ** 2 / self.m.double()).sum(1)
+        out = torch.zeros(self.B, dtype=torch.float64, device=p.device)
+        return out.index_add_(0, self.cfg, ke_atom)
+
+    def _iteration(self):
+        dt = self.dt
+        x0 = self.x.clone()
+        self._neighbours(x0)
+        self.max_cnt.copy_(torch.maximum(self.max_cnt, self.cnt.max()))
+        s0, f = self.surrogate(x0)
+        s0 = s0.clone()
+        p = torch.randn(x0.shape, generator=self.gen,
+                        device=x0.device) * torch.sqrt(self.m * self.kT)
+        k0 = self._kinetic(p)
+        x = x0
+        p = p + 0.5 * dt * f
+        disp = torch.zeros((), dtype=torch.float32, device=x0.device)
+        for i in range(self.n_steps):
+            x = x + dt * p / self.m
+            disp = torch.maximum(disp, (x - x0).norm(dim=1).max())
+            s1, f = self.surrogate(x)
+            if i + 1 < self.n_steps:
+                p = p + dt * f
+        p = p + 0.5 * dt * f
+        k1 = self._kinetic(p)
+        dhs = (s1 - s0) + (k1 - k0)
+        e1 = self.pot.evaluate(x, want_grad=False)[0]
+        dh = (e1 - self.E) + (k1 - k0)
+        logu = torch.log(torch.rand((2, self.B), generator=self.gen,
+                                    device=x.device, dtype=torch.float64))
+        st1 = da_stage1(logu[0], dhs, self.kT)
+        st2 = da_stage2(logu[1], dh, dhs, self.kT)
+        acc = st1 & st2
+        self.x.copy_(torch.where(acc[self.cfg][:, None], x, self.x))
+        self.E.copy_(torch.where(acc, e1, self.E))
+        self.accepted += acc.to(torch.int64)
+        self.stage1 += st1.to(torch.int64)
+        self.max_disp.copy_(torch.maximum(self.max_disp, disp))
+        self.sum_dhs_err += ((dh - dhs) ** 2).sum()
+        if self.buf_size:
+            idx = (self.buf_ptr + torch.arange(self.B, device=x.device)
+                   ) % self.buf_size
+            self.buf_x[idx] = x.reshape(self.B, self.n_per, 3)
+            self.buf_e[idx] = e1 / self.pot.conv
+            self.buf_ptr.add_(self.B)
+
+    def _capture(self):
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        state = (self.x.clone(), self.E.clone())
+        with torch.cuda.stream(s):
+            for _ in range(2):      # warm layouts, workspaces and buffers
+                self._iteration()
+        torch.cuda.current_stream().wait_stream(s)
+        self.x.copy_(state[0])
+        self.E.copy_(state[1])
+        self._reset_counters()
+        self.graph = torch.cuda.CUDAGraph()
+        if hasattr(self.graph, 'register_generator_state'):
+            self.graph.register_generator_state(self.gen)
+        with torch.cuda.graph(self.graph):
+            self._iteration()
+
+    def _reset_counters(self):
+        self.accepted.zero_()
+        self.stage1.zero_()
+        self.max_disp.zero_()
+        self.max_cnt.zero_()
+        self.sum_dhs_err.zero_()
+        self.buf_ptr.zero_()
+        self.proposed = 0
+        self.buf_n = 0
+
+    # ----------------------------------------------------------------- API
+    def step(self, n=1):
+        for _ in range(n):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._iteration()
+            self.proposed += 1
+            self.buf_n = min(self.buf_n + self.B, self.buf_size)
+        return self
+
+    def check(self):
+        """Raise if a neighbour list overflowed or an atom moved more than
+        half the skin within a trajectory (the lists would have missed
+        pairs)."""
+        mc, md = int(self.max_cnt.item()), float(self.max_disp.item())
+        if mc > self.max_nb:
+            raise NativeError(f'neighbour list overflow: {mc} > {self.max_nb}')
+        if md >= 0.5 * self.skin:
+            raise NativeError(f'an atom moved {md:.3f} A within a trajectory '
+                              f'(skin {self.skin} A)')
+        return {'max_neighbours': mc, 'max_displacement': md}
+
+    def train(self, steps=1, batch=32):
+        """Adam steps on random exact (configuration, Rw) pairs of the
+        replay buffer; the iteration then uses the new weights."""
+        if self.buf_n < 2:
+            return None
+        b = min(int(batch), self.buf_n)
+        off = (np.arange(b + 1) * self.n_per).astype(np.int32)
+        loss = None
+        for _ in range(int(steps)):
+            idx = torch.randint(0, self.buf_n, (b,), generator=self.gen,
+                                device=self.x.device)
+            fb = self.sur.features(self.buf_x[idx].reshape(-1, 3), off)
+            loss = self.sur.train_step(fb, off, self.buf_e[idx])
+        self.refresh_weights()
+        return loss
+
+    def acceptance(self):
+        n = max(self.proposed, 1)
+        return {'accepted': (self.accepted.double() / n).cpu().numpy(),
+                'stage1': (self.stage1.double() / n).cpu().numpy()}
+
+    def positions(self):
+        return self.x

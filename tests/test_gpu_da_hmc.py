@@ -1,0 +1,169 @@
+"""Delayed-acceptance HMC on the GPU: the surrogate-force kernels against
+the FP64 oracle, and the sampler's device iteration.
+
+* neighbour lists (pyiid_neighbor_list) against a brute-force search;
+* descriptors from the lists bitwise equal to the all-pairs kernel's;
+* surrogate energies and forces (pyiid_surrogate_forces: BF16 tensor-core
+  MLP forward and input gradient, pair forces) against the oracle fed the
+  same BF16 roundings (oracle/mlp_np.py, whose force formula is pinned by
+  central differences on the CPU);
+* a DelayedAcceptanceHMC iteration captured in a CUDA graph equals the eager
+  iteration bit for bit, and the exact second stage decides as the exact
+  energies say.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import mlp_np as M
+from pyiid_gb300 import structures as S
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def _batch():
+    p1 = S.displaced(S.fcc_nearest(4.08, 140), 0.1, 1)
+    p2 = S.displaced(S.fcc_nearest(4.08, 70), 0.1, 2)
+    return np.concatenate([p1, p2]).astype(np.float32), np.array(
+        [0, 140, 210], np.int32)
+
+
+def _lists(sur, pos_t, off, r_list, max_nb):
+    import torch
+    n = pos_t.shape[0]
+    nbr = torch.full((n, max_nb), -1, dtype=torch.int32, device='cuda')
+    cnt = torch.zeros(n, dtype=torch.int32, device='cuda')
+    offp = np.ascontiguousarray(off, np.int32)
+    sur.ctx.call('pyiid_neighbor_list', ctypes.c_void_p(pos_t.data_ptr()),
+                 offp.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                 len(off) - 1, ctypes.c_float(r_list), max_nb,
+                 ctypes.c_void_p(nbr.data_ptr()),
+                 ctypes.c_void_p(cnt.data_ptr()))
+    torch.cuda.synchronize()
+    return nbr, cnt
+
+
+def test_neighbour_lists_match_brute_force():
+    import torch
+    from pyiid_gb300.surrogate import RBFMLPSurrogate
+    sur = RBFMLPSurrogate()
+    pos, off = _batch()
+    pt = torch.as_tensor(pos, device='cuda')
+    nbr, cnt = _lists(sur, pt, off, 6.5, 128)
+    nbr, cnt = nbr.cpu().numpy(), cnt.cpu().numpy()
+    for c in range(2):
+        a0, a1 = off[c], off[c + 1]
+        d = pos[a0:a1, None].astype(np.float32) - pos[None, a0:a1]
+        r2 = (d * d).sum(-1)
+        for a in range(a0, a1):
+            want = [a0 + b for b in np.nonzero(r2[a - a0] < 6.5 ** 2)[0]
+                    if a0 + b != a]
+            assert cnt[a] == len(want)
+            assert list(nbr[a, :cnt[a]]) == want
+    # a list shorter than the neighbours reports the overflow
+    _, cnt2 = _lists(sur, pt, off, 6.5, 8)
+    assert np.array_equal(cnt2.cpu().numpy(), cnt)
+
+
+def _weights(sur, seed):
+    import torch
+    g = torch.Generator(device='cpu').manual_seed(seed)
+    for k in ('b1', 'b2', 'w3', 'b3'):
+        sur.params[k].copy_(torch.randn(sur.params[k].shape, generator=g)
+                            .to('cuda') * 0.1)
+
+
+def test_surrogate_energy_and_forces_match_oracle():
+    import torch
+    from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
+    sur = RBFMLPSurrogate(seed=5)
+    _weights(sur, 6)
+    pos, off = _batch()
+    pt = torch.as_tensor(pos, device='cuda')
+    nbr, cnt = _lists(sur, pt, off, sur.rc + 1.0, 256)
+    # the sampler's call path, on a stand-in holding only what it reads
+    da = DelayedAcceptanceHMC.__new__(DelayedAcceptanceHMC)
+    da.sur, da.B = sur, 2
+    da.off, da._offp = off, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    da.nbr, da.cnt, da.max_nb = nbr, cnt, 256
+    da.feat = torch.empty((len(pos), sur.C), dtype=torch.bfloat16,
+                          device='cuda')
+    da.es = torch.empty(2, dtype=torch.float64, device='cuda')
+    da.fs = torch.empty((len(pos), 3), dtype=torch.float32, device='cuda')
+
+    class _P:
+        conv = 3.0
+    da.pot = _P()
+    da.w = {'w1b': None, 'b1': None, 'w2b': None, 'b2': None, 'w3': None,
+            'b3': None}
+    w1b, b1, w2b = sur._effective()
+    p = sur.params
+    da.w.update({'w1b': w1b, 'b1': b1, 'w2b': w2b, 'b2': p['b2'],
+                 'w3': p['w3'], 'b3': p['b3']})
+    e, f = da.surrogate(pt)
+    torch.cuda.synchronize()
+    # descriptors from the lists are the all-pairs kernel's, bit for bit
+    assert torch.equal(da.feat, sur.features(pos, off))
+    pc = {k: v.cpu().numpy().astype(np.float64) for k, v in p.items()}
+    eo, fo = M.surrogate_energy_forces(pos, off, sur.C, sur.rc, sur.sigma,
+                                       pc['w1'], pc['b1'], pc['w2'], pc['b2'],
+                                       pc['w3'], pc['b3'], scale=3.0)
+    assert rel(e.cpu().numpy(), 3.0 * eo) < 1e-3
+    assert rel(f.cpu().numpy(), fo) < 3e-2, rel(f.cpu().numpy(), fo)
+
+
+def _au_potential(n_chains, n_atoms=200):
+    import torch
+    from pyiid_gb300 import debye
+    from pyiid_gb300.sampling import PDFPotential, experiment_grids
+    from pyiid_gb300.scatter_factors import species_tables
+    exp, qb, nb, rg = experiment_grids({'rmax': 20.0})
+    ref = S.fcc_nearest(4.08, n_atoms).astype(np.float32)
+    sp, tab, _ = species_tables([79] * n_atoms, qb, nb)
+    gobs = debye.pdf(debye.fq(ref, sp, tab, qb), qb, exp['rstep'], rg,
+                     exp['qmin']).cpu().numpy()
+    pot = PDFPotential([79] * n_atoms, gobs, {'rmax': 20.0}, conv=100.0,
+                       n_configs=n_chains)
+    xs = np.stack([S.displaced(ref, 0.05, 40 + c) for c in range(n_chains)])
+    return pot, xs
+
+
+def test_graph_iteration_equals_eager():
+    from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
+    pot, xs = _au_potential(4)
+    runs = []
+    for graph in (False, True):
+        sur = RBFMLPSurrogate(seed=1)
+        da = DelayedAcceptanceHMC(pot, sur, xs, temperature=300, dt=5e-3,
+                                  n_steps=5, seed=9, graph=graph)
+        da.step(4)
+        runs.append((da.x.cpu().numpy(), da.E.cpu().numpy(),
+                     da.accepted.cpu().numpy(), da.stage1.cpu().numpy()))
+        da.check()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
+
+
+def test_second_stage_uses_exact_energies():
+    """After every iteration the chains' energies are the exact potential of
+    their positions (stage 2 judged with exact energies), and accepted
+    moves moved the atoms."""
+    import torch
+    from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
+    pot, xs = _au_potential(6)
+    sur = RBFMLPSurrogate(seed=2)
+    da = DelayedAcceptanceHMC(pot, sur, xs, temperature=300, dt=5e-3,
+                              n_steps=5, seed=3)
+    x0 = da.x.clone()
+    da.step(5)
+    e = pot.evaluate(da.x, want_grad=False)[0]
+    assert torch.allclose(e, da.E, rtol=0, atol=1e-12)
+    moved = (da.x - x0).reshape(6, -1).abs().amax(1) > 0
+    assert torch.equal(moved, da.accepted > 0)
+    assert bool((da.accepted <= da.stage1).all())

@@ -71,3 +71,32 @@ def test_two_atom_descriptors_in_closed_form(d):
     assert np.allclose(f[0], want, rtol=1e-12, atol=1e-300)
     assert np.allclose(f[1], want, rtol=1e-12, atol=1e-300)
     assert np.all(f[2] == 0)   # no neighbour within the cutoff
+
+
+def test_surrogate_forces_are_minus_the_energy_gradient():
+    """The force formula of the surrogate oracle (descriptor derivatives of
+    both atoms of every pair, back-propagated MLP) against central
+    differences of its energy, all in FP64 (no BF16 rounding)."""
+    from oracle import mlp_np as M
+    rng = np.random.default_rng(5)
+    C, H, rc = 8, 16, 5.0
+    sig = rc / (C - 1)
+    w1 = rng.normal(size=(C, H)) / np.sqrt(C)
+    w2 = rng.normal(size=(H, H)) / np.sqrt(H)
+    b1, b2 = rng.normal(size=H) * .1, rng.normal(size=H) * .1
+    w3, b3 = rng.normal(size=H) * .3, np.array([0.2])
+    pos = rng.uniform(0, 6, (12, 3))
+    off = np.array([0, 7, 12])
+    e, f = M.surrogate_energy_forces(pos, off, C, rc, sig, w1, b1, w2, b2,
+                                     w3, b3, scale=2.5, rounded=False)
+    h = 1e-6
+    for a, c in ((0, 0), (3, 1), (8, 2), (11, 0)):
+        xp, xm = pos.copy(), pos.copy()
+        xp[a, c] += h
+        xm[a, c] -= h
+        ep = M.surrogate_energy_forces(xp, off, C, rc, sig, w1, b1, w2, b2,
+                                       w3, b3, rounded=False)[0].sum()
+        em = M.surrogate_energy_forces(xm, off, C, rc, sig, w1, b1, w2, b2,
+                                       w3, b3, rounded=False)[0].sum()
+        assert abs(-2.5 * (ep - em) / (2 * h) - f[a, c]) <= 1e-6 * max(
+            1.0, abs(f[a, c]))
