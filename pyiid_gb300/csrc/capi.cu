@@ -2286,6 +2286,9 @@ extern "C" int pyiid_surrogate_forces(
     return fail(ctx, PYIID_ERR_INVALID_ARG, "r_cut and sigma must be > 0");
   if (n_hidden < 1 || max_nb < 1)
     return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
+  if (forces && n_centres % 4 != 0)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "forces need n_centres divisible by 4 (got %d)", n_centres);
   const int n = offsets[n_configs];
   CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   int *d_cfg, *d_off;

@@ -303,10 +303,30 @@ __global__ void neighbor_list_kernel(const float *__restrict__ pos,
   if (lane == 0) count[a] = n;
 }
 
-// rbf_features_kernel over a neighbour list instead of every atom of the
-// configuration: the same terms added in the same (increasing b) order, so
-// the descriptors are bitwise those of the all-pairs kernel whenever the
-// list holds every atom within rc.
+// Warp reduce-scatter of 32 per-lane vectors acc[0..31]: afterwards lane l
+// holds sum over lanes of acc[l] in acc[0].  Five butterfly steps; at offset
+// o a lane keeps the half of its live entries selected by bit o of its index
+// and adds the partner's copy of that half (31 shuffles instead of 32 x 5).
+__device__ __forceinline__ float warp_reduce_scatter32(float (&acc)[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < o; ++i) {
+      const float send = up ? acc[i] : acc[i + o];
+      const float keep = up ? acc[i + o] : acc[i];
+      acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  return acc[0];
+}
+
+// rbf_features_kernel over a neighbour list: one warp per atom, lane l takes
+// the neighbours l, l + 32, ... (distance, cutoff and the C Gaussians per
+// pair computed once), then a reduce-scatter gives lane c the sum of centre
+// c (and c + 32 in a second pass when C > 32).  The same terms as the
+// all-pairs kernel, summed in another order.
 __global__ void rbf_features_nl_kernel(const float *__restrict__ pos,
                                        const int *__restrict__ nbr,
                                        const int *__restrict__ count,
@@ -322,28 +342,31 @@ __global__ void rbf_features_nl_kernel(const float *__restrict__ pos,
   const float ax = pos[3 * a], ay = pos[3 * a + 1], az = pos[3 * a + 2];
   const float step = rc / (float)(n_centres - 1);
   const float inv2s2 = 0.5f / (sigma * sigma);
-  const float mu0 = lane * step, mu1 = (lane + 32) * step;
   const float rc2 = rc * rc;
-  float acc0 = 0.f, acc1 = 0.f;
-  for (int i = 0; i < n; ++i) {
-    const int b = nb[i];
-    const float dx = pos[3 * b] - ax, dy = pos[3 * b + 1] - ay,
-                dz = pos[3 * b + 2] - az;
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 >= rc2) continue;
-    const float r = sqrtf(r2);
-    const float fc = 0.5f * (1.f + cospif(r / rc));
-    const float d0 = r - mu0, d1 = r - mu1;
-    acc0 = fmaf(fc, __expf(-d0 * d0 * inv2s2), acc0);
-    acc1 = fmaf(fc, __expf(-d1 * d1 * inv2s2), acc1);
-  }
-  if (lane < n_centres) {
-    fb[(size_t)a * n_centres + lane] = __float2bfloat16_rn(acc0);
-    if (ff) ff[(size_t)a * n_centres + lane] = acc0;
-  }
-  if (lane + 32 < n_centres) {
-    fb[(size_t)a * n_centres + lane + 32] = __float2bfloat16_rn(acc1);
-    if (ff) ff[(size_t)a * n_centres + lane + 32] = acc1;
+  for (int c0 = 0; c0 < n_centres; c0 += 32) {
+    float acc[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) acc[c] = 0.f;
+    for (int i = lane; i < n; i += 32) {
+      const int b = nb[i];
+      const float dx = pos[3 * b] - ax, dy = pos[3 * b + 1] - ay,
+                  dz = pos[3 * b + 2] - az;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 >= rc2) continue;
+      const float r = sqrtf(r2);
+      const float fc = 0.5f * (1.f + cospif(r / rc));
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const float d = r - (float)(c0 + c) * step;
+        acc[c] = fmaf(fc, __expf(-d * d * inv2s2), acc[c]);
+      }
+    }
+    const float v = warp_reduce_scatter32(acc);
+    const int c = c0 + lane;
+    if (c < n_centres) {
+      fb[(size_t)a * n_centres + c] = __float2bfloat16_rn(v);
+      if (ff) ff[(size_t)a * n_centres + c] = v;
+    }
   }
 }
 
@@ -368,8 +391,10 @@ __global__ void broadcast_rows_kernel(const float *__restrict__ v, int rows,
 //   phi_c'(r) = exp(-(r - mu_c)^2 / (2 s^2)) (fc'(r) - fc(r) (r - mu_c)/s^2),
 //   fc'(r) = -(pi / (2 rc)) sin(pi r / rc),
 // (the descriptor of b holds the pair too), forces[a] = -scale dE/dx_a.  One
-// warp per atom, lane = centre (and centre + 32); the x, y, z partial sums
-// are reduced over the warp once per atom.
+// warp per atom; lane l takes the neighbours l, l + 32, ... and loops over
+// the centres with g[a] in registers and g[b] read as float4; the x, y, z
+// sums are reduced over the warp once per atom.  n_centres % 4 == 0 and
+// n_centres <= 64.
 __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
                                      const int *__restrict__ nbr,
                                      const int *__restrict__ count,
@@ -386,14 +411,11 @@ __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
   const float step = rc / (float)(n_centres - 1);
   const float inv_s2 = 1.f / (sigma * sigma);
   const float inv2s2 = 0.5f * inv_s2;
-  const float mu0 = lane * step, mu1 = (lane + 32) * step;
-  const bool c0 = lane < n_centres, c1 = lane + 32 < n_centres;
-  const float ga0 = c0 ? g[(size_t)a * n_centres + lane] : 0.f;
-  const float ga1 = c1 ? g[(size_t)a * n_centres + lane + 32] : 0.f;
   const float rc2 = rc * rc;
   const float kfc = -0.5f * 3.14159265358979f / rc;
+  const float4 *ga4 = reinterpret_cast<const float4 *>(g + (size_t)a * n_centres);
   float fx = 0.f, fy = 0.f, fz = 0.f;
-  for (int i = 0; i < n; ++i) {
+  for (int i = lane; i < n; i += 32) {
     const int b = nb[i];
     const float dx = ax - pos[3 * b], dy = ay - pos[3 * b + 1],
                 dz = az - pos[3 * b + 2];
@@ -403,12 +425,19 @@ __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
     float sn, cs;
     sincospif(r / rc, &sn, &cs);
     const float fc = 0.5f * (1.f + cs), dfc = kfc * sn;
-    const float gb0 = c0 ? g[(size_t)b * n_centres + lane] : 0.f;
-    const float gb1 = c1 ? g[(size_t)b * n_centres + lane + 32] : 0.f;
-    const float d0 = r - mu0, d1 = r - mu1;
-    const float p0 = __expf(-d0 * d0 * inv2s2) * (dfc - fc * d0 * inv_s2);
-    const float p1 = __expf(-d1 * d1 * inv2s2) * (dfc - fc * d1 * inv_s2);
-    const float s = ((ga0 + gb0) * p0 + (ga1 + gb1) * p1) / r;
+    const float4 *gb4 =
+        reinterpret_cast<const float4 *>(g + (size_t)b * n_centres);
+    float s = 0.f;
+    for (int q = 0; q < n_centres / 4; ++q) {
+      const float4 u = ga4[q], w = gb4[q];
+      const float gs[4] = {u.x + w.x, u.y + w.y, u.z + w.z, u.w + w.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float d = r - (float)(4 * q + e) * step;
+        s = fmaf(gs[e], __expf(-d * d * inv2s2) * (dfc - fc * d * inv_s2), s);
+      }
+    }
+    s = s / r;
     fx = fmaf(s, dx, fx);
     fy = fmaf(s, dy, fy);
     fz = fmaf(s, dz, fz);

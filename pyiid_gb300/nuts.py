@@ -182,10 +182,11 @@ class NUTSEngine:
         self.v = torch.ones(B, **f)
         self.tab = torch.zeros((B, self.n_slots), **f)
         if find_step_size:
-            self.step = self.find_step_size()
+            self.step = self.find_step_size().clone()
         else:
             self.step = torch.full((B,), 0.5, **f)
         self.mu = torch.log(10 * self.step)
+        self._cap = 0
 
     # ------------------------------------------------------------ helpers
     def evaluate(self, x):
@@ -253,51 +254,122 @@ class NUTSEngine:
         return eps
 
     # ---------------------------------------------------------- iterations
-    def run(self, iterations):
+    def _ensure_run_buffers(self, its):
+        """Per-run random tables and the sample buffer, reused (and kept at
+        fixed addresses for a captured tick) while they are large enough."""
+        cap = getattr(self, '_cap', 0)
+        if its <= cap:
+            return
+        B, dev, dt = self.B, self.device, self.dtype
+        self._cap = its
+        self._normals = torch.zeros((its, B, self.N, 3), dtype=dt, device=dev)
+        self._tables = torch.zeros((its, B, self.n_slots), dtype=dt,
+                                   device=dev)
+        self._its = torch.zeros((), dtype=torch.int64, device=dev)
+        self._base = torch.zeros(B, dtype=torch.int64, device=dev)
+        self._target = torch.zeros(B, dtype=torch.int64, device=dev)
+        S = its * self.J
+        self._smp_x = torch.zeros((B, S, self.N, 3), dtype=dt, device=dev)
+        self._smp_U = torch.zeros((B, S), dtype=dt, device=dev)
+        self._smp_n = torch.zeros(B, dtype=torch.int64, device=dev)
+        self._graph = None
+
+    def run(self, iterations, graph=False):
         """Advance every chain by ``iterations`` iterations (chains that
-        finish first idle under the mask).  Returns the ticks taken."""
-        B, its, dev = self.B, int(iterations), self.device
+        finish first idle under the mask).  With ``graph`` (CUDA only) one
+        tick is captured once and replayed.  Returns the ticks taken."""
+        B, its = self.B, int(iterations)
         if its < 1:
             return 0
+        self._ensure_run_buffers(its)
         normals = np.empty((its, B, self.N, 3))
         tables = np.empty((its, B, self.n_slots))
         for c, rs in enumerate(self.rs):
             for t in range(its):
                 normals[t, c] = rs.standard_normal((self.N, 3))
                 tables[t, c] = rs.random_sample(self.n_slots)
-        self._normals = torch.as_tensor(normals, dtype=self.dtype, device=dev)
-        self._tables = torch.as_tensor(tables, dtype=self.dtype, device=dev)
-        self._base = self.iteration.clone()
-        self._target = self.iteration + its
-        self._start_iteration(torch.ones(B, dtype=torch.bool, device=dev))
+        self._normals[:its].copy_(torch.as_tensor(normals, dtype=self.dtype))
+        self._tables[:its].copy_(torch.as_tensor(tables, dtype=self.dtype))
+        self._its.fill_(its)
+        self._base.copy_(self.iteration)
+        self._target.copy_(self.iteration + its)
+        self._smp_n.zero_()
+        self._start_iteration(torch.ones(B, dtype=torch.bool,
+                                         device=self.device))
+        use_graph = graph and self.device.type == 'cuda'
+        if use_graph and self._graph is None:
+            self._capture_tick()
+        per_tick = 2 if self.reevaluate else 1
         ticks = 0
         while bool((self.iteration < self._target).any()):
-            self.tick()
+            if use_graph:
+                self._graph.replay()
+                self.evaluations += per_tick
+            else:
+                self.tick()
             ticks += 1
+        self._collect()
         return ticks
+
+    def _capture_tick(self):
+        """Capture one tick.  The warm-up tick runs on a side stream on a
+        copy of the state, which is then restored, so capturing consumes no
+        step of the chains."""
+        saved = self._state_tensors()
+        backup = [t.clone() for t in saved]
+        ev = self.evaluations
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.tick()
+        torch.cuda.current_stream().wait_stream(s)
+        for t, b in zip(saved, backup):
+            t.copy_(b)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.tick()
+        for t, b in zip(saved, backup):
+            t.copy_(b)
+        self.evaluations = ev
+        self._graph = g
+
+    def _state_tensors(self):
+        out = [self.x, self.U, self.F, self.hbar, self.m_it, self.iteration,
+               self.accepted, self.leapfrogs, self.samples_total,
+               self.first_x, self.first_p, self.prop_x, self.prop_F,
+               self.prop_U, self.stk_n, self.stk_s, self.stk_asum,
+               self.stk_na, self.H0, self.u, self.n_tot, self.j, self.leaf,
+               self.v, self.tab, self.step, self._smp_x, self._smp_U,
+               self._smp_n]
+        for d in (self.ex, self.ep, self.eF, self.eU, self.eH):
+            out.extend(d.values())
+        return out
 
     def _start_iteration(self, mask):
         """New momenta, slice variable and depth-0 tree for chains in mask."""
-        k = (self.iteration - self._base).clamp(0, self._tables.shape[0] - 1)
+        k = torch.minimum(self.iteration - self._base, self._its - 1
+                          ).clamp(min=0)
         tab = self._tables[k, self.ar]
         p = self._momenta(self._normals[k, self.ar])
         H = self.U + self.kinetic(p)
         m1, m3 = mask, mask[:, None, None]
-        self.tab = torch.where(mask[:, None], tab, self.tab)
-        self.H0 = torch.where(m1, H, self.H0)
-        self.u = torch.where(m1, tab[:, 0], self.u)
-        self.n_tot = torch.where(m1, torch.ones_like(self.n_tot), self.n_tot)
-        self.j = torch.where(m1, torch.zeros_like(self.j), self.j)
-        self.leaf = torch.where(m1, torch.zeros_like(self.leaf), self.leaf)
+        self.tab.copy_(torch.where(mask[:, None], tab, self.tab))
+        self.H0.copy_(torch.where(m1, H, self.H0))
+        self.u.copy_(torch.where(m1, tab[:, 0], self.u))
+        self.n_tot.copy_(torch.where(m1, torch.ones_like(self.n_tot),
+                                     self.n_tot))
+        self.j.copy_(torch.where(m1, torch.zeros_like(self.j), self.j))
+        self.leaf.copy_(torch.where(m1, torch.zeros_like(self.leaf),
+                                    self.leaf))
         v0 = torch.where(tab[:, slot_direction(self.J, 0)] < 0.5, -1.0, 1.0
                          ).to(self.dtype)
-        self.v = torch.where(m1, v0, self.v)
+        self.v.copy_(torch.where(m1, v0, self.v))
         for s in ('neg', 'pos', 'front'):
-            self.ex[s] = torch.where(m3, self.x, self.ex[s])
-            self.ep[s] = torch.where(m3, p, self.ep[s])
-            self.eF[s] = torch.where(m3, self.F, self.eF[s])
-            self.eU[s] = torch.where(m1, self.U, self.eU[s])
-            self.eH[s] = torch.where(m1, H, self.eH[s])
+            self.ex[s].copy_(torch.where(m3, self.x, self.ex[s]))
+            self.ep[s].copy_(torch.where(m3, p, self.ep[s]))
+            self.eF[s].copy_(torch.where(m3, self.F, self.eF[s]))
+            self.eU[s].copy_(torch.where(m1, self.U, self.eU[s]))
+            self.eH[s].copy_(torch.where(m1, H, self.eH[s]))
 
     def tick(self):
         """One leapfrog step of every active chain and the tree updates."""
@@ -378,12 +450,12 @@ class NUTSEngine:
         self.stk_na[lvl, ar] = torch.where(st, na, self.stk_na[lvl, ar])
         # the leaf is the new front of every active chain
         a1, a3 = act, act[:, None, None]
-        self.ex['front'] = torch.where(a3, x1, fx)
-        self.ep['front'] = torch.where(a3, p1, fp)
-        self.eF['front'] = torch.where(a3, F1, fF)
-        self.eU['front'] = torch.where(a1, U1, self.eU['front'])
-        self.eH['front'] = torch.where(a1, H1, fH)
-        self.leaf = torch.where(act & ~done, self.leaf + 1, self.leaf)
+        self.ex['front'].copy_(torch.where(a3, x1, fx))
+        self.ep['front'].copy_(torch.where(a3, p1, fp))
+        self.eF['front'].copy_(torch.where(a3, F1, fF))
+        self.eU['front'].copy_(torch.where(a1, U1, self.eU['front']))
+        self.eH['front'].copy_(torch.where(a1, H1, fH))
+        self.leaf.copy_(torch.where(act & ~done, self.leaf + 1, self.leaf))
         self._finish_subtree(done, n, s, asum, na, pidx)
 
     def _finish_subtree(self, done, n, s, asum, na, pidx):
@@ -396,24 +468,29 @@ class NUTSEngine:
         pF = self.prop_F[pidx, ar]
         self._record(take, px, pU)
         t3 = take[:, None, None]
-        self.x = torch.where(t3, px, self.x)
-        self.U = torch.where(take, pU, self.U)
-        self.F = torch.where(t3, pF, self.F)
+        self.x.copy_(torch.where(t3, px, self.x))
+        self.U.copy_(torch.where(take, pU, self.U))
+        self.F.copy_(torch.where(t3, pF, self.F))
         self.accepted += take.to(torch.int64)
-        self.n_tot = torch.where(done, self.n_tot + n, self.n_tot)
+        self.n_tot.copy_(torch.where(done, self.n_tot + n, self.n_tot))
         # the doubling extended the tree on side v: that edge is the front
         for side, msk in (('neg', done & (self.v < 0)),
                           ('pos', done & (self.v > 0))):
             m3 = msk[:, None, None]
-            self.ex[side] = torch.where(m3, self.ex['front'], self.ex[side])
-            self.ep[side] = torch.where(m3, self.ep['front'], self.ep[side])
-            self.eF[side] = torch.where(m3, self.eF['front'], self.eF[side])
-            self.eU[side] = torch.where(msk, self.eU['front'], self.eU[side])
-            self.eH[side] = torch.where(msk, self.eH['front'], self.eH[side])
+            self.ex[side].copy_(torch.where(m3, self.ex['front'],
+                                            self.ex[side]))
+            self.ep[side].copy_(torch.where(m3, self.ep['front'],
+                                            self.ep[side]))
+            self.eF[side].copy_(torch.where(m3, self.eF['front'],
+                                            self.eF[side]))
+            self.eU[side].copy_(torch.where(msk, self.eU['front'],
+                                            self.eU[side]))
+            self.eH[side].copy_(torch.where(msk, self.eH['front'],
+                                            self.eH[side]))
         span = (self.ex['pos'] - self.ex['neg']).flatten(1)
         ok = (((span * (self.ep['neg'] / self.masses).flatten(1)).sum(1) >= 0) &
               ((span * (self.ep['pos'] / self.masses).flatten(1)).sum(1) >= 0))
-        self.j = torch.where(done, self.j + 1, self.j)
+        self.j.copy_(torch.where(done, self.j + 1, self.j))
         self.samples_total += torch.where(done, 2 ** self.j,
                                           torch.zeros_like(self.j))
         s_new = s & ok & (self.j < J)
@@ -421,35 +498,56 @@ class NUTSEngine:
         # next doubling: the direction of depth j, from that side's edge
         vj = torch.where(
             self.tab[ar, (1 + self.j).clamp(max=J)] < 0.5, -1.0, 1.0).to(dt)
-        self.v = torch.where(cont, vj, self.v)
-        self.leaf = torch.where(done, torch.zeros_like(self.leaf), self.leaf)
+        self.v.copy_(torch.where(cont, vj, self.v))
+        self.leaf.copy_(torch.where(done, torch.zeros_like(self.leaf),
+                                    self.leaf))
         back = (cont & (self.v < 0))
         fwd = (cont & (self.v > 0))
         for msk, side in ((back, 'neg'), (fwd, 'pos')):
             m3 = msk[:, None, None]
-            self.ex['front'] = torch.where(m3, self.ex[side], self.ex['front'])
-            self.ep['front'] = torch.where(m3, self.ep[side], self.ep['front'])
-            self.eF['front'] = torch.where(m3, self.eF[side], self.eF['front'])
-            self.eU['front'] = torch.where(msk, self.eU[side], self.eU['front'])
-            self.eH['front'] = torch.where(msk, self.eH[side], self.eH['front'])
+            self.ex['front'].copy_(torch.where(m3, self.ex[side],
+                                               self.ex['front']))
+            self.ep['front'].copy_(torch.where(m3, self.ep[side],
+                                               self.ep['front']))
+            self.eF['front'].copy_(torch.where(m3, self.eF[side],
+                                               self.eF['front']))
+            self.eU['front'].copy_(torch.where(msk, self.eU[side],
+                                               self.eU['front']))
+            self.eH['front'].copy_(torch.where(msk, self.eH[side],
+                                               self.eH['front']))
         # iteration over: dual averaging on the last subtree's statistic
         over = done & ~s_new
         mf = self.m_it.to(dt)
         w = 1.0 / (mf + self.t0)
         hbar = (1 - w) * self.hbar + w * (self.accept_target - asum / na)
         step = torch.exp(self.mu - (torch.sqrt(mf) / self.gamma) * hbar)
-        self.hbar = torch.where(over, hbar, self.hbar)
-        self.step = torch.where(over, step, self.step)
-        self.m_it = self.m_it + over.to(torch.int64)
-        self.iteration = self.iteration + over.to(torch.int64)
+        self.hbar.copy_(torch.where(over, hbar, self.hbar))
+        self.step.copy_(torch.where(over, step, self.step))
+        self.m_it += over.to(torch.int64)
+        self.iteration += over.to(torch.int64)
         again = over & (self.iteration < self._target)
         self._start_iteration(again)
 
     def _record(self, take, px, pU):
-        if bool(take.any()):
-            for c in torch.nonzero(take).flatten().tolist():
-                self.samples[c].append(px[c].clone())
-                self.sample_energies[c].append(float(pU[c]))
+        """Accepted proposals into the per-run sample buffer (device)."""
+        ar = self.ar
+        i = self._smp_n.clamp(max=self._smp_x.shape[1] - 1)
+        t3 = take[:, None, None]
+        self._smp_x[ar, i] = torch.where(t3, px, self._smp_x[ar, i])
+        self._smp_U[ar, i] = torch.where(take, pU, self._smp_U[ar, i])
+        self._smp_n += take.to(torch.int64)
+
+    def _collect(self):
+        """Move the run's samples into the per-chain lists."""
+        counts = self._smp_n.cpu().tolist()
+        if not any(counts):
+            return
+        xs = self._smp_x.cpu()
+        us = self._smp_U.cpu()
+        for c, k in enumerate(counts):
+            for i in range(k):
+                self.samples[c].append(xs[c, i].clone())
+                self.sample_energies[c].append(float(us[c, i]))
 
 
 class _ChainView:
@@ -492,8 +590,10 @@ class BatchedNUTS:
     potential is translation invariant)."""
 
     def __init__(self, pot, starts, temperature=300.0, seeds=None,
-                 escape_level=13, accept_target=0.65, exact=True):
+                 escape_level=13, accept_target=0.65, exact=True,
+                 graph=True):
         self.pot = pot
+        self.graph = bool(graph)
         B = pot.n_configs
         starts = np.asarray(starts, np.float64).reshape(B, -1, 3)
         masses = np.asarray(pot.masses, np.float64).reshape(B, -1)
@@ -523,7 +623,7 @@ class BatchedNUTS:
         return self.engine.evaluations
 
     def step(self, iterations=1):
-        return self.engine.run(iterations)
+        return self.engine.run(iterations, graph=self.graph)
 
     def energies(self):
         return self.engine.U.cpu().numpy()

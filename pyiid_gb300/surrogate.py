@@ -343,7 +343,13 @@ class DelayedAcceptanceHMC:
     with the exact Debye potential (energy only, ``pyiid_batch_potential_grad``
     without gradient) in stage 2, so the chain's target is the exact one
     whatever the surrogate's quality; a poor surrogate costs acceptance, not
-    correctness.  The exact potential is evaluated once per iteration (at
+    correctness.  The surrogate change H~' - H~ is the kinetic change plus
+    the work of the surrogate's forces along the trajectory (trapezoid rule
+    over the leapfrog points): for steps of 1e-3 A the BF16 energies
+    themselves change by less than their rounding, while the work is smooth.
+    Any stage-1 quantity that changes sign when the trajectory is reversed
+    keeps delayed acceptance exact (the stage-2 ratio divides it out), and
+    the work does.  The exact potential is evaluated once per iteration (at
     the trajectory's end), against once per leapfrog step in BatchedHMC.
 
     The neighbour lists are built at the start of every trajectory with
@@ -400,6 +406,7 @@ class DelayedAcceptanceHMC:
         self.max_disp = torch.zeros((), dtype=torch.float32, device=d)
         self.max_cnt = torch.zeros((), dtype=torch.int32, device=d)
         self.sum_dhs_err = torch.zeros((), dtype=torch.float64, device=d)
+        self.sum_work_err = torch.zeros((), dtype=torch.float64, device=d)
         self.proposed = 0
         # replay buffer of exact (configuration, Rw) pairs (equal-size chains)
         self.buf_size = int(buffer_size) if self.n_per else 0
@@ -456,22 +463,30 @@ class DelayedAcceptanceHMC:
         self._neighbours(x0)
         self.max_cnt.copy_(torch.maximum(self.max_cnt, self.cnt.max()))
         s0, f = self.surrogate(x0)
-        s0 = s0.clone()
+        s0, f = s0.clone(), f.clone()
         p = torch.randn(x0.shape, generator=self.gen,
                         device=x0.device) * torch.sqrt(self.m * self.kT)
         k0 = self._kinetic(p)
         x = x0
         p = p + 0.5 * dt * f
         disp = torch.zeros((), dtype=torch.float32, device=x0.device)
+        work = torch.zeros(self.B, dtype=torch.float64, device=x0.device)
         for i in range(self.n_steps):
-            x = x + dt * p / self.m
+            dx = dt * p / self.m
+            x = x + dx
             disp = torch.maximum(disp, (x - x0).norm(dim=1).max())
-            s1, f = self.surrogate(x)
+            s1, f1 = self.surrogate(x)
+            # the surrogate's energy change along the path (trapezoid rule
+            # on its forces): smooth where the BF16 energies are not, and
+            # odd under reversal of the trajectory
+            w_atom = -0.5 * ((f + f1) * dx).double().sum(1)
+            work.index_add_(0, self.cfg, w_atom)
+            f = f1.clone()
             if i + 1 < self.n_steps:
                 p = p + dt * f
         p = p + 0.5 * dt * f
         k1 = self._kinetic(p)
-        dhs = (s1 - s0) + (k1 - k0)
+        dhs = work + (k1 - k0)
         e1 = self.pot.evaluate(x, want_grad=False)[0]
         dh = (e1 - self.E) + (k1 - k0)
         logu = torch.log(torch.rand((2, self.B), generator=self.gen,
@@ -485,6 +500,7 @@ class DelayedAcceptanceHMC:
         self.stage1 += st1.to(torch.int64)
         self.max_disp.copy_(torch.maximum(self.max_disp, disp))
         self.sum_dhs_err += ((dh - dhs) ** 2).sum()
+        self.sum_work_err += ((s1 - s0 - work) ** 2).sum()
         if self.buf_size:
             idx = (self.buf_ptr + torch.arange(self.B, device=x.device)
                    ) % self.buf_size
@@ -496,12 +512,15 @@ class DelayedAcceptanceHMC:
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         state = (self.x.clone(), self.E.clone())
+        rng = self.gen.get_state()
         with torch.cuda.stream(s):
             for _ in range(2):      # warm layouts, workspaces and buffers
                 self._iteration()
         torch.cuda.current_stream().wait_stream(s)
+        # the warm-up consumed no step of the chains
         self.x.copy_(state[0])
         self.E.copy_(state[1])
+        self.gen.set_state(rng)
         self._reset_counters()
         self.graph = torch.cuda.CUDAGraph()
         if hasattr(self.graph, 'register_generator_state'):
@@ -515,6 +534,7 @@ class DelayedAcceptanceHMC:
         self.max_disp.zero_()
         self.max_cnt.zero_()
         self.sum_dhs_err.zero_()
+        self.sum_work_err.zero_()
         self.buf_ptr.zero_()
         self.proposed = 0
         self.buf_n = 0

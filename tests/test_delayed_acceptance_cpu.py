@@ -85,6 +85,7 @@ def test_delayed_acceptance_hmc_keeps_the_exact_target():
             self.cnt = torch.zeros(self.N, dtype=torch.int32)
             self.max_disp = torch.zeros(())
             self.sum_dhs_err = torch.zeros((), dtype=torch.float64)
+            self.sum_work_err = torch.zeros((), dtype=torch.float64)
             self.buf_size, self.buf_n, self.proposed = 0, 0, 0
             self.graph = None
 
