@@ -2249,6 +2249,21 @@ int sf_config_map(pyiid_ctx *ctx, const int32_t *offsets, int n_configs,
 
 }  // namespace
 
+// the fused MLP kernel's dynamic shared memory exceeds the 48 KB default:
+// raise its limit once per device
+int fused_mlp_attr(pyiid_ctx *ctx) {
+  static std::mutex mu;
+  static bool done[64] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  if (ctx->device >= 0 && ctx->device < 64 && done[ctx->device])
+    return PYIID_OK;
+  CUDA_TRY(ctx, cudaFuncSetAttribute(mlp_fused_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(FusedMlpSmem)));
+  if (ctx->device >= 0 && ctx->device < 64) done[ctx->device] = true;
+  return PYIID_OK;
+}
+
 extern "C" int pyiid_neighbor_list(pyiid_ctx *ctx, const float *positions,
                                    const int32_t *offsets, int n_configs,
                                    float r_list, int max_nb, int32_t *nbr_idx,
@@ -2322,6 +2337,27 @@ extern "C" int pyiid_surrogate_forces(
   const __nv_bfloat16 *W2 = static_cast<const __nv_bfloat16 *>(w2_bf16);
   const int warps = 8;
   const int wgrid = (std::max(n, 1) + warps - 1) / warps;
+  if (n > 0 && C == kFC && H == kFH) {
+    // the 32-128-128 net: one fused kernel for y and dE/dfeat
+    rbf_features_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
+        positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, X, nullptr);
+    LAUNCH_CHECK(ctx);
+    TRY(fused_mlp_attr(ctx));
+    const int blocks = std::min((n + 63) / 64, 2 * std::max(1, ctx->n_sms));
+    mlp_fused_kernel<<<blocks, 128, sizeof(FusedMlpSmem), ctx->stream>>>(
+        X, n, W1, b1, W2, b2, w3, b3, y, gx);
+    LAUNCH_CHECK(ctx);
+    reduce_by_config_kernel<<<n_configs, 256, 0, ctx->stream>>>(
+        y, d_off, n_configs, energy);
+    LAUNCH_CHECK(ctx);
+    if (forces) {
+      rbf_forces_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
+          positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, gx, scale,
+          forces);
+      LAUNCH_CHECK(ctx);
+    }
+    return PYIID_OK;
+  }
   if (n > 0) {
     rbf_features_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
         positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, X, nullptr);

@@ -454,6 +454,213 @@ __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
   }
 }
 
+// ------------------------------------------- fused MLP for the 32-128-128 net
+// Forward and descriptor gradient of the per-atom MLP for n_in = 32,
+// n_hidden = 128 in one kernel:
+//   z1 = X W1 + b1, h1 = silu(z1), z2 = h1 W2 + b2, y = silu(z2) . w3 + b3,
+//   g = dE/dX = ((w3 * silu'(z2)) W2^T * silu'(z1)) W1^T   (E = sum_a y_a).
+// A warp owns 16 atoms; every product is an mma.sync m16n8k16 (BF16 in,
+// FP32 accumulate) and the activations never leave registers: the FP32
+// accumulator fragments of one layer, rounded to BF16 and paired, are
+// exactly the A fragments of the next (C frag (g, 2q..2q+1) / (g+8, ..)
+// of column tiles 2t and 2t+1 = A frag of k-tile t).  z1 is recomputed tile
+// by tile in the backward pass instead of being kept.  The four weight
+// layouts the B fragments need (consecutive k in one 32-bit word) are staged
+// once per CTA in shared memory with padded rows (conflict-free loads); CTAs
+// stay resident and loop over atom blocks.  y is written per atom (summed
+// per configuration by reduce_by_config_kernel) and g as FP32 [n][32].
+constexpr int kFC = 32, kFH = 128;
+constexpr int kLd1 = kFC + 8;   // rows of 32 (+8 pad) bf16: W1T [h][c]
+constexpr int kLd2 = kFH + 8;   // rows of 128 (+8 pad): W2T, W2, W1
+struct FusedMlpSmem {
+  __nv_bfloat16 w1t[kFH * kLd1];  // B of layer 1:  [h][c]
+  __nv_bfloat16 w2t[kFH * kLd2];  // B of layer 2:  [o][i]
+  __nv_bfloat16 w2[kFH * kLd2];   // B of dh1:      [i][o]
+  __nv_bfloat16 w1[kFC * kLd2];   // B of g:        [c][h]
+  float b1[kFH], b2[kFH], w3[kFH];
+};
+
+__device__ __forceinline__ unsigned pack2f(float lo, float hi) {
+  return pack_bf16(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
+}
+__device__ __forceinline__ float silu_f(float x) {
+  return x / (1.f + __expf(-x));
+}
+__device__ __forceinline__ float dsilu_f(float x) {
+  const float s = 1.f / (1.f + __expf(-x));
+  return s * (1.f + x * (1.f - s));
+}
+__device__ __forceinline__ unsigned ld_u32(const __nv_bfloat16 *p) {
+  return *reinterpret_cast<const unsigned *>(p);
+}
+
+__global__ void __launch_bounds__(128, 2)
+    mlp_fused_kernel(const __nv_bfloat16 *__restrict__ X, int n_atoms,
+                     const __nv_bfloat16 *__restrict__ W1,
+                     const float *__restrict__ b1,
+                     const __nv_bfloat16 *__restrict__ W2,
+                     const float *__restrict__ b2,
+                     const float *__restrict__ w3, const float *__restrict__ b3,
+                     float *__restrict__ y, float *__restrict__ gout) {
+  extern __shared__ __align__(16) unsigned char fused_smem[];
+  FusedMlpSmem &S = *reinterpret_cast<FusedMlpSmem *>(fused_smem);
+  const int tid = threadIdx.x;
+  // stage the weights: W1 [c][h], W2 [i][o] row-major in global memory
+  for (int e = tid; e < kFC * kFH; e += blockDim.x) {
+    const int c = e / kFH, h = e % kFH;
+    const __nv_bfloat16 v = W1[e];
+    S.w1[c * kLd2 + h] = v;
+    S.w1t[h * kLd1 + c] = v;
+  }
+  for (int e = tid; e < kFH * kFH; e += blockDim.x) {
+    const int i = e / kFH, o = e % kFH;
+    const __nv_bfloat16 v = W2[e];
+    S.w2[i * kLd2 + o] = v;
+    S.w2t[o * kLd2 + i] = v;
+  }
+  for (int e = tid; e < kFH; e += blockDim.x) {
+    S.b1[e] = b1[e];
+    S.b2[e] = b2[e];
+    S.w3[e] = w3[e];
+  }
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, q = lane & 3;
+  const float bias3 = b3[0];
+  const int n_blocks = (n_atoms + 15) / 16;
+  for (int blk = blockIdx.x * 4 + warp; blk < n_blocks;
+       blk += gridDim.x * 4) {
+    const int r0 = blk * 16;
+    const int ra = r0 + g, rb = r0 + g + 8;
+    const bool va = ra < n_atoms, vb = rb < n_atoms;
+    // A fragments of X (2 k-tiles of 16 descriptors)
+    unsigned xa[2][4];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int k = 16 * t + 2 * q;
+      xa[t][0] = va ? ld_u32(X + (size_t)ra * kFC + k) : 0u;
+      xa[t][1] = vb ? ld_u32(X + (size_t)rb * kFC + k) : 0u;
+      xa[t][2] = va ? ld_u32(X + (size_t)ra * kFC + k + 8) : 0u;
+      xa[t][3] = vb ? ld_u32(X + (size_t)rb * kFC + k + 8) : 0u;
+    }
+    // layer 1: z1 [16 x 128] -> h1 as A fragments (8 k-tiles)
+    unsigned h1[8][4];
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const __nv_bfloat16 *p0 = S.w1t + (8 * j + g) * kLd1 + 16 * t + 2 * q;
+        const __nv_bfloat16 *p1 = p0 + 8 * kLd1;
+        const unsigned bb0[2] = {ld_u32(p0), ld_u32(p0 + 8)};
+        const unsigned bb1[2] = {ld_u32(p1), ld_u32(p1 + 8)};
+        mma_bf16_16816(c0, xa[t], bb0);
+        mma_bf16_16816(c1, xa[t], bb1);
+      }
+      const int n0 = 8 * j + 2 * q, n1 = n0 + 8;
+      h1[j / 2][0] = pack2f(silu_f(c0[0] + S.b1[n0]), silu_f(c0[1] + S.b1[n0 + 1]));
+      h1[j / 2][1] = pack2f(silu_f(c0[2] + S.b1[n0]), silu_f(c0[3] + S.b1[n0 + 1]));
+      h1[j / 2][2] = pack2f(silu_f(c1[0] + S.b1[n1]), silu_f(c1[1] + S.b1[n1 + 1]));
+      h1[j / 2][3] = pack2f(silu_f(c1[2] + S.b1[n1]), silu_f(c1[3] + S.b1[n1 + 1]));
+    }
+    // layer 2 (z2 kept for the backward pass), output y
+    float z2[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) z2[j][e] = 0.f;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const __nv_bfloat16 *p = S.w2t + (8 * j + g) * kLd2 + 16 * t + 2 * q;
+        const unsigned bb[2] = {ld_u32(p), ld_u32(p + 8)};
+        mma_bf16_16816(z2[j], h1[t], bb);
+      }
+    }
+    float ya = 0.f, yb = 0.f;
+    unsigned dz2[8][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int n = 8 * j + 2 * q;
+      float d[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int col = n + (e & 1);
+        const float z = z2[j][e] + S.b2[col];
+        const float w = S.w3[col];
+        if (e < 2) ya = fmaf(silu_f(z), w, ya); else yb = fmaf(silu_f(z), w, yb);
+        d[e] = w * dsilu_f(z);
+      }
+      if ((j & 1) == 0) {
+        dz2[j / 2][0] = pack2f(d[0], d[1]);
+        dz2[j / 2][1] = pack2f(d[2], d[3]);
+      } else {
+        dz2[j / 2][2] = pack2f(d[0], d[1]);
+        dz2[j / 2][3] = pack2f(d[2], d[3]);
+      }
+    }
+    ya += __shfl_xor_sync(0xffffffffu, ya, 1);
+    ya += __shfl_xor_sync(0xffffffffu, ya, 2);
+    yb += __shfl_xor_sync(0xffffffffu, yb, 1);
+    yb += __shfl_xor_sync(0xffffffffu, yb, 2);
+    if (q == 0) {
+      if (va) y[ra] = ya + bias3;
+      if (vb) y[rb] = yb + bias3;
+    }
+    // dh1 = dz2 W2^T, then dz1 = dh1 * silu'(z1) (z1 recomputed per tile),
+    // packed as A fragments of the last product
+    unsigned dz1[8][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const __nv_bfloat16 *p = S.w2 + (8 * j + g) * kLd2 + 16 * t + 2 * q;
+        const unsigned bb[2] = {ld_u32(p), ld_u32(p + 8)};
+        mma_bf16_16816(acc, dz2[t], bb);
+      }
+      float z1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const __nv_bfloat16 *p = S.w1t + (8 * j + g) * kLd1 + 16 * t + 2 * q;
+        const unsigned bb[2] = {ld_u32(p), ld_u32(p + 8)};
+        mma_bf16_16816(z1, xa[t], bb);
+      }
+      const int n = 8 * j + 2 * q;
+      float d[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        d[e] = acc[e] * dsilu_f(z1[e] + S.b1[n + (e & 1)]);
+      if ((j & 1) == 0) {
+        dz1[j / 2][0] = pack2f(d[0], d[1]);
+        dz1[j / 2][1] = pack2f(d[2], d[3]);
+      } else {
+        dz1[j / 2][2] = pack2f(d[0], d[1]);
+        dz1[j / 2][3] = pack2f(d[2], d[3]);
+      }
+    }
+    // g = dz1 W1^T  [16 x 32]
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const __nv_bfloat16 *p = S.w1 + (8 * j + g) * kLd2 + 16 * t + 2 * q;
+        const unsigned bb[2] = {ld_u32(p), ld_u32(p + 8)};
+        mma_bf16_16816(acc, dz1[t], bb);
+      }
+      const int c = 8 * j + 2 * q;
+      if (va) {
+        gout[(size_t)ra * kFC + c] = acc[0];
+        gout[(size_t)ra * kFC + c + 1] = acc[1];
+      }
+      if (vb) {
+        gout[(size_t)rb * kFC + c] = acc[2];
+        gout[(size_t)rb * kFC + c + 1] = acc[3];
+      }
+    }
+  }
+}
+
 __global__ void to_bf16_kernel(const float *__restrict__ x, size_t n,
                                __nv_bfloat16 *__restrict__ y) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;

@@ -121,3 +121,19 @@ def test_reference_arm_line_follows_the_contract(monkeypatch):
     assert line['measured_full_evaluations']['n1000']['extrapolated'] is False
     # both arms share one config block
     assert line['config'] == bench.config_dict(1500, 25)
+
+
+def test_ess_estimator_on_known_processes():
+    """Geyer's initial positive sequence: white noise keeps about T samples
+    per chain, an AR(1) chain with rho = 0.9 about T (1 - rho) / (1 + rho)."""
+    import bench
+    rng = np.random.default_rng(0)
+    T, B = 4000, 4
+    w = rng.normal(size=(T, B))
+    assert 0.8 * T < bench.ess_sum(w) / B < 1.2 * T
+    x = np.zeros((T, B))
+    for t in range(1, T):
+        x[t] = 0.9 * x[t - 1] + rng.normal(size=B)
+    want = T * 0.1 / 1.9
+    assert 0.7 * want < bench.ess_sum(x) / B < 1.3 * want
+    assert bench.ess_sum(np.ones((10, 2))) == 0.0

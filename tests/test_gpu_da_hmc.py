@@ -79,10 +79,14 @@ def _weights(sur, seed):
                             .to('cuda') * 0.1)
 
 
-def test_surrogate_energy_and_forces_match_oracle():
+@pytest.mark.parametrize('centres,hidden', [(32, 128), (16, 64)],
+                         ids=['fused-32-128', 'gemm-16-64'])
+def test_surrogate_energy_and_forces_match_oracle(centres, hidden):
+    """The 32-128-128 net runs the fused kernel, other sizes the GEMM
+    chain; both against the oracle."""
     import torch
     from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
-    sur = RBFMLPSurrogate(seed=5)
+    sur = RBFMLPSurrogate(n_centres=centres, n_hidden=hidden, seed=5)
     _weights(sur, 6)
     pos, off = _batch()
     pt = torch.as_tensor(pos, device='cuda')
