@@ -955,7 +955,7 @@ def run_delayed_acceptance(torch, iters=30, pool=256, pretrain_steps=300):
             rws.append((e / pot.conv).cpu().numpy())
             if train_every and (i + 1) % train_every == 0:
                 t = time.perf_counter()
-                sampler.train(steps=20, batch=64)
+                sampler.train(steps=4, batch=32)
                 torch.cuda.synchronize()
                 ms += 1e3 * (time.perf_counter() - t)
         return ms * 1e-3, np.array(rws)
@@ -989,8 +989,9 @@ def run_delayed_acceptance(torch, iters=30, pool=256, pretrain_steps=300):
                      'ess_rw_per_s': ess_sum(tr) / s,
                      'rms_stage2_log_ratio_kT': float(
                          (da.sum_dhs_err / (iters * 64)).sqrt()) / da.kT,
-                     'online_training': (f'20 Adam steps every {every} '
-                                         'iterations (timed)') if every
+                     'online_training': (f'4 Adam steps on 32 buffered '
+                                         f'pairs every {every} iterations '
+                                         '(timed)') if every
                      else 'none',
                      'exact_evaluations_per_iteration': '1 energy only',
                      'lists': da.check()}

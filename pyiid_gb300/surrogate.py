@@ -563,18 +563,20 @@ class DelayedAcceptanceHMC:
         return {'max_neighbours': mc, 'max_displacement': md}
 
     def train(self, steps=1, batch=32):
-        """Adam steps on random exact (configuration, Rw) pairs of the
-        replay buffer; the iteration then uses the new weights."""
+        """``steps`` Adam steps on one random batch of exact (configuration,
+        Rw) pairs of the replay buffer (descriptors computed once for the
+        batch); the iteration then uses the new weights."""
         if self.buf_n < 2:
             return None
         b = min(int(batch), self.buf_n)
         off = (np.arange(b + 1) * self.n_per).astype(np.int32)
+        idx = torch.randint(0, self.buf_n, (b,), generator=self.gen,
+                            device=self.x.device)
+        fb = self.sur.features(self.buf_x[idx].reshape(-1, 3), off)
+        target = self.buf_e[idx]
         loss = None
         for _ in range(int(steps)):
-            idx = torch.randint(0, self.buf_n, (b,), generator=self.gen,
-                                device=self.x.device)
-            fb = self.sur.features(self.buf_x[idx].reshape(-1, 3), off)
-            loss = self.sur.train_step(fb, off, self.buf_e[idx])
+            loss = self.sur.train_step(fb, off, target)
         self.refresh_weights()
         return loss
 
