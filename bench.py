@@ -697,6 +697,20 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
     cpu = 1.0 / float(np.mean(t))
     gpu = 1e3 / ms
     single = single_config_au1000(torch)
+    # the one-pass kernel's FP32 issue roofline at this size: lane operations
+    # of its inner loop (8.5 per ordered pair-bin) over 152 SMs x 128 lanes
+    # at the maximum SM clock, with the whole call's time (kernel, part
+    # combine and finish)
+    k_ret = n_bins - k_begin
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    lane_peak = sms * FP32_LANES_PER_SM * 2.07e9 / 1e12
+    lane = 2 * pairs * k_ret * (LANE_OPS_GRAD_LOOP + 0.5) / (ms * 1e-3) / 1e12
+    roof = {'bound': 'fp32 issue', 'kernel': 'fqgrad2_kernel',
+            'achieved': lane, 'peak': lane_peak, 'unit': 'T lane-op/s',
+            'frac': lane / lane_peak,
+            'peak_source': f'{sms} SMs x {FP32_LANES_PER_SM} lanes x 2070 MHz',
+            'flop_eq_tflops': pairs * k_ret * (FLOPS_GRAD_TERM +
+                                               FLOPS_F_TERM) / (ms * 1e-3) / 1e12}
     return {'workload': '1000-atom fcc Au, exact F(Q) + full dF/dx, '
                         'Q 0.1-25 step 0.05 (498 bins returned)',
             'pairs': pairs, 'ms_per_eval': ms, 'evals_per_s': gpu,
@@ -715,6 +729,7 @@ def _run_fq_grad_au1000(torch, reps, cpu_reps):
                                    'warm-up'},
             'gpu_over_cpu_port': gpu / cpu,
             'e2e_over_cpu_port': 1e3 / e2e_ms / cpu,
+            'roofline': roof,
             'single_configuration': single}
 
 
@@ -872,12 +887,27 @@ def _run_hmc(torch, iters):
         pot.evaluate(x)
     e1.record()
     e1.synchronize()
+    ev_ms = e0.elapsed_time(e1) / 3
+    # one evaluation = F(Q) of the 64 configurations (3 lane-ops per unordered
+    # pair-bin) + the symmetric adjoint (5 lane-ops per unordered pair-bin)
+    # on the PDF grid
+    k_pdf = pot.n_bins
+    pairs64 = 64 * 1000 * 999 // 2
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    lane_peak = sms * FP32_LANES_PER_SM * 2.07e9 / 1e12
+    lane = pairs64 * k_pdf * (3 + 5) / (ev_ms * 1e-3) / 1e12
     return {'workload': '1000-atom fcc Au, 64 chains, 10 leapfrog x dt 1e-3, 300 K, E = 100 Rw',
+            'roofline': {'bound': 'fp32 issue',
+                         'kernel': 'fq_pair3_kernel + adjoint_sym_kernel',
+                         'achieved': lane, 'peak': lane_peak,
+                         'unit': 'T lane-op/s', 'frac': lane / lane_peak,
+                         'counted': '3 (F) + 5 (adjoint) lane-ops per '
+                                    'unordered pair-bin, whole evaluation'},
             'hmc_iterations_per_s': iters / s,
             'accepted_steps_per_s': acc / s,
             'acceptance': acc / (iters * 64),
             'ms_per_iteration': 1e3 * s / iters,
-            'ms_per_force_eval_64_chains': e0.elapsed_time(e1) / 3,
+            'ms_per_force_eval_64_chains': ev_ms,
             'variants': {k: v['best'] for k, v in tuned.items()},
             'launch': 'CUDA graph replay per HMC iteration (11 batched exact evaluations)'}
 
@@ -955,7 +985,7 @@ def run_delayed_acceptance(torch, iters=30, pool=256, pretrain_steps=300):
             rws.append((e / pot.conv).cpu().numpy())
             if train_every and (i + 1) % train_every == 0:
                 t = time.perf_counter()
-                sampler.train(steps=4, batch=32)
+                sampler.train(steps=1, batch=16)
                 torch.cuda.synchronize()
                 ms += 1e3 * (time.perf_counter() - t)
         return ms * 1e-3, np.array(rws)
@@ -989,7 +1019,7 @@ def run_delayed_acceptance(torch, iters=30, pool=256, pretrain_steps=300):
                      'ess_rw_per_s': ess_sum(tr) / s,
                      'rms_stage2_log_ratio_kT': float(
                          (da.sum_dhs_err / (iters * 64)).sqrt()) / da.kT,
-                     'online_training': (f'4 Adam steps on 32 buffered '
+                     'online_training': (f'1 Adam step on 16 buffered '
                                          f'pairs every {every} iterations '
                                          '(timed)') if every
                      else 'none',

@@ -114,6 +114,9 @@ const FqGradEntry kFqGradTable[] = {
     {{16, 8, 0}, fqgrad2_kernel<16, 8, 2>},
     {{32, 16, 0}, fqgrad2_kernel<32, 16, 1>},
     {{24, 16, 0}, fqgrad2_kernel<24, 16, 1>},
+    // small particles: the 1,024 pair records of a tile shared by 16 chunk
+    // threads per atom instead of 8
+    {{16, 16, 0}, fqgrad2_kernel<16, 16, 1>},
 };
 constexpr int kNumFqGrad = sizeof(kFqGradTable) / sizeof(kFqGradTable[0]);
 size_t fqgrad_smem(const GradVariant &v) {
