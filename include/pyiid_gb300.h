@@ -476,7 +476,8 @@ int pyiid_neighbor_list(pyiid_ctx *ctx, const float *positions,
  *   dE/dx_a = sum_{b in list(a), r_ab < r_cut} sum_c (dE/dfeat[a][c] +
  *             dE/dfeat[b][c]) dphi_c/dr (x_a - x_b) / r_ab.
  *   energy    : device double [n_configs], E = sum_a y_a (unscaled)
- *   forces    : device float [total][3] = -scale dE/dx, or NULL (energy only)
+ *   forces    : device float [total][3] = -scale dE/dx, or NULL (energy
+ *               only); forces need n_centres divisible by 8
  *   feat_bf16 : device bfloat16 [total][n_centres] for the descriptors, or
  *               NULL (context workspace)
  * Other arguments as pyiid_rbf_features / pyiid_mlp_forward.  Uses its own

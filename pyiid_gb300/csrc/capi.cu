@@ -114,9 +114,6 @@ const FqGradEntry kFqGradTable[] = {
     {{16, 8, 0}, fqgrad2_kernel<16, 8, 2>},
     {{32, 16, 0}, fqgrad2_kernel<32, 16, 1>},
     {{24, 16, 0}, fqgrad2_kernel<24, 16, 1>},
-    // small particles: the 1,024 pair records of a tile shared by 16 chunk
-    // threads per atom instead of 8
-    {{16, 16, 0}, fqgrad2_kernel<16, 16, 1>},
 };
 constexpr int kNumFqGrad = sizeof(kFqGradTable) / sizeof(kFqGradTable[0]);
 size_t fqgrad_smem(const GradVariant &v) {
@@ -2304,9 +2301,9 @@ extern "C" int pyiid_surrogate_forces(
     return fail(ctx, PYIID_ERR_INVALID_ARG, "r_cut and sigma must be > 0");
   if (n_hidden < 1 || max_nb < 1)
     return fail(ctx, PYIID_ERR_INVALID_ARG, "bad sizes");
-  if (forces && n_centres % 4 != 0)
+  if (forces && n_centres % 8 != 0)
     return fail(ctx, PYIID_ERR_INVALID_ARG,
-                "forces need n_centres divisible by 4 (got %d)", n_centres);
+                "forces need n_centres divisible by 8 (got %d)", n_centres);
   const int n = offsets[n_configs];
   CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   int *d_cfg, *d_off;
@@ -2346,16 +2343,18 @@ extern "C" int pyiid_surrogate_forces(
         positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, X, nullptr);
     LAUNCH_CHECK(ctx);
     TRY(fused_mlp_attr(ctx));
-    const int blocks = std::min((n + 63) / 64, 2 * std::max(1, ctx->n_sms));
-    mlp_fused_kernel<<<blocks, 128, sizeof(FusedMlpSmem), ctx->stream>>>(
-        X, n, W1, b1, W2, b2, w3, b3, y, gx);
+    TRY(ensure(ctx, "sf_gh", (size_t)std::max(n, 1) * C * sizeof(__half), &p));
+    __half *gh = static_cast<__half *>(p);
+    const int blocks = std::min((n + 127) / 128, 2 * std::max(1, ctx->n_sms));
+    mlp_fused_kernel<<<blocks, 256, sizeof(FusedMlpSmem), ctx->stream>>>(
+        X, n, W1, b1, W2, b2, w3, b3, y, gh);
     LAUNCH_CHECK(ctx);
     reduce_by_config_kernel<<<n_configs, 256, 0, ctx->stream>>>(
         y, d_off, n_configs, energy);
     LAUNCH_CHECK(ctx);
     if (forces) {
-      rbf_forces_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
-          positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, gx, scale,
+      rbf_forces_nl_kernel<__half><<<wgrid, 32 * warps, 0, ctx->stream>>>(
+          positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, gh, scale,
           forces);
       LAUNCH_CHECK(ctx);
     }
@@ -2389,7 +2388,7 @@ extern "C" int pyiid_surrogate_forces(
   silu_backward_kernel<<<512, 256, 0, ctx->stream>>>(h1, pre1, nh, h1b, h1);
   LAUNCH_CHECK(ctx);
   TRY((gemm<false, true>(ctx, h1b, H, W1, H, gx, C, n, C, H, 0)));
-  rbf_forces_nl_kernel<<<wgrid, 32 * warps, 0, ctx->stream>>>(
+  rbf_forces_nl_kernel<float><<<wgrid, 32 * warps, 0, ctx->stream>>>(
       positions, nbr_idx, nbr_cnt, max_nb, n, C, r_cut, sigma, gx, scale,
       forces);
   LAUNCH_CHECK(ctx);

@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace pyiid {
@@ -392,15 +393,33 @@ __global__ void broadcast_rows_kernel(const float *__restrict__ v, int rows,
 //   fc'(r) = -(pi / (2 rc)) sin(pi r / rc),
 // (the descriptor of b holds the pair too), forces[a] = -scale dE/dx_a.  One
 // warp per atom; lane l takes the neighbours l, l + 32, ... and loops over
-// the centres with g[a] in registers and g[b] read as float4; the x, y, z
-// sums are reduced over the warp once per atom.  n_centres % 4 == 0 and
-// n_centres <= 64.
+// the centres with g[a] in registers and g[b] read 16 bytes at a time
+// (FP32 or FP16 rows); the x, y, z sums are reduced over the warp once per
+// atom.  n_centres % 4 == 0 (FP32) or % 8 == 0 (FP16), n_centres <= 64.
+__device__ __forceinline__ void load_g8(const float *p, float (&v)[8]) {
+  const float4 a = reinterpret_cast<const float4 *>(p)[0];
+  const float4 b = reinterpret_cast<const float4 *>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void load_g8(const __half *p, float (&v)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4 *>(p);
+  const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[i]));
+    v[2 * i] = f.x;
+    v[2 * i + 1] = f.y;
+  }
+}
+
+template <typename GT>
 __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
                                      const int *__restrict__ nbr,
                                      const int *__restrict__ count,
                                      int max_nb, int n_atoms, int n_centres,
                                      float rc, float sigma,
-                                     const float *__restrict__ g, float scale,
+                                     const GT *__restrict__ g, float scale,
                                      float *__restrict__ forces) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int a = blockIdx.x * (blockDim.x >> 5) + warp;
@@ -413,7 +432,7 @@ __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
   const float inv2s2 = 0.5f * inv_s2;
   const float rc2 = rc * rc;
   const float kfc = -0.5f * 3.14159265358979f / rc;
-  const float4 *ga4 = reinterpret_cast<const float4 *>(g + (size_t)a * n_centres);
+  const GT *ga = g + (size_t)a * n_centres;
   float fx = 0.f, fy = 0.f, fz = 0.f;
   for (int i = lane; i < n; i += 32) {
     const int b = nb[i];
@@ -425,16 +444,17 @@ __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
     float sn, cs;
     sincospif(r / rc, &sn, &cs);
     const float fc = 0.5f * (1.f + cs), dfc = kfc * sn;
-    const float4 *gb4 =
-        reinterpret_cast<const float4 *>(g + (size_t)b * n_centres);
+    const GT *gb = g + (size_t)b * n_centres;
     float s = 0.f;
-    for (int q = 0; q < n_centres / 4; ++q) {
-      const float4 u = ga4[q], w = gb4[q];
-      const float gs[4] = {u.x + w.x, u.y + w.y, u.z + w.z, u.w + w.w};
+    for (int q = 0; q < n_centres / 8; ++q) {
+      float u[8], w[8];
+      load_g8(ga + 8 * q, u);
+      load_g8(gb + 8 * q, w);
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float d = r - (float)(4 * q + e) * step;
-        s = fmaf(gs[e], __expf(-d * d * inv2s2) * (dfc - fc * d * inv_s2), s);
+      for (int e = 0; e < 8; ++e) {
+        const float d = r - (float)(8 * q + e) * step;
+        s = fmaf(u[e] + w[e], __expf(-d * d * inv2s2) *
+                                  (dfc - fc * d * inv_s2), s);
       }
     }
     s = s / r;
@@ -467,8 +487,10 @@ __global__ void rbf_forces_nl_kernel(const float *__restrict__ pos,
 // by tile in the backward pass instead of being kept.  The four weight
 // layouts the B fragments need (consecutive k in one 32-bit word) are staged
 // once per CTA in shared memory with padded rows (conflict-free loads); CTAs
-// stay resident and loop over atom blocks.  y is written per atom (summed
-// per configuration by reduce_by_config_kernel) and g as FP32 [n][32].
+// stay resident and loop over atom blocks (any multiple of 32 threads per
+// CTA; the warps share the staged weights).  y is written per atom (summed
+// per configuration by reduce_by_config_kernel) and g as FP16 [n][32] (the
+// force kernel gathers one row per neighbour: half the bytes of FP32).
 constexpr int kFC = 32, kFH = 128;
 constexpr int kLd1 = kFC + 8;   // rows of 32 (+8 pad) bf16: W1T [h][c]
 constexpr int kLd2 = kFH + 8;   // rows of 128 (+8 pad): W2T, W2, W1
@@ -494,14 +516,14 @@ __device__ __forceinline__ unsigned ld_u32(const __nv_bfloat16 *p) {
   return *reinterpret_cast<const unsigned *>(p);
 }
 
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(256, 2)
     mlp_fused_kernel(const __nv_bfloat16 *__restrict__ X, int n_atoms,
                      const __nv_bfloat16 *__restrict__ W1,
                      const float *__restrict__ b1,
                      const __nv_bfloat16 *__restrict__ W2,
                      const float *__restrict__ b2,
                      const float *__restrict__ w3, const float *__restrict__ b3,
-                     float *__restrict__ y, float *__restrict__ gout) {
+                     float *__restrict__ y, __half *__restrict__ gout) {
   extern __shared__ __align__(16) unsigned char fused_smem[];
   FusedMlpSmem &S = *reinterpret_cast<FusedMlpSmem *>(fused_smem);
   const int tid = threadIdx.x;
@@ -528,8 +550,9 @@ __global__ void __launch_bounds__(128, 2)
   const int g = lane >> 2, q = lane & 3;
   const float bias3 = b3[0];
   const int n_blocks = (n_atoms + 15) / 16;
-  for (int blk = blockIdx.x * 4 + warp; blk < n_blocks;
-       blk += gridDim.x * 4) {
+  const int wpb = blockDim.x >> 5;
+  for (int blk = blockIdx.x * wpb + warp; blk < n_blocks;
+       blk += gridDim.x * wpb) {
     const int r0 = blk * 16;
     const int ra = r0 + g, rb = r0 + g + 8;
     const bool va = ra < n_atoms, vb = rb < n_atoms;
@@ -649,14 +672,12 @@ __global__ void __launch_bounds__(128, 2)
         mma_bf16_16816(acc, dz1[t], bb);
       }
       const int c = 8 * j + 2 * q;
-      if (va) {
-        gout[(size_t)ra * kFC + c] = acc[0];
-        gout[(size_t)ra * kFC + c + 1] = acc[1];
-      }
-      if (vb) {
-        gout[(size_t)rb * kFC + c] = acc[2];
-        gout[(size_t)rb * kFC + c + 1] = acc[3];
-      }
+      if (va)
+        *reinterpret_cast<__half2 *>(gout + (size_t)ra * kFC + c) =
+            __floats2half2_rn(acc[0], acc[1]);
+      if (vb)
+        *reinterpret_cast<__half2 *>(gout + (size_t)rb * kFC + c) =
+            __floats2half2_rn(acc[2], acc[3]);
     }
   }
 }
