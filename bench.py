@@ -1087,6 +1087,26 @@ def run_delayed_acceptance_single_atom(torch, iters=20):
     return out
 
 
+def run_surrogate_forces(torch, reps=20):
+    """The surrogate's energy and forces for the 64 x 1,000-atom chains of
+    the delayed-acceptance workload (one pyiid_surrogate_forces call:
+    neighbour-list descriptors, fused MLP forward and descriptor gradient,
+    forces), after one neighbour-list build; mean CUDA-event time."""
+    from pyiid_gb300.surrogate import RBFMLPSurrogate, DelayedAcceptanceHMC
+    pot, start = setup_au1000_chains(torch)
+    da = DelayedAcceptanceHMC(pot, RBFMLPSurrogate(seed=0), start,
+                              temperature=300.0, dt=1e-3, n_steps=10, seed=4)
+    x = da.x.clone()
+    da._neighbours(x)
+    ms = time_ms(torch, lambda: da.surrogate(x), reps)
+    return {'workload': 'surrogate energy + forces, 64 x 1000-atom Au, '
+                        '32 centres / 8 A, MLP 32-128-128-1',
+            'ms_per_call': ms, 'atoms': int(x.shape[0]),
+            'neighbour_list_ms': time_ms(torch, lambda: da._neighbours(x),
+                                         reps),
+            'max_neighbours': int(da.cnt.max().item())}
+
+
 def setup_au1000_chains(torch, n_chains=64):
     """The 64-chain single-atom workload: 1,000-atom fcc Au (a = 4.08 A),
     gobs = G(r) of the undisplaced particle, chains started from seeded
@@ -1377,6 +1397,8 @@ WORKLOADS = {
         lambda torch, **kw: run_delayed_acceptance_single_atom(torch, **kw),
     'exact_incremental_mh':
         lambda torch, **kw: run_incremental_mh(torch, **kw),
+    'surrogate_forces_au1000x64':
+        lambda torch, **kw: run_surrogate_forces(torch, **kw),
     'gcmc_au500': lambda torch, **kw: run_gcmc(torch, **kw),
     'nuts_64_chains_au1000': lambda torch, **kw: run_nuts(torch, **kw),
 }

@@ -673,6 +673,9 @@ int set_attrs(pyiid_ctx *ctx) {
   CUDA_TRY(ctx, cudaFuncSetAttribute(move_gram_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      2 * kGramCH * 3200 * (int)sizeof(float)));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_rows_T_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)gemm_tf32_smem()));
   ctx->attrs_set = true;
   return PYIID_OK;
 }
@@ -1182,11 +1185,14 @@ int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
   CUDA_TRY(ctx, cudaSetDevice(ctx->device));
   TMatrix *T;
   TRY(get_tmatrix(ctx, n_bins, qstep, rstep, rgrid, n_r, qmin, &T));
+  TRY(set_attrs(ctx));
   const int rows = 3 * n_atoms;
+  if ((rows + 127) / 128 > 65535)
+    return fail(ctx, PYIID_ERR_INVALID_ARG,
+                "n_atoms > 2,796,160 is not supported");
   dim3 grid((n_r + 127) / 128, (rows + 127) / 128);
-  gemm_rows_T_kernel<<<grid, 256, 0, ctx->stream>>>(grad_fq, T->d_T, rows,
-                                                    n_bins, n_r, T->kmin,
-                                                    grad_pdf);
+  gemm_rows_T_kernel<<<grid, 256, gemm_tf32_smem(), ctx->stream>>>(
+      grad_fq, T->d_T, rows, n_bins, n_r, T->kmin, grad_pdf);
   LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }

@@ -319,7 +319,9 @@ def grad_pdf(grad_fq_t, qstep, rstep, rgrid, qmin):
                           f'{list(g.shape)})')
     n, _, k = g.shape
     rg = _np(rgrid, np.float64)
-    out = torch.zeros((n, 3, len(rg)), dtype=torch.float64, device=g.device)
+    # every element is written by the kernel (a zero fill cost 15 us of the
+    # 0.18 ms call at N = 1000)
+    out = torch.empty((n, 3, len(rg)), dtype=torch.float64, device=g.device)
     if n and len(rg):
         ctx = context(g.device.index)
         ctx.call('pyiid_grad_pdf', ctypes.c_void_p(g.data_ptr()), n, k,
