@@ -27,6 +27,7 @@
 #include "move_kernels.cuh"
 #include "spring_kernels.cuh"
 #include "transform_kernels.cuh"
+#include "umma_gemm.cuh"
 
 using namespace pyiid;
 
@@ -215,12 +216,18 @@ struct TMatrix {
   // Gram matrix T T^T (single-atom moves), built on first use
   double *d_M64 = nullptr;
   float *d_M32 = nullptr;
+  // T^T split into TF32 high and low parts, packed for the tensor-core
+  // G(r) gradient (umma::pack_b_kernel), built on first use
+  float *d_Bhi = nullptr, *d_Blo = nullptr;
+  int b_rows_pad = 0;
 };
 
 void free_tmatrix(TMatrix *M) {
   cudaFree(M->d_T);
   cudaFree(M->d_M64);
   cudaFree(M->d_M32);
+  cudaFree(M->d_Bhi);
+  cudaFree(M->d_Blo);
 }
 
 struct NaTable {
@@ -250,6 +257,9 @@ struct pyiid_ctx {
   int adj_variant = 0;  // 0: symmetric (each pair once), 1: owner-computes
   int fqgrad_variant = 0;
   int n_sms = 0;  // streaming multiprocessors of the device
+  // device word a kernel sets when one of its bounded waits gave up
+  // (reported and cleared by pyiid_synchronize)
+  int *d_status = nullptr;
 };
 
 namespace {
@@ -673,9 +683,14 @@ int set_attrs(pyiid_ctx *ctx) {
   CUDA_TRY(ctx, cudaFuncSetAttribute(move_gram_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      2 * kGramCH * 3200 * (int)sizeof(float)));
-  CUDA_TRY(ctx, cudaFuncSetAttribute(gemm_rows_T_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)gemm_tf32_smem()));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(
+                    umma::tf32x3_gemm_persistent<256, 2>,
+                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    umma::PersistShape<256, 2>::kSmem));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(
+                    umma::tf32x3_gemm_persistent<128, 3>,
+                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    umma::PersistShape<128, 3>::kSmem));
   ctx->attrs_set = true;
   return PYIID_OK;
 }
@@ -858,6 +873,7 @@ int pyiid_destroy(pyiid_ctx *ctx) {
   for (auto &L : ctx->layouts) free_layout(L.get());
   for (auto &T : ctx->tmats) free_tmatrix(T.get());
   for (auto &N : ctx->nas) cudaFree(N->d_na);
+  cudaFree(ctx->d_status);
   delete ctx;
   return PYIID_OK;
 }
@@ -871,6 +887,18 @@ int pyiid_set_stream(pyiid_ctx *ctx, void *stream) {
 int pyiid_synchronize(pyiid_ctx *ctx) {
   if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (ctx->d_status) {
+    int v = 0;
+    CUDA_TRY(ctx, cudaMemcpy(&v, ctx->d_status, sizeof(int),
+                             cudaMemcpyDeviceToHost));
+    if (v) {
+      CUDA_TRY(ctx, cudaMemset(ctx->d_status, 0, sizeof(int)));
+      return fail(ctx, PYIID_ERR_TIMEOUT,
+                  "a kernel's wait on its own pipeline gave up (code %d); "
+                  "its output is not valid",
+                  v);
+    }
+  }
   return PYIID_OK;
 }
 
@@ -1187,12 +1215,61 @@ int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
   TRY(get_tmatrix(ctx, n_bins, qstep, rstep, rgrid, n_r, qmin, &T));
   TRY(set_attrs(ctx));
   const int rows = 3 * n_atoms;
-  if ((rows + 127) / 128 > 65535)
-    return fail(ctx, PYIID_ERR_INVALID_ARG,
-                "n_atoms > 2,796,160 is not supported");
-  dim3 grid((n_r + 127) / 128, (rows + 127) / 128);
-  gemm_rows_T_kernel<<<grid, 256, gemm_tf32_smem(), ctx->stream>>>(
-      grad_fq, T->d_T, rows, n_bins, n_r, T->kmin, grad_pdf);
+  const int kw = n_bins - T->kmin;
+  if (kw <= 0) {  // every bin below qmin: an all-zero product
+    CUDA_TRY(ctx, cudaMemsetAsync(grad_pdf, 0,
+                                  (size_t)rows * n_r * sizeof(double),
+                                  ctx->stream));
+    return PYIID_OK;
+  }
+  const int k_tiles = (kw + umma::kBK - 1) / umma::kBK;
+  const int m_tiles = (rows + umma::kBM - 1) / umma::kBM;
+  const int a_rows_pad = m_tiles * umma::kBM;
+  const int pack_grid = 8 * ctx->n_sms;
+  if (!T->d_Bhi) {
+    // T^T packed once per T matrix, rows padded to a multiple of 256 (the
+    // widest column tile)
+    T->b_rows_pad = (n_r + 255) / 256 * 256;
+    const size_t nb = (size_t)k_tiles * umma::kBK * T->b_rows_pad;
+    CUDA_TRY(ctx, cudaMalloc(&T->d_Bhi, nb * sizeof(float)));
+    CUDA_TRY(ctx, cudaMalloc(&T->d_Blo, nb * sizeof(float)));
+    umma::pack_b_kernel<<<pack_grid, 256, 0, ctx->stream>>>(
+        T->d_T, n_bins, n_r, T->kmin, T->b_rows_pad, k_tiles, T->d_Bhi,
+        T->d_Blo);
+    LAUNCH_CHECK(ctx);
+  }
+  if (!ctx->d_status) {
+    CUDA_TRY(ctx, cudaMalloc(&ctx->d_status, sizeof(int)));
+    CUDA_TRY(ctx, cudaMemset(ctx->d_status, 0, sizeof(int)));
+  }
+  void *ahi, *alo;
+  const size_t na = (size_t)k_tiles * umma::kBK * a_rows_pad * sizeof(float);
+  TRY(ensure(ctx, "gp_ahi", na, &ahi));
+  TRY(ensure(ctx, "gp_alo", na, &alo));
+  umma::pack_a_kernel<<<pack_grid, 256, 0, ctx->stream>>>(
+      grad_fq, rows, n_bins, T->kmin, a_rows_pad, k_tiles, (float *)ahi,
+      (float *)alo);
+  LAUNCH_CHECK(ctx);
+  // 128 x 256 output tiles when they give every SM at least two, else
+  // 128 x 128 (more CTAs for few rows); one persistent CTA per SM
+  const int n256 = (n_r + 255) / 256, n128 = (n_r + 127) / 128;
+  if ((long long)m_tiles * n256 >= 2LL * ctx->n_sms) {
+    const int tiles = m_tiles * n256;
+    umma::tf32x3_gemm_persistent<256, 2>
+        <<<std::min(tiles, ctx->n_sms), 192,
+           umma::PersistShape<256, 2>::kSmem, ctx->stream>>>(
+            (const float *)ahi, (const float *)alo, T->d_Bhi, T->d_Blo,
+            k_tiles, a_rows_pad, T->b_rows_pad, m_tiles, n256, rows, n_r,
+            grad_pdf, ctx->d_status);
+  } else {
+    const int tiles = m_tiles * n128;
+    umma::tf32x3_gemm_persistent<128, 3>
+        <<<std::min(tiles, ctx->n_sms), 192,
+           umma::PersistShape<128, 3>::kSmem, ctx->stream>>>(
+            (const float *)ahi, (const float *)alo, T->d_Bhi, T->d_Blo,
+            k_tiles, a_rows_pad, T->b_rows_pad, m_tiles, n128, rows, n_r,
+            grad_pdf, ctx->d_status);
+  }
   LAUNCH_CHECK(ctx);
   return PYIID_OK;
 }

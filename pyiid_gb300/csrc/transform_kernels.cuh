@@ -226,191 +226,6 @@ __global__ void gradfq_coef_kernel(const double *__restrict__ na,
   }
 }
 
-// Compat G(r) gradient (grad_pdf, kernels/master_kernel.py:272-290: one
-// F -> G transform per row of the [N, 3, K] gradient):
-// out[row][i] = sum_{k >= kmin} A[row][k] T[k][i]   (FP64 output)
-// Rows are the 3N rows of a reference-convention grad_fq.
-//
-// On the tensor cores with FP32-level accuracy: every operand x is split
-// into x_hi (its sign, exponent and top 10 mantissa bits: exactly what a
-// TF32 multiply reads) and x_lo = x - x_hi (exact in FP32), and
-// A T ~= A_lo T_hi + A_hi T_lo + A_hi T_hi  (mma.sync m16n8k8 TF32, FP32
-// accumulate; A_lo T_lo and the 13 bits of x_lo the multiplier ignores
-// are below 2^-20 of the product).  Norm-wise error against FP64 2.7e-6.
-// The split is a bit mask and one subtraction per operand (a conversion
-// instruction per operand half cost 17 % of the time).
-// CTA tile 128 rows x 128 r, 8 warps of 64 x 32 (4 x 4 tiles of 16 x 8);
-// K in steps of 16 through a 4-stage cp.async ring (the tiles of step
-// t + 3 load while step t multiplies; A rows are not 16-byte aligned, so A
-// moves 4 bytes per copy, T 16).  A fragments are read from row-major
-// [row][k] tiles padded to 20 floats, T fragments from [k][r] tiles padded to
-// 136: both conflict-free.  The three products of a step run as three
-// passes over independent tiles, two m-tiles at a time (no product waits on
-// the accumulator of the previous one).  Two CTAs per SM.
-constexpr int kGemmBK = 16, kGemmPadA = 20, kGemmPadB = 136, kGemmStages = 4;
-
-constexpr size_t gemm_tf32_smem() {
-  return (size_t)kGemmStages * (128 * kGemmPadA + kGemmBK * kGemmPadB) *
-         sizeof(float);
-}
-
-__device__ __forceinline__ void tf32_split(float x, unsigned &hi,
-                                           unsigned &lo) {
-  hi = __float_as_uint(x) & 0xffffe000u;
-  lo = __float_as_uint(x - __uint_as_float(hi));
-}
-
-__device__ __forceinline__ void mma_tf32_1688(float (&c)[4],
-                                              const unsigned (&a)[4],
-                                              const unsigned (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// cp.async of 4 / 16 bytes; ok == false zero-fills the destination (the
-// source address is not read)
-__device__ __forceinline__ void cp_async4(float *dst, const float *src,
-                                          bool ok) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d),
-               "l"(src), "r"(ok ? 4 : 0));
-}
-__device__ __forceinline__ void cp_async16(float *dst, const float *src,
-                                           bool ok) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d),
-               "l"(src), "r"(ok ? 16 : 0));
-}
-
-__global__ void __launch_bounds__(256, 2)
-    gemm_rows_T_kernel(const float *__restrict__ A, const float *__restrict__ T,
-                       int n_rows, int n_bins, int n_r, int kmin,
-                       double *__restrict__ out) {
-  extern __shared__ __align__(16) float gsm[];
-  float(*sA)[128][kGemmPadA] = reinterpret_cast<float(*)[128][kGemmPadA]>(gsm);
-  float(*sB)[kGemmBK][kGemmPadB] = reinterpret_cast<float(*)[kGemmBK][kGemmPadB]>(
-      gsm + kGemmStages * 128 * kGemmPadA);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, q = lane & 3;
-  const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32;
-  const int row0 = blockIdx.y * 128, col0 = blockIdx.x * 128;
-  const bool vec_t =
-      (n_r % 4) == 0 && (reinterpret_cast<uintptr_t>(T) & 15) == 0;
-  const int n_tiles =
-      n_bins > kmin ? (n_bins - kmin + kGemmBK - 1) / kGemmBK : 0;
-  auto issue = [&](int t) {
-    const int st = t % kGemmStages, k0 = kmin + t * kGemmBK;
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-      const int idx = e * 256 + tid;
-      const int r = idx / kGemmBK, kk = idx % kGemmBK;
-      const int gr = row0 + r, gk = k0 + kk;
-      const bool ok = gr < n_rows && gk < n_bins;
-      cp_async4(&sA[st][r][kk], ok ? A + (size_t)gr * n_bins + gk : A, ok);
-    }
-#pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      const int idx = e * 256 + tid;
-      const int kk = idx >> 5, cc = (idx & 31) * 4;
-      const int gk = k0 + kk, gc = col0 + cc;
-      if (vec_t) {
-        const bool ok = gk < n_bins && gc < n_r;
-        cp_async16(&sB[st][kk][cc], ok ? T + (size_t)gk * n_r + gc : T, ok);
-      } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const bool ok = gk < n_bins && gc + j < n_r;
-          cp_async4(&sB[st][kk][cc + j], ok ? T + (size_t)gk * n_r + gc + j : T,
-                    ok);
-        }
-      }
-    }
-  };
-  float c[4][4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) c[i][j][e] = 0.f;
-#pragma unroll
-  for (int t = 0; t < kGemmStages - 1; ++t) {
-    if (t < n_tiles) issue(t);
-    asm volatile("cp.async.commit_group;\n" ::);
-  }
-  for (int t = 0; t < n_tiles; ++t) {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(kGemmStages - 2));
-    __syncthreads();
-    const int st = t % kGemmStages;
-#pragma unroll
-    for (int k8 = 0; k8 < kGemmBK; k8 += 8) {
-      unsigned bh[4][2], bl[4][2];
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        tf32_split(sB[st][k8 + q][wn + 8 * nt + g], bh[nt][0], bl[nt][0]);
-        tf32_split(sB[st][k8 + q + 4][wn + 8 * nt + g], bh[nt][1], bl[nt][1]);
-      }
-#pragma unroll
-      for (int m2 = 0; m2 < 4; m2 += 2) {
-        unsigned ah[2][4], al[2][4];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int r = wm + 16 * (m2 + u) + g;
-          tf32_split(sA[st][r][k8 + q], ah[u][0], al[u][0]);
-          tf32_split(sA[st][r + 8][k8 + q], ah[u][1], al[u][1]);
-          tf32_split(sA[st][r][k8 + q + 4], ah[u][2], al[u][2]);
-          tf32_split(sA[st][r + 8][k8 + q + 4], ah[u][3], al[u][3]);
-        }
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-          for (int nt = 0; nt < 4; ++nt)
-            mma_tf32_1688(c[m2 + u][nt], al[u], bh[nt]);
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-          for (int nt = 0; nt < 4; ++nt)
-            mma_tf32_1688(c[m2 + u][nt], ah[u], bl[nt]);
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-          for (int nt = 0; nt < 4; ++nt)
-            mma_tf32_1688(c[m2 + u][nt], ah[u], bh[nt]);
-      }
-    }
-    // the stage read in the previous step is free (every thread passed the
-    // barrier above): refill it with step t + stages - 1
-    if (t + kGemmStages - 1 < n_tiles) issue(t + kGemmStages - 1);
-    asm volatile("cp.async.commit_group;\n" ::);
-  }
-  asm volatile("cp.async.wait_group 0;\n" ::);
-  // double2 stores need 16-byte alignment of every row start
-  const bool vec_o =
-      (n_r % 2) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
-#pragma unroll
-  for (int mt = 0; mt < 4; ++mt)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int gr = row0 + wm + 16 * mt + g + 8 * h;
-      if (gr >= n_rows) continue;
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int gc = col0 + wn + 8 * nt + 2 * q;
-        const double v0 = c[mt][nt][2 * h], v1 = c[mt][nt][2 * h + 1];
-        double *o = out + (size_t)gr * n_r + gc;
-        if (vec_o && gc + 1 < n_r) {
-          *reinterpret_cast<double2 *>(o) = make_double2(v0, v1);
-        } else {
-          if (gc < n_r) o[0] = v0;
-          if (gc + 1 < n_r) o[1] = v1;
-        }
-      }
-    }
-}
-
 // Compat potential gradient from an explicit grad_pdf: one warp per row,
 // grad[row] = sum_i c_i gpdf[row][i], with c recomputed from (gcalc, gobs).
 __global__ void potential_grad_rows_kernel(const double *__restrict__ gpdf,

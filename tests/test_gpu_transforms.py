@@ -1,9 +1,10 @@
 """The F(Q) -> G(r) maps on the GPU against the oracle's T matrix: the
-compat gradient transform (pyiid_grad_pdf, a 3xTF32 tensor-core GEMM with
-FP32 accumulation and FP64 output) over several CTA tiles, both load paths
-(n_r a multiple of 4 or not), K not a multiple of the 16-bin step, qmin > 0
-(rows below kmin skipped) and qmin above the whole Q range (an all-zero
-product); and the batched forward transform (pyiid_pdf).
+compat gradient transform (pyiid_grad_pdf, a 3xTF32 tcgen05 GEMM with
+FP32 accumulation in tensor memory and FP64 output) over several output
+tiles and both tile widths (few rows: 128 columns; many: 256), n_r even or
+odd (paired or single FP64 stores), K not a multiple of the 32-bin k step,
+qmin > 0 (rows below kmin skipped) and qmin above the whole Q range (an
+all-zero product); and the batched forward transform (pyiid_pdf).
 Tolerance: norm-wise relative 1e-5 (3xTF32 products, ~3e-6 measured, and
 FP32 sums of K terms)."""
 import numpy as np
@@ -33,7 +34,9 @@ def D():
                                           (43, 330, 4000, 0.0),
                                           (1, 17, 130, 0.0),
                                           (200, 64, 257, 1.0),
-                                          (5, 17, 130, 1.4)])
+                                          (5, 17, 130, 1.4),
+                                          (1000, 330, 4000, 0.0),
+                                          (1001, 331, 3999, 0.5)])
 def test_grad_pdf_matches_oracle(D, n, k, n_r, qmin):
     rng = np.random.default_rng(n + k)
     g = rng.standard_normal((n, 3, k)).astype(np.float32)
@@ -41,6 +44,9 @@ def test_grad_pdf_matches_oracle(D, n, k, n_r, qmin):
     rg = np.arange(n_r) * rstep
     got = D.grad_pdf(torch.as_tensor(g, device='cuda'), qstep, rstep, rg,
                      qmin).cpu().numpy()
+    # no bounded wait of the tensor-core pipeline gave up
+    from pyiid_gb300._native import context
+    context().synchronize()
     want = O.grad_pdf(g, rstep, qstep, rg, qmin)
     assert got.shape == (n, 3, n_r)
     if not np.any(want):
