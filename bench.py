@@ -565,38 +565,66 @@ def run_batched(torch, steps=5):
 
 def _run_batched(torch, steps):
     from pyiid_gb300 import autotune, debye
+    from pyiid_gb300._native import context
     pos, sp, off, tab, sizes = batched_workload()
     p = torch.as_tensor(pos, device='cuda')
     out = torch.empty((len(sizes), 500), dtype=torch.float32, device='cuda')
     tuned = autotune.tune_call(
         lambda: debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out),
         kernels=('fq',), reps=2)
-    s = torch.cuda.Stream()
-    s.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(s):
-        for _ in range(3):
+    ctx = context()
+
+    def graph_ms(variant, n=steps):
+        """mean time of n replays of the batch captured in a CUDA graph"""
+        ctx.set_variant('fq', variant)
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(3):
+                debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out)
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
             debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out)
-    torch.cuda.current_stream().wait_stream(s)
-    g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
-        debye.batch_fq(p, sp, off, tab, 0.05, 2, out=out)
-    g.replay()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for _ in range(steps):
         g.replay()
-    ev1.record()
-    ev1.synchronize()
-    ms = ev0.elapsed_time(ev1) / steps
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(n):
+            g.replay()
+        ev1.record()
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1) / n
+
+    # the two launch forms of the group-reduction kernel, same bins per
+    # thread: one CTA per work unit (hardware dispatch in largest-first
+    # order) and the persistent form (resident CTAs, device work counter)
+    shapes = {(i['bins_per_thread'], i['pairs_per_thread']): idx
+              for idx, i in autotune.variants('fq')}
+    forms = {}
+    for L in (56, 48):
+        forms[f'{L}_bins_per_thread'] = {
+            'one_cta_per_unit_ms': graph_ms(shapes[(L, -3)], 10),
+            'persistent_ms': graph_ms(shapes[(L, -13)], 10)}
+    best = tuned['fq']['best']
+    ms = graph_ms(best)
+    info = dict(autotune.variants('fq'))[best]
+    persistent = info['pairs_per_thread'] == -13
     pairs = int(np.sum(sizes.astype(np.int64) * (sizes - 1) // 2))
     assert torch.isfinite(out).all()
     return {'workload': '256 fcc Au/Pt alloys, N~U{55..2000}, Q 0.1-25 step 0.05',
             'atoms': int(sizes.sum()), 'pairs': pairs,
             'ms_per_batch': ms, 'configs_per_s': len(sizes) / (ms * 1e-3),
             'pair_bin_terms_per_s': pairs * 498 / (ms * 1e-3),
-            'fq_variant': tuned['fq']['best'],
-            'launch': 'CUDA graph replay: 1 pair-sum + 1 finishing kernel'}
+            'fq_variant': best,
+            'fq_shape': {'bins_per_thread': info['bins_per_thread'],
+                         'persistent': persistent},
+            'launch_forms': forms,
+            'launch': ('CUDA graph replay: counter reset + 1 persistent '
+                       'pair-sum + 1 finishing kernel') if persistent else
+                      ('CUDA graph replay: 1 pair-sum (one CTA per work '
+                       'unit) + 1 finishing kernel')}
 
 
 def run_fq_grad_au1000(torch, reps=100, cpu_reps=2):

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <map>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -55,9 +56,13 @@ using GradKernel = void (*)(const float *, const int *, const int4 *,
                             const int2 *, float, float, int, int, int,
                             const float *, int, float *, JSplit);
 
+using FqPersistKernel = void (*)(const float *, const int *, const int4 *,
+                                 const int4 *, const int *, float, float, int,
+                                 int, int, int, int, int, int *, double *);
 struct FqEntry {
   FqVariant v;
-  FqKernel k;
+  FqKernel k;             // one CTA per work unit
+  FqPersistKernel kp = nullptr;  // persistent form of the same shape
 };
 struct GradEntry {
   GradVariant v;
@@ -74,7 +79,8 @@ struct FqGradEntry {
 
 // NP <= 0 marks the packed (FP32x2) even/odd kernels: 0 one pair per
 // thread at a time, -2 two pairs interleaved, -3 (and -4) the per-tile-pair
-// group reduction at 3 (4) CTAs per SM
+// group reduction at 3 (4) CTAs per SM, -13 its persistent form (CTAs
+// resident on every SM taking work units from a counter) at 3 CTAs per SM
 const FqEntry kFqTable[] = {
     {{32, 0}, fq_pair2_kernel<32>},   {{48, 0}, fq_pair2_kernel<48>},
     {{64, 0}, fq_pair2_kernel<64>},   {{24, 0}, fq_pair2_kernel<24>},
@@ -91,6 +97,9 @@ const FqEntry kFqTable[] = {
     {{16, -4}, fq_pair3_kernel<16, 4>},
     {{48, -3}, fq_pair3_kernel<48, 3>}, {{40, -3}, fq_pair3_kernel<40, 3>},
     {{56, -3}, fq_pair3_kernel<56, 3>},
+    {{56, -13}, fq_pair3_kernel<56, 3>, fq_pair3_persistent<56, 3>},
+    {{48, -13}, fq_pair3_kernel<48, 3>, fq_pair3_persistent<48, 3>},
+    {{40, -13}, fq_pair3_kernel<40, 3>, fq_pair3_persistent<40, 3>},
 };
 // (the last template argument is the minimum resident CTAs per SM, i.e. the
 // register budget: 2 x 256 threads -> 128 registers, 3 x 256 -> 85)
@@ -260,6 +269,8 @@ struct pyiid_ctx {
   // device word a kernel sets when one of its bounded waits gave up
   // (reported and cleared by pyiid_synchronize)
   int *d_status = nullptr;
+  // resident CTAs per SM of a persistent kernel at a shared-memory size
+  std::map<std::pair<const void *, size_t>, int> occupancy;
 };
 
 namespace {
@@ -669,11 +680,17 @@ int set_attrs(pyiid_ctx *ctx) {
                       kFqGradTable[i].k,
                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                       (int)fqgrad_smem(kFqGradTable[i].v)));
-  for (int i = 0; i < kNumFq; ++i)
+  for (int i = 0; i < kNumFq; ++i) {
     CUDA_TRY(ctx, cudaFuncSetAttribute(
                       kFqTable[i].k,
                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                       (int)fq_smem(kFqTable[i].v)));
+    if (kFqTable[i].kp)
+      CUDA_TRY(ctx, cudaFuncSetAttribute(
+                        kFqTable[i].kp,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        (int)fq_smem(kFqTable[i].v)));
+  }
   CUDA_TRY(ctx, cudaFuncSetAttribute(adjoint_sym_kernel<kAdjRS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      160 * 1024));
@@ -789,10 +806,29 @@ int run_fq(pyiid_ctx *ctx, const Layout *L, const float *positions,
     void *p;
     TRY(ensure(ctx, "fq_partial", (size_t)n_items * n_bins * sizeof(double), &p));
     partial = static_cast<double *>(p);
-    dim3 grid(n_items, n_cb);
-    E.k<<<grid, kBlock, fq_smem(E.v, n_chunks), ctx->stream>>>(
-        positions, L->d_perm, L->d_tiles, L->d_items, L->d_item_order, dq_hi,
-        dq_lo, kb0, n_chunks, n_groups, n_bins, partial);
+    const size_t smem = fq_smem(E.v, n_chunks);
+    if (E.kp) {
+      // one launch of resident CTAs drawing work units from a counter
+      void *ctr;
+      TRY(ensure(ctx, "fq_counter", sizeof(int), &ctr));
+      CUDA_TRY(ctx, cudaMemsetAsync(ctr, 0, sizeof(int), ctx->stream));
+      int &per_sm = ctx->occupancy[{(const void *)E.kp, smem}];
+      if (per_sm == 0)
+        CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &per_sm, E.kp, kBlock, smem));
+      const int n_units = n_items * n_cb;
+      const int grid = std::max(
+          1, std::min(n_units, std::max(per_sm, 1) * ctx->n_sms));
+      E.kp<<<grid, kBlock, smem, ctx->stream>>>(
+          positions, L->d_perm, L->d_tiles, L->d_items, L->d_item_order,
+          dq_hi, dq_lo, kb0, n_chunks, n_groups, n_bins, n_cb, n_units,
+          static_cast<int *>(ctr), partial);
+    } else {
+      dim3 grid(n_items, n_cb);
+      E.k<<<grid, kBlock, smem, ctx->stream>>>(
+          positions, L->d_perm, L->d_tiles, L->d_items, L->d_item_order,
+          dq_hi, dq_lo, kb0, n_chunks, n_groups, n_bins, partial);
+    }
     LAUNCH_CHECK(ctx);
   }
   dim3 g2((n_bins + 127) / 128, L->n_configs);

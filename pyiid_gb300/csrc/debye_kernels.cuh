@@ -601,14 +601,14 @@ __host__ __device__ constexpr int fq3_scratch_floats(int L) {
 // fits MINB CTAs per SM (e.g. 4 x 256 threads at <= 64 registers) instead
 // of two.  Dynamic shared memory: fq3_scratch_floats(L) floats of records
 // and group scratch + n_chunks * L doubles.
-template <int L, int MINB>
-__global__ void __launch_bounds__(kBlock, MINB)
-    fq_pair3_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
-                    const int4 *__restrict__ tiles,
-                    const int4 *__restrict__ items,
-                   const int *__restrict__ order, float dq_hi, float dq_lo,
-                    int kb0, int n_chunks, int n_groups, int n_bins,
-                    double *__restrict__ partial) {
+// One work unit: work item `item` (tile I against a run of tiles J), bin
+// block yb (n_chunks * L bins), written to partial row `item`.
+template <int L>
+__device__ __forceinline__ void fq_pair3_unit(
+    const float *__restrict__ pos, const int *__restrict__ perm,
+    const int4 *__restrict__ tiles, const int4 *__restrict__ items, int item,
+    int yb, float dq_hi, float dq_lo, int kb0, int n_chunks, int n_groups,
+    int n_bins, double *__restrict__ partial) {
   static_assert(L % 2 == 0, "L must be even");
   constexpr int M = L / 2;
   extern __shared__ float4 smem[];
@@ -618,14 +618,13 @@ __global__ void __launch_bounds__(kBlock, MINB)
   double *acc64 = reinterpret_cast<double *>(scratch + fq3_scratch_floats(L));
   __shared__ float4 sI[kTile], sJ[kTile];
 
-  const int item = order ? order[blockIdx.x] : (int)blockIdx.x;
   const int4 it = items[item];
   const int4 ti = tiles[it.x];
   const int tid = threadIdx.x;
   const int c = tid % n_chunks;
   const int g = tid / n_chunks;
   const bool active = g < n_groups;
-  const int kbase = kb0 + (blockIdx.y * n_chunks + c) * L;
+  const int kbase = kb0 + (yb * n_chunks + c) * L;
   const float kf = (float)kbase;
   const int nk = n_chunks * L;
 
@@ -698,11 +697,56 @@ __global__ void __launch_bounds__(kBlock, MINB)
     }
   }
   __syncthreads();
-  const int kfirst = kb0 + blockIdx.y * nk;
+  const int kfirst = kb0 + yb * nk;
   double *out = partial + (size_t)item * n_bins;
   for (int i = tid; i < nk; i += blockDim.x) {
     const int k = kfirst + i;
     if (k < n_bins) out[k] = acc64[i];
+  }
+}
+
+// One CTA per work unit: blockIdx.x = position in `order` (largest items
+// first), blockIdx.y = bin block.
+template <int L, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB)
+    fq_pair3_kernel(const float *__restrict__ pos, const int *__restrict__ perm,
+                    const int4 *__restrict__ tiles,
+                    const int4 *__restrict__ items,
+                    const int *__restrict__ order, float dq_hi, float dq_lo,
+                    int kb0, int n_chunks, int n_groups, int n_bins,
+                    double *__restrict__ partial) {
+  const int item = order ? order[blockIdx.x] : (int)blockIdx.x;
+  fq_pair3_unit<L>(pos, perm, tiles, items, item, blockIdx.y, dq_hi, dq_lo,
+                   kb0, n_chunks, n_groups, n_bins, partial);
+}
+
+// Persistent form: as many CTAs as fit on the device at once, each taking
+// work units u = 0, 1, ... (item order[u / n_cb], bin block u % n_cb) from
+// a device counter (*counter = 0 at launch) until none is left.  The
+// partial rows, and so the fixed-order reduction behind them, are those of
+// fq_pair3_kernel: results are bitwise equal.
+template <int L, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB)
+    fq_pair3_persistent(const float *__restrict__ pos,
+                        const int *__restrict__ perm,
+                        const int4 *__restrict__ tiles,
+                        const int4 *__restrict__ items,
+                        const int *__restrict__ order, float dq_hi,
+                        float dq_lo, int kb0, int n_chunks, int n_groups,
+                        int n_bins, int n_cb, int n_units, int *counter,
+                        double *__restrict__ partial) {
+  __shared__ int s_unit;
+  while (true) {
+    // (the previous unit's last shared-memory reads are behind this
+    // barrier pair as well)
+    if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1);
+    __syncthreads();
+    const int u = s_unit;
+    __syncthreads();
+    if (u >= n_units) break;
+    const int j = u / n_cb;
+    fq_pair3_unit<L>(pos, perm, tiles, items, order ? order[j] : j, u % n_cb,
+                     dq_hi, dq_lo, kb0, n_chunks, n_groups, n_bins, partial);
   }
 }
 

@@ -315,6 +315,42 @@ def test_batch_fq_uneven_alloys_matches_oracle(D):
         assert np.array_equal(single, got[i])
 
 
+def test_persistent_batch_fq_equals_one_cta_per_unit(D):
+    """The persistent F(Q) form (resident CTAs drawing work units from a
+    device counter) writes the partial rows the one-CTA-per-unit launch
+    writes: an uneven alloy batch is bitwise equal, and equal to the oracle,
+    on two calls in a row (the counter is reset per launch)."""
+    from pyiid_gb300 import autotune
+    from pyiid_gb300._native import context
+    rng = np.random.default_rng(29)
+    sizes = [int(n) for n in rng.integers(2, 400, 24)]
+    pos, nums, off = [], [], [0]
+    for i, n in enumerate(sizes):
+        pos.append(S.random_cube(n, 14.0, 80 + i))
+        nums.append(rng.choice([78, 79], n))
+        off.append(off[-1] + n)
+    pos = np.concatenate(pos)
+    sp, tab, _ = species_tables(np.concatenate(nums), 0.05, 500)
+    shapes = {(i['bins_per_thread'], i['pairs_per_thread']): idx
+              for idx, i in autotune.variants('fq')}
+    ctx = context()
+    old = ctx.get_variant('fq')
+    try:
+        ctx.set_variant('fq', shapes[(56, -3)])
+        want = D.batch_fq(pos, sp, np.array(off), tab, 0.05, 2).cpu().numpy()
+        ctx.set_variant('fq', shapes[(56, -13)])
+        for _ in range(2):
+            got = D.batch_fq(pos, sp, np.array(off), tab, 0.05,
+                             2).cpu().numpy()
+            assert np.array_equal(got, want)
+    finally:
+        ctx.set_variant('fq', old)
+    for i in (0, 7, 23):
+        a, b = off[i], off[i + 1]
+        o = O.fq(pos[a:b], tab[sp[a:b]], 0.05)
+        assert rel(got[i, 2:], o[2:]) <= TOL_F
+
+
 @pytest.mark.parametrize('variant', [0, 1])
 def test_adjoint_variants_match_oracle(D, variant):
     """Symmetric (each pair once) and owner-computes adjoints agree with the
