@@ -126,8 +126,13 @@ const FqGradEntry kFqGradTable[] = {
     {{24, 16, 0}, fqgrad2_kernel<24, 16, 1>},
 };
 constexpr int kNumFqGrad = sizeof(kFqGradTable) / sizeof(kFqGradTable[0]);
+// dF/dx alone: the packed kernels keep four record arrays per tile pair
+// (the fourth: pair-only products), the scalar ones three
+size_t grad_smem(const GradVariant &v) {
+  return (v.NP == 0 ? 4 : 3) * kTile * kTile * sizeof(float4);
+}
 size_t fqgrad_smem(const GradVariant &v) {
-  return 3 * kTile * kTile * sizeof(float4) +
+  return 4 * kTile * kTile * sizeof(float4) +
          (2 * (size_t)v.CPC * v.CPC * v.L + kTile * kTile) * sizeof(float);
 }
 constexpr int kNumFq = sizeof(kFqTable) / sizeof(kFqTable[0]);
@@ -674,7 +679,7 @@ int set_attrs(pyiid_ctx *ctx) {
     CUDA_TRY(ctx, cudaFuncSetAttribute(
                       kGradTable[i].k,
                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                      3 * kTile * kTile * (int)sizeof(float4)));
+                      (int)grad_smem(kGradTable[i].v)));
   for (int i = 0; i < kNumFqGrad; ++i)
     CUDA_TRY(ctx, cudaFuncSetAttribute(
                       kFqGradTable[i].k,
@@ -999,7 +1004,7 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
     const int chunks_total = (n_bins - kb0 + Lb - 1) / Lb;
     const int gy = (chunks_total + cpc - 1) / cpc;
     const int n_tiles = (int)L->tiles.size();
-    const size_t smem = 3 * kTile * kTile * sizeof(float4);
+    const size_t smem = grad_smem(E.v);
     // the packed kernels split the tiles J of a small configuration (the
     // scalar ones never do)
     if (E.v.NP == 0)

@@ -799,9 +799,12 @@ __device__ __forceinline__ void gradfq2_body(
   float4 *recA = smem;
   float4 *recB = smem + kTile * kTile;
   float4 *recC = smem + 2 * kTile * kTile;
+  // pair-only products the chunk threads of a pair would otherwise each
+  // form: (sigma2 dx, sigma2 dy, sigma2 dz, sigma2 (-r^2) with F(Q))
+  float4 *recE = smem + 3 * kTile * kTile;
   // WITH_F: per warp [CPC][L] FP32 F(Q) sums and their Kahan compensations
   // behind the records
-  float *fsum = reinterpret_cast<float *>(smem + 3 * kTile * kTile);
+  float *fsum = reinterpret_cast<float *>(smem + 4 * kTile * kTile);
   float *fcmp = fsum + CPC * CPC * L;
   float *recD = fcmp + CPC * CPC * L;  // WITH_F: cos theta of each record
   __shared__ float4 sI[kTile], sJ[kTile];
@@ -927,9 +930,10 @@ __device__ __forceinline__ void gradfq2_body(
     const bool same = (tj == I);
     for (int q = tid; q < kTile * kTile; q += blockDim.x) {
       const int b = q / kTile, a = q % kTile;
-      float4 ra = make_float4(0.f, 0.f, 0.f, 1.f);
+      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f);
       float4 rb = make_float4(0.f, 0.f, 0.f, 0.f);
       float4 rc = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 re = make_float4(0.f, 0.f, 0.f, 0.f);
       if (a < ti.y && b < tJ.y && !(same && a == b)) {
         const float4 pa = sI[a];
         const float4 pb = sJ[b];
@@ -938,11 +942,15 @@ __device__ __forceinline__ void gradfq2_body(
                                    dq_lo, dx, dy, dz);
         const float beta = -(p.inv_r * p.inv_r * p.inv_r);
         const float gam = __fdividef(-p.r * dq_hi, 2.0f * p.ch);  // 2ch in [1.41, 2]
-        ra = make_float4(p.th_hi, p.th_lo, p.kappa, p.sigma2);
-        // beta sh is rebuilt as (kappa/2) beta; its slot and c.w (recD
-        // with F(Q)) carry (sin theta, cos theta) for the rotated odd seed
+        // a.w: beta sh as (kappa/2) beta; b.y and c.w (recD with F(Q))
+        // carry (sin theta, cos theta) for the rotated odd seed
+        ra = make_float4(p.th_hi, p.th_lo, p.kappa,
+                         __fmul_rn(0.5f * p.kappa, beta));
         rb = make_float4(beta * p.ch, p.sth, beta, gam);
-        rc = make_float4(dx, dy, dz, WITH_F ? -(p.r * p.r) : p.cth);
+        const float fe = WITH_F ? -(p.r * p.r) : 0.f;
+        rc = make_float4(dx, dy, dz, WITH_F ? fe : p.cth);
+        re = make_float4(p.sigma2 * dx, p.sigma2 * dy, p.sigma2 * dz,
+                         p.sigma2 * fe);
         if constexpr (WITH_F) recD[q] = p.cth;
       } else if constexpr (WITH_F) {
         recD[q] = 0.f;
@@ -950,6 +958,7 @@ __device__ __forceinline__ void gradfq2_body(
       recA[q] = ra;
       recB[q] = rb;
       recC[q] = rc;
+      recE[q] = re;
     }
     __syncthreads();
     auto pair_loop = [&](auto use_f) {
@@ -959,18 +968,17 @@ __device__ __forceinline__ void gradfq2_body(
         const float4 ra = recA[q];
         const float4 rb = recB[q];
         const float4 rc = recC[q];
+        const float4 re = recE[q];
         float2 s, co;
         seed_sincos2r(kf, ra.x, ra.y, rb.y, WITH_F ? recD[q] : rc.w, s, co);
-        const float bsh = __fmul_rn(0.5f * ra.z, rb.z);
         float2 t = __fmul2_rn(f2(rb.z), s);
-        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(bsh)));
+        float2 w = __ffma2_rn(co, f2(rb.x), __fmul2_rn(s, f2(ra.w)));
         float2 kg = make_float2(kf * rb.w, (kf + 1.0f) * rb.w);
         const float2 dkg = f2(2.0f * rb.w);
         const float2 kp = f2(ra.z), km = f2(-ra.z);
         const float2 dx2 = f2(rc.x), dy2 = f2(rc.y), dz2 = f2(rc.z);
-        const float2 sx2 = f2(ra.w * rc.x), sy2 = f2(ra.w * rc.y),
-                     sz2 = f2(ra.w * rc.z);
-        const float2 fe2 = f2(rc.w), fo2 = f2(ra.w * rc.w);
+        const float2 sx2 = f2(re.x), sy2 = f2(re.y), sz2 = f2(re.z);
+        const float2 fe2 = f2(rc.w), fo2 = f2(re.w);
 #pragma unroll
         for (int m = 0; m < M; ++m) {
           const float2 wn = __ffma2_rn(km, t, w);
