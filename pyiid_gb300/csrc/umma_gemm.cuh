@@ -233,6 +233,28 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 
 constexpr int kStagePitch = 33;  // floats per staged row (conflict-free)
 
+// FP32 -> FP64 on the integer pipes, exact for every non-NaN input (a NaN
+// stays a NaN with its payload).  binary32 sign | 8-bit exponent | 23-bit
+// fraction becomes binary64 sign | exponent + (1023 - 127) | fraction and 29
+// zero bits; zero keeps only its sign; infinity and NaN take exponent 2047;
+// a subnormal is first scaled by 2^24 (exact in FP32, then normal) and its
+// binary64 exponent lowered by 24.  No branch and no conversion instruction:
+// F2F.F64.F32 issues to the FP64 unit at about one result per clock per SM
+// on this part, which made the 12 M conversions of a 3,000 x 4,000 output
+// the limit of the whole GEMM (~20 us).
+__device__ __forceinline__ double widen_f32(float x) {
+  uint32_t u = __float_as_uint(x);
+  const bool sub = ((u & 0x7f800000u) == 0u) && (u & 0x007fffffu);
+  u = sub ? __float_as_uint(x * 16777216.0f) : u;
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t bias =
+      e == 0u ? 0u : (e == 255u ? 0x70000000u : 0x38000000u);
+  const uint32_t hi =
+      ((u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + bias)) -
+      (sub ? (24u << 20) : 0u);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 template <int BN, int S>
 struct PersistShape {
   static constexpr int kTileB = BN * kBK;
@@ -281,6 +303,8 @@ __global__ void __launch_bounds__(192, 1)
   auto acc_empty = [&](int b) { return bars + 8 * (2 * S + 2 + b); };
   const uint32_t done = bars + 8 * (2 * S + 4);
   const int total = m_tiles * n_tiles;
+  const int first = (int)blockIdx.x, stride = (int)gridDim.x;
+  auto row_tile = [&](int t) { return t / n_tiles; };
 
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
@@ -316,9 +340,9 @@ __global__ void __launch_bounds__(192, 1)
   if (tid == 0) {
     int g = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
-      const float *ah = a_hi + (size_t)(t / n_tiles) * kTileA;
-      const float *al = a_lo + (size_t)(t / n_tiles) * kTileA;
+    for (int t = first; t < total && ok; t += stride) {
+      const float *ah = a_hi + (size_t)row_tile(t) * kTileA;
+      const float *al = a_lo + (size_t)row_tile(t) * kTileA;
       const float *bh = b_hi + (size_t)(t % n_tiles) * G::kTileB;
       const float *bl = b_lo + (size_t)(t % n_tiles) * G::kTileB;
       for (int kt = 0; kt < k_tiles; ++kt, ++g) {
@@ -342,7 +366,7 @@ __global__ void __launch_bounds__(192, 1)
     constexpr uint32_t idesc = idesc_tf32(kBM, BN);
     int g = 0, li = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < total && ok; t += gridDim.x, ++li) {
+    for (int t = first; t < total && ok; t += stride, ++li) {
       const int b = li & 1, ub = li >> 1;
       if (ub > 0 && !mbar_wait(acc_empty(b), (ub - 1) & 1)) {
         atomicCAS(&words[1], 0u, (unsigned)kErrAccumWait);
@@ -385,7 +409,7 @@ __global__ void __launch_bounds__(192, 1)
     const bool pairs =
         (n_r % 2) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
     int li = 0;
-    for (int t = blockIdx.x; t < total; t += gridDim.x, ++li) {
+    for (int t = first; t < total; t += stride, ++li) {
       const int b = li & 1, ub = li >> 1;
       // the warp leaves together (the loads below are warp-collective)
       if (!__all_sync(0xffffffffu, mbar_wait(acc_full(b), ub & 1))) {
@@ -393,7 +417,7 @@ __global__ void __launch_bounds__(192, 1)
         break;
       }
       tc_fence_after();
-      const int row0 = (t / n_tiles) * kBM + q * 32;
+      const int row0 = row_tile(t) * kBM + q * 32;
       const int col0 = (t % n_tiles) * BN;
 #pragma unroll 1
       for (int c = 0; c < BN; c += 32) {
@@ -412,8 +436,8 @@ __global__ void __launch_bounds__(192, 1)
             const int rr = 2 * i + (lane >> 4), row = row0 + rr;
             if (row < n_rows && col < n_r)
               *reinterpret_cast<double2 *>(out + (size_t)row * n_r + col) =
-                  make_double2((double)stg[rr * kStagePitch + cc],
-                               (double)stg[rr * kStagePitch + cc + 1]);
+                  make_double2(widen_f32(stg[rr * kStagePitch + cc]),
+                               widen_f32(stg[rr * kStagePitch + cc + 1]));
           }
         } else {
           const int col = col0 + c + lane;
@@ -422,7 +446,7 @@ __global__ void __launch_bounds__(192, 1)
             const int row = row0 + rr;
             if (row < n_rows && col < n_r)
               out[(size_t)row * n_r + col] =
-                  (double)stg[rr * kStagePitch + lane];
+                  widen_f32(stg[rr * kStagePitch + lane]);
           }
         }
       }
