@@ -64,7 +64,10 @@ int pyiid_destroy(pyiid_ctx *ctx);
 /* Enqueue subsequent work on `stream` (a cudaStream_t; NULL = legacy default). */
 int pyiid_set_stream(pyiid_ctx *ctx, void *stream);
 
-/* Wait for all work enqueued by this context. */
+/* Wait for all work enqueued by this context.  Returns PYIID_ERR_TIMEOUT
+ * (and clears the condition) when a kernel launched since the last call
+ * gave up one of its bounded waits on its own pipeline (the tensor-core
+ * G(r) gradient of pyiid_grad_pdf); that kernel's output is then invalid. */
 int pyiid_synchronize(pyiid_ctx *ctx);
 
 /* Last error message of `ctx` (or of the last failed pyiid_create when ctx is
