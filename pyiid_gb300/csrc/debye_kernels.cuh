@@ -807,7 +807,9 @@ __device__ __forceinline__ void gradfq2_body(
   float *fsum = reinterpret_cast<float *>(smem + 4 * kTile * kTile);
   float *fcmp = fsum + CPC * CPC * L;
   float *recD = fcmp + CPC * CPC * L;  // WITH_F: cos theta of each record
-  __shared__ float4 sI[kTile], sJ[kTile];
+  // positions of tile I and of two tiles J: the next J tile's positions are
+  // loaded while the current tile's records are built
+  __shared__ float4 sI[kTile], sJb[2][kTile];
 
   const int4 ti = tiles[I];
   const int2 ct = cfg_tiles[ti.z];
@@ -913,8 +915,13 @@ __device__ __forceinline__ void gradfq2_body(
 
   const int n_cfg_tiles = ct.y - ct.x;
   const int j_end = ct.x + (int)((long long)(part + 1) * n_cfg_tiles / js.n);
-  for (int tj = ct.x + (int)((long long)part * n_cfg_tiles / js.n);
-       tj < j_end; ++tj) {
+  const int j_begin = ct.x + (int)((long long)part * n_cfg_tiles / js.n);
+  if (j_begin < j_end) {
+    const int4 t0 = tiles[j_begin];
+    if (tid < t0.y) sJb[0][tid] = load_atom(pos, perm, t0.x + tid);
+  }
+  int jb = 0;
+  for (int tj = j_begin; tj < j_end; ++tj, jb ^= 1) {
     const int4 tJ = tiles[tj];
     if (cur_sb >= 0 && tJ.w != cur_sb) flush(cur_sb, false);
     if constexpr (WITH_F) {
@@ -924,9 +931,17 @@ __device__ __forceinline__ void gradfq2_body(
       }
     }
     cur_sb = tJ.w;
+    // tile J's positions are in sJb[jb]; the previous tile's loop, its
+    // records and sJb[jb ^ 1] are free
     __syncthreads();
-    if (tid < tJ.y) sJ[tid] = load_atom(pos, perm, tJ.x + tid);
-    __syncthreads();
+    const float4 *sJ = sJb[jb];
+    const bool has_next = tj + 1 < j_end;
+    int4 tN = make_int4(0, 0, 0, 0);
+    float4 pN = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (has_next) {
+      tN = tiles[tj + 1];
+      if (tid < tN.y) pN = load_atom(pos, perm, tN.x + tid);
+    }
     const bool same = (tj == I);
     for (int q = tid; q < kTile * kTile; q += blockDim.x) {
       const int b = q / kTile, a = q % kTile;
@@ -960,6 +975,7 @@ __device__ __forceinline__ void gradfq2_body(
       recC[q] = rc;
       recE[q] = re;
     }
+    if (has_next && tid < tN.y) sJb[jb ^ 1][tid] = pN;
     __syncthreads();
     auto pair_loop = [&](auto use_f) {
       constexpr bool UF = WITH_F && decltype(use_f)::value;

@@ -159,7 +159,7 @@ def test_graph_iteration_equals_eager():
 
 def test_second_stage_uses_exact_energies():
     """After every iteration the chains' energies are the exact potential of
-    their positions (stage 2 judged with exact energies), and accepted
+    their positions (stage 2 decided on exact energies), and accepted
     moves moved the atoms."""
     import torch
     from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
