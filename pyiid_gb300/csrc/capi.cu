@@ -757,7 +757,7 @@ int choose_jsplit(pyiid_ctx *ctx, const void *kernel, int threads,
   int best_s = 1;
   if (ctas < 2 * slots) {
     double best = 1e300;
-    for (int S = 1; S <= std::min(8, n_tiles); ++S) {
+    for (int S = 1; S <= std::min(kMaxJSplit, n_tiles); ++S) {
       const double waves = std::ceil((double)(ctas * S) / (double)slots);
       const double cost = waves / S * (1.0 + 0.02 * (S - 1));
       if (cost < best) {
@@ -1026,7 +1026,7 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
         JSplit{n_split, gsize, 0});
     LAUNCH_CHECK(ctx);
     if (n_split > 1) {
-      combine_grad_parts_kernel<<<2 * std::max(1, ctx->n_sms), 256, 0,
+      combine_grad_parts_kernel<<<8 * std::max(1, ctx->n_sms), 256, 0,
                                   ctx->stream>>>(gout, n_split, gsize, gsize,
                                                  n_bins, kbo, grad);
       LAUNCH_CHECK(ctx);
@@ -1104,7 +1104,7 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
         JSplit{n_split, gsize, (size_t)n_tiles * n_bins});
     LAUNCH_CHECK(ctx);
     if (n_split > 1) {
-      combine_grad_parts_kernel<<<2 * std::max(1, ctx->n_sms), 256, 0,
+      combine_grad_parts_kernel<<<8 * std::max(1, ctx->n_sms), 256, 0,
                                   ctx->stream>>>(gout, n_split, gsize, gsize,
                                                  n_bins, kbo, grad);
       LAUNCH_CHECK(ctx);

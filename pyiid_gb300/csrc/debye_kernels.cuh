@@ -40,6 +40,7 @@ struct JSplit {
   int n;
   size_t out_stride, fpart_stride;
 };
+constexpr int kMaxJSplit = 8;  // parts of a split (choose_jsplit's bound)
 
 
 // Tile descriptor: start (in sorted order), atom count, configuration, species.
@@ -1124,17 +1125,25 @@ __global__ void combine_grad_parts_kernel(const float *__restrict__ parts,
   const size_t nt = (size_t)gridDim.x * blockDim.x;
   const bool aligned = ((reinterpret_cast<uintptr_t>(parts) |
                          reinterpret_cast<uintptr_t>(grad)) & 15) == 0;
-  if (n_bins % 4 == 0 && aligned) {
+  if (n_bins % 4 == 0 && aligned && n_parts <= kMaxJSplit) {
     const float4 *p4 = reinterpret_cast<const float4 *>(parts);
     float4 *g4 = reinterpret_cast<float4 *>(grad);
     for (size_t i = t0; i < n / 4; i += nt) {
+      // every part's load in flight before the fixed-order sum (n_parts is
+      // at most kMaxJSplit)
+      float4 a[kMaxJSplit];
+#pragma unroll
+      for (int p = 0; p < kMaxJSplit; ++p)
+        if (p < n_parts) a[p] = p4[p * (stride / 4) + i];
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int p = 0; p < n_parts; ++p) {
-        const float4 a = p4[p * (stride / 4) + i];
-        v.x += a.x;
-        v.y += a.y;
-        v.z += a.z;
-        v.w += a.w;
+#pragma unroll
+      for (int p = 0; p < kMaxJSplit; ++p) {
+        if (p < n_parts) {
+          v.x += a[p].x;
+          v.y += a[p].y;
+          v.z += a[p].z;
+          v.w += a[p].w;
+        }
       }
       const int k = (int)((4 * i) % n_bins);
       v.x = k >= kbo ? nan_to_num_f(v.x) : 0.f;
