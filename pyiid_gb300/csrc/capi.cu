@@ -770,6 +770,23 @@ int choose_jsplit(pyiid_ctx *ctx, const void *kernel, int threads,
   return PYIID_OK;
 }
 
+// A J split of one configuration's n_tiles tiles into n parts (part p covers
+// [p n_tiles / n, (p + 1) n_tiles / n)), dispatched largest part first.
+JSplit make_jsplit(int n, int n_tiles, size_t out_stride, size_t fpart_stride) {
+  JSplit js{n, out_stride, fpart_stride, {}};
+  int idx[kMaxJSplit], size[kMaxJSplit];
+  for (int p = 0; p < n && p < kMaxJSplit; ++p) {
+    idx[p] = p;
+    size[p] = (int)((long long)(p + 1) * n_tiles / n -
+                    (long long)p * n_tiles / n);
+  }
+  std::stable_sort(idx, idx + std::min(n, kMaxJSplit),
+                   [&](int a, int b) { return size[a] > size[b]; });
+  for (int p = 0; p < kMaxJSplit; ++p)
+    js.order[p] = (unsigned char)(p < n ? idx[p] : p);
+  return js;
+}
+
 int check_common(pyiid_ctx *ctx, int n_configs, const int32_t *offsets,
                  int n_species, int n_bins, double qbin, int k_begin) {
   if (!ctx) return fail(nullptr, PYIID_ERR_INVALID_ARG, "null context");
@@ -1023,7 +1040,7 @@ int pyiid_grad_fq(pyiid_ctx *ctx, const float *positions,
     E.k<<<grid, kTile * cpc, smem, ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
         chunks_total, n_bins, coef, n_species, gout,
-        JSplit{n_split, gsize, 0});
+        make_jsplit(n_split, n_tiles, gsize, 0));
     LAUNCH_CHECK(ctx);
     if (n_split > 1) {
       combine_grad_parts_kernel<<<8 * std::max(1, ctx->n_sms), 256, 0,
@@ -1101,7 +1118,7 @@ int pyiid_fq_grad(pyiid_ctx *ctx, const float *positions,
     E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
         chunks_total, n_bins, coef, n_species, gout, d_ftab, fpart, 0,
-        JSplit{n_split, gsize, (size_t)n_tiles * n_bins});
+        make_jsplit(n_split, n_tiles, gsize, (size_t)n_tiles * n_bins));
     LAUNCH_CHECK(ctx);
     if (n_split > 1) {
       combine_grad_parts_kernel<<<8 * std::max(1, ctx->n_sms), 256, 0,
@@ -1189,7 +1206,7 @@ int pyiid_fq_grad_part(pyiid_ctx *ctx, const float *positions,
     E.k<<<grid, kTile * cpc, fqgrad_smem(E.v), ctx->stream>>>(
         positions, L->d_perm, L->d_tiles, L->d_cfg_tiles, dq_hi, dq_lo, kb0,
         chunks_total, n_bins, coef, n_species, grad, d_ftab, fpart, t0,
-        JSplit{1, 0, 0});
+        make_jsplit(1, 1, 0, 0));
     LAUNCH_CHECK(ctx);
   }
   fqgrad_finish_kernel<<<(n_bins + 3) / 4, 128, 0, ctx->stream>>>(

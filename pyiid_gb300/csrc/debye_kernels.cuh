@@ -36,11 +36,14 @@ constexpr int kJMaxTiles = 32;  // max J tiles per F(Q) work item
 // writes raw partial rows (no NaN mapping) at out + z * out_stride and its
 // F(Q) rows at fpart + z * fpart_stride; combine_grad_parts_kernel and the
 // finishing kernel add the parts in a fixed order.  n = 1: no split.
+constexpr int kMaxJSplit = 8;  // parts of a split (choose_jsplit's bound)
 struct JSplit {
   int n;
   size_t out_stride, fpart_stride;
+  // part handled by blockIdx.z: the parts with more tiles J first, so that
+  // the last wave of CTAs holds the shorter ones
+  unsigned char order[kMaxJSplit];
 };
-constexpr int kMaxJSplit = 8;  // parts of a split (choose_jsplit's bound)
 
 
 // Tile descriptor: start (in sorted order), atom count, configuration, species.
@@ -790,7 +793,7 @@ __device__ __forceinline__ void gradfq2_body(
     JSplit js) {
   // tile I of this CTA (tile0: first tile of a part of the tile list)
   const int I = tile0 + (int)blockIdx.x;
-  const int part = js.n > 1 ? (int)blockIdx.z : 0;
+  const int part = js.n > 1 ? (int)js.order[blockIdx.z] : 0;
   out += part * js.out_stride;
   if constexpr (WITH_F) fpart += part * js.fpart_stride;
   static_assert(L % 2 == 0, "L must be even");
