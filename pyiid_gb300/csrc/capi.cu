@@ -230,10 +230,12 @@ struct TMatrix {
   // Gram matrix T T^T (single-atom moves), built on first use
   double *d_M64 = nullptr;
   float *d_M32 = nullptr;
-  // T^T split into TF32 high and low parts, packed for the tensor-core
-  // G(r) gradient (umma::pack_b_kernel), built on first use
-  float *d_Bhi = nullptr, *d_Blo = nullptr;
-  int b_rows_pad = 0;
+  // T^T scaled by 2^e_t and split into FP16 high and low parts, packed for
+  // the tensor-core G(r) gradient (umma::pack_b_f16_kernel), built on first
+  // use; t_amax = max |T| over the bins from kmin
+  void *d_Bhi = nullptr, *d_Blo = nullptr;
+  int b_rows_pad = 0, e_t = 0;
+  float t_amax = 0.f;
 };
 
 void free_tmatrix(TMatrix *M) {
@@ -658,6 +660,8 @@ int get_tmatrix(pyiid_ctx *ctx, int n_bins, double qstep, double rstep,
   M->n_bins = n_bins;
   M->n_r = n_r;
   M->kmin = std::max(kz, 0);
+  for (size_t i = (size_t)M->kmin * n_r; i < T.size(); ++i)
+    M->t_amax = std::max(M->t_amax, std::fabs(T[i]));
   TRY(upload(ctx, &M->d_T, T));
   ctx->tmats.insert(ctx->tmats.begin(), std::move(M));
   while (ctx->tmats.size() > 4) {
@@ -706,11 +710,11 @@ int set_attrs(pyiid_ctx *ctx) {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      2 * kGramCH * 3200 * (int)sizeof(float)));
   CUDA_TRY(ctx, cudaFuncSetAttribute(
-                    umma::tf32x3_gemm_persistent<256, 2>,
+                    umma::f16x2_gemm_persistent<256, 2>,
                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                     umma::PersistShape<256, 2>::kSmem));
   CUDA_TRY(ctx, cudaFuncSetAttribute(
-                    umma::tf32x3_gemm_persistent<128, 3>,
+                    umma::f16x2_gemm_persistent<128, 3>,
                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                     umma::PersistShape<128, 3>::kSmem));
   ctx->attrs_set = true;
@@ -1280,7 +1284,7 @@ int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
                                   ctx->stream));
     return PYIID_OK;
   }
-  const int k_tiles = (kw + umma::kBK - 1) / umma::kBK;
+  const int k_tiles = (kw + umma::kBK16 - 1) / umma::kBK16;
   const int m_tiles = (rows + umma::kBM - 1) / umma::kBM;
   const int a_rows_pad = m_tiles * umma::kBM;
   const int pack_grid = 8 * ctx->n_sms;
@@ -1288,45 +1292,49 @@ int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
     // T^T packed once per T matrix, rows padded to a multiple of 256 (the
     // widest column tile)
     T->b_rows_pad = (n_r + 255) / 256 * 256;
-    const size_t nb = (size_t)k_tiles * umma::kBK * T->b_rows_pad;
-    CUDA_TRY(ctx, cudaMalloc(&T->d_Bhi, nb * sizeof(float)));
-    CUDA_TRY(ctx, cudaMalloc(&T->d_Blo, nb * sizeof(float)));
-    umma::pack_b_kernel<<<pack_grid, 256, 0, ctx->stream>>>(
-        T->d_T, n_bins, n_r, T->kmin, T->b_rows_pad, k_tiles, T->d_Bhi,
-        T->d_Blo);
+    T->e_t = umma::fp16_scale_exp(T->t_amax);
+    const size_t nb = (size_t)k_tiles * umma::kRowBytes * T->b_rows_pad;
+    CUDA_TRY(ctx, cudaMalloc(&T->d_Bhi, nb));
+    CUDA_TRY(ctx, cudaMalloc(&T->d_Blo, nb));
+    umma::pack_b_f16_kernel<<<pack_grid, 256, 0, ctx->stream>>>(
+        T->d_T, n_bins, n_r, T->kmin, T->b_rows_pad, k_tiles, T->e_t,
+        static_cast<__half *>(T->d_Bhi), static_cast<__half *>(T->d_Blo));
     LAUNCH_CHECK(ctx);
   }
   if (!ctx->d_status) {
     CUDA_TRY(ctx, cudaMalloc(&ctx->d_status, sizeof(int)));
     CUDA_TRY(ctx, cudaMemset(ctx->d_status, 0, sizeof(int)));
   }
-  void *ahi, *alo;
-  const size_t na = (size_t)k_tiles * umma::kBK * a_rows_pad * sizeof(float);
+  void *ahi, *alo, *rexp;
+  const size_t na = (size_t)k_tiles * umma::kRowBytes * a_rows_pad;
   TRY(ensure(ctx, "gp_ahi", na, &ahi));
   TRY(ensure(ctx, "gp_alo", na, &alo));
-  umma::pack_a_kernel<<<pack_grid, 256, 0, ctx->stream>>>(
-      grad_fq, rows, n_bins, T->kmin, a_rows_pad, k_tiles, (float *)ahi,
-      (float *)alo);
+  TRY(ensure(ctx, "gp_rexp", (size_t)a_rows_pad * sizeof(int), &rexp));
+  // one warp per row (its largest magnitude, then the scaled split)
+  umma::pack_a_f16_kernel<<<pack_grid, 256, 0, ctx->stream>>>(
+      grad_fq, rows, n_bins, T->kmin, a_rows_pad, k_tiles,
+      static_cast<__half *>(ahi), static_cast<__half *>(alo),
+      static_cast<int *>(rexp));
   LAUNCH_CHECK(ctx);
   // 128 x 256 output tiles when they give every SM at least two, else
   // 128 x 128 (more CTAs for few rows); one persistent CTA per SM
   const int n256 = (n_r + 255) / 256, n128 = (n_r + 127) / 128;
   if ((long long)m_tiles * n256 >= 2LL * ctx->n_sms) {
     const int tiles = m_tiles * n256;
-    umma::tf32x3_gemm_persistent<256, 2>
-        <<<std::min(tiles, ctx->n_sms), 192,
+    umma::f16x2_gemm_persistent<256, 2>
+        <<<std::min(tiles, ctx->n_sms), umma::kGemmThreads,
            umma::PersistShape<256, 2>::kSmem, ctx->stream>>>(
-            (const float *)ahi, (const float *)alo, T->d_Bhi, T->d_Blo,
-            k_tiles, a_rows_pad, T->b_rows_pad, m_tiles, n256, rows, n_r,
-            grad_pdf, ctx->d_status);
+            ahi, alo, T->d_Bhi, T->d_Blo, k_tiles, a_rows_pad,
+            T->b_rows_pad, m_tiles, n256, rows, n_r,
+            static_cast<const int *>(rexp), T->e_t, grad_pdf, ctx->d_status);
   } else {
     const int tiles = m_tiles * n128;
-    umma::tf32x3_gemm_persistent<128, 3>
-        <<<std::min(tiles, ctx->n_sms), 192,
+    umma::f16x2_gemm_persistent<128, 3>
+        <<<std::min(tiles, ctx->n_sms), umma::kGemmThreads,
            umma::PersistShape<128, 3>::kSmem, ctx->stream>>>(
-            (const float *)ahi, (const float *)alo, T->d_Bhi, T->d_Blo,
-            k_tiles, a_rows_pad, T->b_rows_pad, m_tiles, n128, rows, n_r,
-            grad_pdf, ctx->d_status);
+            ahi, alo, T->d_Bhi, T->d_Blo, k_tiles, a_rows_pad,
+            T->b_rows_pad, m_tiles, n128, rows, n_r,
+            static_cast<const int *>(rexp), T->e_t, grad_pdf, ctx->d_status);
   }
   LAUNCH_CHECK(ctx);
   return PYIID_OK;

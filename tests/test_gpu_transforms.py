@@ -1,12 +1,14 @@
 """The F(Q) -> G(r) maps on the GPU against the oracle's T matrix: the
-compat gradient transform (pyiid_grad_pdf, a 3xTF32 tcgen05 GEMM with
-FP32 accumulation in tensor memory and FP64 output) over several output
-tiles and both tile widths (few rows: 128 columns; many: 256), n_r even or
-odd (paired or single FP64 stores), K not a multiple of the 32-bin k step,
-qmin > 0 (rows below kmin skipped) and qmin above the whole Q range (an
-all-zero product); and the batched forward transform (pyiid_pdf).
-Tolerance: norm-wise relative 1e-5 (3xTF32 products, ~3e-6 measured, and
-FP32 sums of K terms)."""
+compat gradient transform (pyiid_grad_pdf: operands scaled by powers of
+two and split into two FP16 halves, three tcgen05 kind::f16 products with
+FP32 accumulation in tensor memory, FP64 output) over several output tiles
+and both tile widths (few rows: 128 columns; many: 256), n_r even or odd
+(paired or single FP64 stores), K not a multiple of the 64-bin k step,
+qmin > 0 (rows below kmin skipped), qmin above the whole Q range (an
+all-zero product) and rows of magnitudes 1e-30 .. 1e+30 (per-row scales);
+and the batched forward transform (pyiid_pdf).
+Tolerance: norm-wise relative 1e-5 (~1.2e-6 measured: 22-bit halves and
+FP32 sums of K terms); per row 1e-5 of the row's norm."""
 import numpy as np
 import pytest
 import torch
@@ -53,6 +55,29 @@ def test_grad_pdf_matches_oracle(D, n, k, n_r, qmin):
         assert not np.any(got)
         return
     assert rel(got, want) <= TOL, rel(got, want)
+
+
+def test_grad_pdf_rows_of_very_different_magnitude(D):
+    """Each row of grad_fq is scaled by its own power of two before the FP16
+    split: rows from 1e-30 to 1e+30 (and an all-zero row) keep the relative
+    accuracy of a row of order one."""
+    rng = np.random.default_rng(11)
+    n, k, n_r = 61, 330, 4000
+    g = rng.standard_normal((n, 3, k))
+    mags = 10.0 ** np.linspace(-30, 30, n)
+    g = (g * mags[:, None, None]).astype(np.float32)
+    g[7] = 0.0
+    qstep, rstep = 0.0756865, 0.01
+    rg = np.arange(n_r) * rstep
+    got = D.grad_pdf(torch.as_tensor(g, device='cuda'), qstep, rstep, rg,
+                     0.0).cpu().numpy()
+    want = O.grad_pdf(g, rstep, qstep, rg, 0.0)
+    assert not np.any(got[7])
+    for a in range(n):
+        if a == 7:
+            continue
+        e = np.linalg.norm(got[a] - want[a]) / np.linalg.norm(want[a])
+        assert e <= TOL, (a, mags[a], e)
 
 
 @pytest.mark.parametrize('b,k,n_r,qmin', [(64, 330, 4000, 0.0),
