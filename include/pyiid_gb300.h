@@ -190,8 +190,9 @@ int pyiid_pdf(pyiid_ctx *ctx, const float *fq, int n_configs, int n_bins,
  * reference-convention grad_fq.
  *   grad_fq  : device float  [n_atoms][3][n_bins]
  *   grad_pdf : device double [n_atoms][3][n_r]   (every element written)
- * FP32 products on the tensor cores split three ways (3xTF32), FP32
- * accumulation: relative error ~3e-6 of the FP64 product.
+ * On the tensor cores: rows scaled by powers of two and split into two FP16
+ * halves, three products with FP32 accumulation; relative error ~1.2e-6 of
+ * the FP64 product.
  * Replaces grad_pdf of kernels/master_kernel.py:276-290 and
  * gpu_wrappers/gpu_wrap.py:197-284 (the `self.grad_pdf` plug-in). */
 int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
