@@ -613,8 +613,18 @@ def _run_batched(torch, steps):
     persistent = info['pairs_per_thread'] == -13
     pairs = int(np.sum(sizes.astype(np.int64) * (sizes - 1) // 2))
     assert torch.isfinite(out).all()
+    # FP32 issue roofline: the F(Q) loop issues 3 lane-ops per unordered
+    # pair-bin (per two bins: FFMA2 + FFMA2 recurrence, FADD2/FFMA2 sum)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    lane_peak = sms * FP32_LANES_PER_SM * 2.07e9 / 1e12
+    lane = pairs * 498 * 3 / (ms * 1e-3) / 1e12
     return {'workload': '256 fcc Au/Pt alloys, N~U{55..2000}, Q 0.1-25 step 0.05',
             'atoms': int(sizes.sum()), 'pairs': pairs,
+            'roofline': {'bound': 'fp32 issue', 'kernel': 'fq_pair3_kernel',
+                         'achieved': lane, 'peak': lane_peak,
+                         'unit': 'T lane-op/s', 'frac': lane / lane_peak,
+                         'counted': '3 lane-ops per unordered pair-bin, '
+                                    'whole batch (pair sums and finish)'},
             'ms_per_batch': ms, 'configs_per_s': len(sizes) / (ms * 1e-3),
             'pair_bin_terms_per_s': pairs * 498 / (ms * 1e-3),
             'fq_variant': best,
