@@ -348,10 +348,23 @@ __global__ void rbf_features_nl_kernel(const float *__restrict__ pos,
     float acc[32];
 #pragma unroll
     for (int c = 0; c < 32; ++c) acc[c] = 0.f;
+    // the next neighbour's position is gathered while this one's Gaussians
+    // are summed (the gathers were the kernel's top stall)
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    if (lane < n) {
+      const int b = nb[lane];
+      bx = pos[3 * b];
+      by = pos[3 * b + 1];
+      bz = pos[3 * b + 2];
+    }
     for (int i = lane; i < n; i += 32) {
-      const int b = nb[i];
-      const float dx = pos[3 * b] - ax, dy = pos[3 * b + 1] - ay,
-                  dz = pos[3 * b + 2] - az;
+      const float dx = bx - ax, dy = by - ay, dz = bz - az;
+      if (i + 32 < n) {
+        const int b = nb[i + 32];
+        bx = pos[3 * b];
+        by = pos[3 * b + 1];
+        bz = pos[3 * b + 2];
+      }
       const float r2 = dx * dx + dy * dy + dz * dz;
       if (r2 >= rc2) continue;
       const float r = sqrtf(r2);
