@@ -510,9 +510,13 @@ int pyiid_surrogate_forces(pyiid_ctx *ctx, const float *positions,
  * fixed, atomics/gpu_atomics.py:120-184).
  *   kernel: PYIID_KERNEL_FQ (pyiid_fq and the F(Q) part of the batched call),
  *           PYIID_KERNEL_GRAD_FQ (pyiid_grad_fq), PYIID_KERNEL_FQ_GRAD
- *           (pyiid_fq_grad) or PYIID_KERNEL_ADJOINT
+ *           (pyiid_fq_grad), PYIID_KERNEL_ADJOINT
  *           (the gradient of pyiid_batch_potential_grad: variant 0 evaluates
- *           each unordered pair once, variant 1 twice).
+ *           each unordered pair once, variant 1 twice) or PYIID_KERNEL_MLP
+ *           (the 32-128-128 surrogate network of pyiid_surrogate_forces:
+ *           variant 0 register-resident mma.sync, params {16 atoms per warp,
+ *           0, 256 threads}; variant 1 on tcgen05 tensor memory, params
+ *           {128 atoms per CTA, 1, 128 threads}).
  *   params (pyiid_variant_info): {bins per thread, pairs per thread, threads
  *   per CTA}; pairs per thread <= 0 marks the packed (FP32x2) even/odd
  *   kernels (0: one pair per thread at a time, -2: two interleaved, -3/-4:
@@ -522,7 +526,8 @@ enum {
   PYIID_KERNEL_FQ = 0,
   PYIID_KERNEL_GRAD_FQ = 1,
   PYIID_KERNEL_ADJOINT = 2,
-  PYIID_KERNEL_FQ_GRAD = 3
+  PYIID_KERNEL_FQ_GRAD = 3,
+  PYIID_KERNEL_MLP = 4
 };
 int pyiid_variant_count(int kernel);
 int pyiid_variant_info(int kernel, int variant, int *params, int n_params);

@@ -97,7 +97,7 @@ _SIGNATURES = {
     'pyiid_get_variant': (_c_int, [_vp, _c_int]),
 }
 
-KERNELS = {'fq': 0, 'grad_fq': 1, 'adjoint': 2, 'fq_grad': 3}
+KERNELS = {'fq': 0, 'grad_fq': 1, 'adjoint': 2, 'fq_grad': 3, 'mlp': 4}
 
 
 class NativeError(RuntimeError):

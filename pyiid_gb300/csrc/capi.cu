@@ -272,6 +272,7 @@ struct pyiid_ctx {
   int grad_variant = 0;
   int adj_variant = 0;  // 0: symmetric (each pair once), 1: owner-computes
   int fqgrad_variant = 0;
+  int mlp_variant = 0;  // 0: mma.sync (mlp_fused_kernel), 1: tcgen05
   int n_sms = 0;  // streaming multiprocessors of the device
   // device word a kernel sets when one of its bounded waits gave up
   // (reported and cleared by pyiid_synchronize)
@@ -916,6 +917,14 @@ int pyiid_create(pyiid_ctx **out, int device) {
   if (!ctx) return fail(nullptr, PYIID_ERR_OOM, "out of host memory");
   ctx->device = device;
   ctx->n_sms = prop.multiProcessorCount;
+  // the device status word of the kernels with bounded waits (allocated
+  // here, not at first use, which may be inside a graph capture)
+  if (cudaMalloc(&ctx->d_status, sizeof(int)) != cudaSuccess ||
+      cudaMemset(ctx->d_status, 0, sizeof(int)) != cudaSuccess) {
+    cudaFree(ctx->d_status);
+    delete ctx;
+    return fail(nullptr, PYIID_ERR_OOM, "cannot allocate the status word");
+  }
   *out = ctx;
   return PYIID_OK;
 }
@@ -1300,10 +1309,6 @@ int pyiid_grad_pdf(pyiid_ctx *ctx, const float *grad_fq, int n_atoms,
         T->d_T, n_bins, n_r, T->kmin, T->b_rows_pad, k_tiles, T->e_t,
         static_cast<__half *>(T->d_Bhi), static_cast<__half *>(T->d_Blo));
     LAUNCH_CHECK(ctx);
-  }
-  if (!ctx->d_status) {
-    CUDA_TRY(ctx, cudaMalloc(&ctx->d_status, sizeof(int)));
-    CUDA_TRY(ctx, cudaMemset(ctx->d_status, 0, sizeof(int)));
   }
   void *ahi, *alo, *rexp;
   const size_t na = (size_t)k_tiles * umma::kRowBytes * a_rows_pad;
@@ -1876,6 +1881,8 @@ int pyiid_variant_count(int kernel) {
       return 2;
     case PYIID_KERNEL_FQ_GRAD:
       return kNumFqGrad;
+    case PYIID_KERNEL_MLP:
+      return 2;
     default:
       return -1;
   }
@@ -1902,6 +1909,12 @@ int pyiid_variant_info(int kernel, int variant, int *params, int n_params) {
     params[2] = kTile * kFqGradTable[variant].v.CPC;
     return PYIID_OK;
   }
+  if (kernel == PYIID_KERNEL_MLP && (variant == 0 || variant == 1)) {
+    params[0] = variant == 1 ? 128 : 16;  // atoms per CTA tile / per warp
+    params[1] = variant == 1 ? 1 : 0;     // tensor memory used
+    params[2] = variant == 1 ? 128 : 256;  // threads per CTA
+    return PYIID_OK;
+  }
   if (kernel == PYIID_KERNEL_ADJOINT && (variant == 0 || variant == 1)) {
     params[0] = kAdjRS;               // bins between re-seeds
     params[1] = variant == 0 ? 1 : 2; // evaluations per unordered pair
@@ -1924,6 +1937,8 @@ int pyiid_set_variant(pyiid_ctx *ctx, int kernel, int variant) {
     ctx->grad_variant = variant;
   else if (kernel == PYIID_KERNEL_FQ_GRAD)
     ctx->fqgrad_variant = variant;
+  else if (kernel == PYIID_KERNEL_MLP)
+    ctx->mlp_variant = variant;
   else
     ctx->adj_variant = variant;
   return PYIID_OK;
@@ -1935,6 +1950,7 @@ int pyiid_get_variant(const pyiid_ctx *ctx, int kernel) {
   if (kernel == PYIID_KERNEL_GRAD_FQ) return ctx->grad_variant;
   if (kernel == PYIID_KERNEL_ADJOINT) return ctx->adj_variant;
   if (kernel == PYIID_KERNEL_FQ_GRAD) return ctx->fqgrad_variant;
+  if (kernel == PYIID_KERNEL_MLP) return ctx->mlp_variant;
   return -1;
 }
 
@@ -2130,6 +2146,7 @@ extern "C" int pyiid_fq_noalloc(pyiid_ctx *ctx, const float *positions,
 // surrogate.  The forward pass keeps its activations in the context
 // workspace; pyiid_mlp_backward differentiates the most recent forward.
 #include "surrogate_kernels.cuh"
+#include "mlp_tc.cuh"
 
 namespace {
 
@@ -2409,6 +2426,9 @@ int fused_mlp_attr(pyiid_ctx *ctx) {
   CUDA_TRY(ctx, cudaFuncSetAttribute(mlp_fused_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sizeof(FusedMlpSmem)));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(mlptc::mlp_tc_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     mlptc::kSmemBytes));
   if (ctx->device >= 0 && ctx->device < 64) done[ctx->device] = true;
   return PYIID_OK;
 }
@@ -2494,9 +2514,21 @@ extern "C" int pyiid_surrogate_forces(
     TRY(fused_mlp_attr(ctx));
     TRY(ensure(ctx, "sf_gh", (size_t)std::max(n, 1) * C * sizeof(__half), &p));
     __half *gh = static_cast<__half *>(p);
-    const int blocks = std::min((n + 127) / 128, 2 * std::max(1, ctx->n_sms));
-    mlp_fused_kernel<<<blocks, 256, sizeof(FusedMlpSmem), ctx->stream>>>(
-        X, n, W1, b1, W2, b2, w3, b3, y, gh);
+    if (ctx->mlp_variant == 1) {
+      // tensor-memory MLP: one persistent CTA per SM, 128 atoms per tile
+      // (measured 151 us against 70 us for the register-resident kernel on
+      // 64,000 atoms: the SiLU epilogues, one thread per row on 4 warps,
+      // dominate; kept as a variant)
+      const int tiles = (n + mlptc::kRows - 1) / mlptc::kRows;
+      mlptc::mlp_tc_kernel<<<std::min(tiles, std::max(1, ctx->n_sms)), 128,
+                             mlptc::kSmemBytes, ctx->stream>>>(
+          X, n, W1, b1, W2, b2, w3, b3, y, gh, ctx->d_status);
+    } else {
+      const int blocks =
+          std::min((n + 127) / 128, 2 * std::max(1, ctx->n_sms));
+      mlp_fused_kernel<<<blocks, 256, sizeof(FusedMlpSmem), ctx->stream>>>(
+          X, n, W1, b1, W2, b2, w3, b3, y, gh);
+    }
     LAUNCH_CHECK(ctx);
     reduce_by_config_kernel<<<n_configs, 256, 0, ctx->stream>>>(
         y, d_off, n_configs, energy);

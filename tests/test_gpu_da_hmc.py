@@ -79,11 +79,27 @@ def _weights(sur, seed):
                             .to('cuda') * 0.1)
 
 
-@pytest.mark.parametrize('centres,hidden', [(32, 128), (16, 64)],
-                         ids=['fused-32-128', 'gemm-16-64'])
-def test_surrogate_energy_and_forces_match_oracle(centres, hidden):
-    """The 32-128-128 net runs the fused kernel, other sizes the GEMM
-    chain; both against the oracle."""
+@pytest.mark.parametrize('centres,hidden,mlp', [(32, 128, 0), (32, 128, 1),
+                                               (16, 64, 0)],
+                         ids=['fused-32-128-mma.sync', 'fused-32-128-tcgen05',
+                              'gemm-16-64'])
+def test_surrogate_energy_and_forces_match_oracle(centres, hidden, mlp):
+    """The 32-128-128 net runs one fused kernel (register-resident mma.sync
+    variant 0, tensor-memory tcgen05 variant 1), other sizes the GEMM
+    chain; all against the oracle."""
+    import torch
+    from pyiid_gb300._native import context
+    from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
+    ctx = context()
+    old_mlp = ctx.get_variant('mlp')
+    ctx.set_variant('mlp', mlp)
+    try:
+        _check_surrogate(centres, hidden)
+    finally:
+        ctx.set_variant('mlp', old_mlp)
+
+
+def _check_surrogate(centres, hidden):
     import torch
     from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
     sur = RBFMLPSurrogate(n_centres=centres, n_hidden=hidden, seed=5)
