@@ -1185,7 +1185,22 @@ def run_incremental_mh(torch, pot=None, start=None, n_steps=8192):
     dt = time.perf_counter() - t
     acc = int(mc.state['accepted'].sum().item()) - a0
     props = n_steps * pot.n_configs
-    return {'accepted_steps_per_s': acc / dt,
+    # move_delta_kernel's loop: per two bins of one partner, 4 FFMA2 of the
+    # two recurrences (old and new position) and 2-3 for their difference:
+    # 3.25 lane-ops per pair term (one position, one bin)
+    dev_s = ev0.elapsed_time(ev1) * 1e-3
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    lane_peak = sms * FP32_LANES_PER_SM * 2.07e9 / 1e12
+    terms = props * 2 * 999 * pot.n_bins
+    lane = terms * 3.25 / dev_s / 1e12
+    return {'roofline': {'bound': 'latency (fp32 issue counted)',
+                         'kernel': 'move_delta_kernel + move_gram_kernel',
+                         'achieved': lane, 'peak': lane_peak,
+                         'unit': 'T lane-op/s', 'frac': lane / lane_peak,
+                         'counted': '3.25 lane-ops per pair term, whole '
+                                    'step (two dependent launches of about '
+                                    '42 M pair terms for 64 chains)'},
+            'accepted_steps_per_s': acc / dt,
             'proposals_per_s': props / dt,
             'acceptance': acc / props,
             'us_per_step_all_chains': 1e6 * dt / n_steps,
