@@ -297,8 +297,12 @@ __global__ void __launch_bounds__(128, 1)
   }
   if (tid == 0 && phase != 4u * (uint32_t)((n_tiles - (int)blockIdx.x +
                                             (int)gridDim.x - 1) /
-                                           (int)gridDim.x))
+                                           (int)gridDim.x)) {
     atomicCAS(err, 0, kErrAccumWait);
+    // a product that timed out may still be writing tensor memory: one more
+    // bounded wait for its commit before the columns are freed
+    mbar_wait(bar, (phase - 1u) & 1u);
+  }
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {

@@ -275,6 +275,80 @@ def test_small_configurations_split_over_ctas(D, n):
     assert rel(gd1, gd) <= 1e-6
 
 
+def _fq_grad_sampled_check(pos, numbers, f, g, qbin, nb, kb, rows=8):
+    """F(Q) on every 8th bin and the full gradient rows of a few seeded
+    atoms against FP64 sums; zeros below k_begin."""
+    sp, tab, _ = species_tables(numbers, qbin, nb)
+    q = pos.astype(np.float32).astype(np.float64)
+    per = tab[sp].astype(np.float64)
+    na = O.normalization(tab[sp])
+    assert np.all(f[:kb] == 0) and np.all(g[:, :, :kb] == 0)
+    idx = np.arange(kb, nb, 8)
+    Q = idx * qbin
+    s = np.zeros(len(idx))
+    for i0 in range(1, len(q)):
+        d = np.sqrt(((q[i0] - q[:i0]) ** 2).sum(1))
+        s += ((per[i0, idx][None] * per[:i0][:, idx])
+              * np.sin(Q[None] * d[:, None]) / d[:, None]).sum(0)
+    want_f = 2 * s / na[idx]
+    assert rel(f[idx], want_f) <= TOL_F, rel(f[idx], want_f)
+    Qa = np.arange(nb) * qbin
+    for a in np.random.default_rng(len(q)).choice(len(q), rows, replace=False):
+        others = np.delete(np.arange(len(q)), a)
+        d = q[a] - q[others]
+        r = np.sqrt((d * d).sum(1))[:, None]
+        qr = Qa[None] * r
+        w = (per[a][None] * per[others]) * (Qa[None] * np.cos(qr)
+                                            - np.sin(qr) / r) / r ** 2
+        want = -np.einsum('jk,jc->ck', w, d) / na
+        assert rel(g[a, :, kb:], want[:, kb:]) <= TOL_G, a
+
+
+def test_split_across_sizes_kbegin_species_and_variants(D):
+    """Configurations whose tiles J are split over CTAs (parts ordered
+    largest first, combined in part order): alternating sizes, odd and zero
+    k_begin, three species and every launch variant, each against FP64 sums
+    with zeros below k_begin, the gradient-only call within 1e-6, and the
+    same input twice bitwise equal."""
+    from pyiid_gb300 import autotune
+    from pyiid_gb300._native import context
+    qbin, nb = 0.05, 500
+    fcc = S.displaced(S.fcc_nearest(4.08, 1000), 0.05, 21)
+    tri = S.random_cube(300, 18.0, 8)
+    tri_n = list(np.random.default_rng(8).choice([46, 78, 79], 300))
+    first = None
+    for pos, nums, kb in ((fcc, [79] * 1000, 3), (*alloy(64, 9, 11.0), 0),
+                          (tri, tri_n, 2), (fcc, [79] * 1000, 3)):
+        sp, tab, _ = species_tables(nums, qbin, nb)
+        f, g = (t.cpu().numpy() for t in D.fq_grad(pos, sp, tab, qbin, kb))
+        _fq_grad_sampled_check(pos, nums, f, g, qbin, nb, kb)
+        g1 = D.grad_fq(pos, sp, tab, qbin, kb).cpu().numpy()
+        assert rel(g1, g) <= 1e-6
+        assert np.all(g1[:, :, :kb] == 0)
+        if len(pos) == 1000:
+            if first is None:
+                first = (f, g)
+            else:
+                assert np.array_equal(first[0], f)
+                assert np.array_equal(first[1], g)
+    ctx = context()
+    old = ctx.get_variant('fq_grad')
+    sp, tab, _ = species_tables(tri_n, qbin, nb)
+    try:
+        ref = None
+        for idx, _ in autotune.variants('fq_grad'):
+            ctx.set_variant('fq_grad', idx)
+            f, g = (t.cpu().numpy()
+                    for t in D.fq_grad(tri, sp, tab, qbin, 3))
+            if ref is None:
+                _fq_grad_sampled_check(tri, tri_n, f, g, qbin, nb, 3, rows=4)
+                ref = (f, g)
+            assert rel(f, ref[0]) <= 1e-6 and rel(g, ref[1]) <= 1e-6, idx
+            assert np.all(f[:3] == 0) and np.all(g[:, :, :3] == 0)
+    finally:
+        ctx.set_variant('fq_grad', old)
+
+
 def test_split_combine_into_an_output_at_an_odd_offset(D):
     """A small configuration (J-split, partial rows combined) written into a
     gradient that starts 4 bytes past a 16-byte boundary: the combine takes
