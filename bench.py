@@ -1498,14 +1498,30 @@ def main():
                          'result (for profiling)')
     ap.add_argument('--workload-steps', type=int, default=None,
                     help='steps of --only-workload exact_incremental_mh')
+    ap.add_argument('--variant', action='append', default=[],
+                    metavar='KERNEL=INDEX',
+                    help='launch variant for --only-workload (e.g. mlp=1: '
+                         'the tcgen05 surrogate MLP); repeatable')
     args = ap.parse_args()
     if args.only_workload:
         import torch
+        from pyiid_gb300._native import context, KERNELS
         fn = WORKLOADS[args.only_workload]
         kw = {}
         if args.workload_steps and args.only_workload == 'exact_incremental_mh':
             kw['n_steps'] = args.workload_steps
-        print(json.dumps({args.only_workload: fn(torch, **kw)}))
+        chosen = {}
+        for v in args.variant:
+            kern, _, idx = v.partition('=')
+            if kern not in KERNELS or not idx.lstrip('-').isdigit():
+                ap.error(f'--variant {v}: expected one of {sorted(KERNELS)}'
+                         '=INDEX')
+            context().set_variant(kern, int(idx))
+            chosen[kern] = int(idx)
+        out = fn(torch, **kw)
+        if chosen:
+            out['variants_set'] = chosen
+        print(json.dumps({args.only_workload: out}))
         return
     rank, world, local = dist_env()
     if args.impl == 'reference':
