@@ -516,7 +516,9 @@ int pyiid_surrogate_forces(pyiid_ctx *ctx, const float *positions,
  *           (the 32-128-128 surrogate network of pyiid_surrogate_forces:
  *           variant 0 register-resident mma.sync, params {16 atoms per warp,
  *           0, 256 threads}; variant 1 on tcgen05 tensor memory, params
- *           {128 atoms per CTA, 1, 128 threads}).
+ *           {128 atoms per CTA, 1, 128 threads}; variant 2 on tcgen05 with
+ *           two 128-atom tiles in flight per CTA and two threads per row,
+ *           params {256, 1, 512}; the default).
  *   params (pyiid_variant_info): {bins per thread, pairs per thread, threads
  *   per CTA}; pairs per thread <= 0 marks the packed (FP32x2) even/odd
  *   kernels (0: one pair per thread at a time, -2: two interleaved, -3/-4:

@@ -272,7 +272,9 @@ struct pyiid_ctx {
   int grad_variant = 0;
   int adj_variant = 0;  // 0: symmetric (each pair once), 1: owner-computes
   int fqgrad_variant = 0;
-  int mlp_variant = 0;  // 0: mma.sync (mlp_fused_kernel), 1: tcgen05
+  // 0: mma.sync (mlp_fused_kernel), 1: tcgen05 one tile per CTA, 2: tcgen05
+  // two tiles in flight per CTA (default: 57 against 70 us for mma.sync)
+  int mlp_variant = 2;
   int n_sms = 0;  // streaming multiprocessors of the device
   // device word a kernel sets when one of its bounded waits gave up
   // (reported and cleared by pyiid_synchronize)
@@ -1882,7 +1884,7 @@ int pyiid_variant_count(int kernel) {
     case PYIID_KERNEL_FQ_GRAD:
       return kNumFqGrad;
     case PYIID_KERNEL_MLP:
-      return 2;
+      return 3;
     default:
       return -1;
   }
@@ -1909,10 +1911,11 @@ int pyiid_variant_info(int kernel, int variant, int *params, int n_params) {
     params[2] = kTile * kFqGradTable[variant].v.CPC;
     return PYIID_OK;
   }
-  if (kernel == PYIID_KERNEL_MLP && (variant == 0 || variant == 1)) {
-    params[0] = variant == 1 ? 128 : 16;  // atoms per CTA tile / per warp
-    params[1] = variant == 1 ? 1 : 0;     // tensor memory used
-    params[2] = variant == 1 ? 128 : 256;  // threads per CTA
+  if (kernel == PYIID_KERNEL_MLP && variant >= 0 && variant <= 2) {
+    // atoms in flight per CTA (per warp for mma.sync), tensor memory used,
+    // threads per CTA
+    const int info[3][3] = {{16, 0, 256}, {128, 1, 128}, {256, 1, 512}};
+    for (int i = 0; i < 3; ++i) params[i] = info[variant][i];
     return PYIID_OK;
   }
   if (kernel == PYIID_KERNEL_ADJOINT && (variant == 0 || variant == 1)) {
@@ -2429,6 +2432,9 @@ int fused_mlp_attr(pyiid_ctx *ctx) {
   CUDA_TRY(ctx, cudaFuncSetAttribute(mlptc::mlp_tc_kernel,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      mlptc::kSmemBytes));
+  CUDA_TRY(ctx, cudaFuncSetAttribute(mlptc::mlp_tc2_kernel,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     mlptc::kSmemBytes2));
   if (ctx->device >= 0 && ctx->device < 64) done[ctx->device] = true;
   return PYIID_OK;
 }
@@ -2514,14 +2520,20 @@ extern "C" int pyiid_surrogate_forces(
     TRY(fused_mlp_attr(ctx));
     TRY(ensure(ctx, "sf_gh", (size_t)std::max(n, 1) * C * sizeof(__half), &p));
     __half *gh = static_cast<__half *>(p);
+    const int tiles = (n + mlptc::kRows - 1) / mlptc::kRows;
     if (ctx->mlp_variant == 1) {
       // tensor-memory MLP: one persistent CTA per SM, 128 atoms per tile
       // (measured 151 us against 70 us for the register-resident kernel on
       // 64,000 atoms: the SiLU epilogues, one thread per row on 4 warps,
       // dominate; kept as a variant)
-      const int tiles = (n + mlptc::kRows - 1) / mlptc::kRows;
       mlptc::mlp_tc_kernel<<<std::min(tiles, std::max(1, ctx->n_sms)), 128,
                              mlptc::kSmemBytes, ctx->stream>>>(
+          X, n, W1, b1, W2, b2, w3, b3, y, gh, ctx->d_status);
+    } else if (ctx->mlp_variant == 2) {
+      // two tiles in flight per CTA, two threads per row
+      mlptc::mlp_tc2_kernel<<<std::min((tiles + 1) / 2,
+                                       std::max(1, ctx->n_sms)),
+                              512, mlptc::kSmemBytes2, ctx->stream>>>(
           X, n, W1, b1, W2, b2, w3, b3, y, gh, ctx->d_status);
     } else {
       const int blocks =

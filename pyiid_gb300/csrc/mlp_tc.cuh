@@ -24,10 +24,12 @@
 // on time-out the CTA records an error in *err and stops.
 //
 // Measured on 64 x 1,000 atoms: 151 us against 70 us for the register-
-// resident mma.sync kernel, which stays the default (variant 0; this is
-// variant 1).  The products are small (tensor pipe busy 1.7 % of the time);
-// the SiLU and SiLU' epilogues run one thread per row on 4 warps per SM at
-// 15 % issue, where the mma.sync kernel spreads them over 16 warps.
+// resident mma.sync kernel (launch variant 0; this is variant 1).  The
+// products are small (tensor pipe busy 1.7 % of the time); the SiLU and
+// SiLU' epilogues run one thread per row on 4 warps per SM at 15 % issue,
+// where the mma.sync kernel spreads them over 16 warps.  mlp_tc2_kernel
+// below (variant 2, the default) keeps two tiles in flight per CTA with two
+// threads per row: 57 us.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -310,6 +312,251 @@ __global__ void __launch_bounds__(128, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(
                      tmem),
                  "r"(256)
+                 : "memory");
+  }
+}
+
+// Two tiles in flight, two threads per row (launch variant 2).  512 threads
+// in two slots of 8 warps; slot s takes tiles 2 blockIdx.x + s, + 2
+// gridDim.x, ... with its own X and activation blocks, its own 256 tensor-
+// memory columns, mbarrier and named barrier, so one slot's epilogues run
+// while the other's product is in flight.  Warp w of a slot reads lane
+// quarter w mod 4 (rows 32 (w mod 4) ..) and column half (w / 4) mod 2 of
+// every 128-column result; the layer-2 output y is the fixed-order sum of
+// the halves' partial dot products (bias on half 0).  The weights are staged
+// once per CTA for both slots.  Each slot's wait is bounded; a time-out ends
+// that slot's loop for all its threads (bar.red.or over the slot) and is
+// recorded in *err.
+constexpr int kSlotBytes = 3 * kBlk;               // X + 2 activation blocks
+constexpr int kOffSlots = kOffX;                   // after the weights
+constexpr int kOffVec2 = kOffSlots + 2 * kSlotBytes;
+constexpr int kOffY2 = kOffVec2 + 3 * kHid * 4;    // [slot][half][row] FP32
+constexpr int kOffBar2 = kOffY2 + 2 * 2 * kRows * 4;
+constexpr int kSmemBytes2 = kOffBar2 + 32 + 1024;  // + alignment slack
+static_assert(kSmemBytes2 <= 232448, "shared memory per CTA");
+static_assert(kOffSlots % 1024 == 0 && kSlotBytes % 1024 == 0,
+              "operand blocks 1024-byte aligned");
+
+__device__ __forceinline__ void slot_sync(int id) {
+  asm volatile("bar.sync %0, 256;\n" ::"r"(id) : "memory");
+}
+// barrier over the slot's 256 threads; true if any thread passed true
+__device__ __forceinline__ bool slot_sync_or(int id, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n"
+      " bar.red.or.pred q, %2, 256, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id)
+      : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(512, 1)
+    mlp_tc2_kernel(const __nv_bfloat16 *__restrict__ X, int n_atoms,
+                   const __nv_bfloat16 *__restrict__ W1,
+                   const float *__restrict__ b1,
+                   const __nv_bfloat16 *__restrict__ W2,
+                   const float *__restrict__ b2, const float *__restrict__ w3,
+                   const float *__restrict__ b3, float *__restrict__ y,
+                   __half *__restrict__ gout, int *err) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = smem_addr(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  unsigned char *sp = smem_raw + (base - raw);
+  float *sb1 = reinterpret_cast<float *>(sp + kOffVec2);
+  float *sb2 = sb1 + kHid, *sw3 = sb2 + kHid;
+  float *sy = reinterpret_cast<float *>(sp + kOffY2);
+  uint32_t *slot_p = reinterpret_cast<uint32_t *>(sp + kOffBar2 + 16);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int s = warp >> 3;        // tile slot
+  const int h = (warp >> 2) & 1;  // column half
+  const int q = warp & 3;         // tensor-memory lane quarter
+  const int r = 32 * q + lane;    // row of the tile
+  const uint32_t bar = base + kOffBar2 + 8 * s;
+  const int xo = kOffSlots + s * kSlotBytes;  // this slot's X block
+  const int ao = xo + kBlk;                   // and activation blocks
+  unsigned char *act = sp + ao;
+  const int bar_id = 1 + s;
+  const bool issuer = (tid & 255) == 0;
+
+  for (int e = tid; e < kIn * kHid; e += blockDim.x) {
+    const int c = e / kHid, hh = e % kHid;
+    const __nv_bfloat16 v = W1[e];
+    *reinterpret_cast<__nv_bfloat16 *>(sp + kOffW1T + bf16_at(hh, c)) = v;
+    *reinterpret_cast<__nv_bfloat16 *>(sp + kOffW1 + (hh >> 6) * (32 * 128) +
+                                       bf16_at(c, hh & 63)) = v;
+  }
+  for (int e = tid; e < kHid * kHid; e += blockDim.x) {
+    const int i = e / kHid, o = e % kHid;
+    const __nv_bfloat16 v = W2[e];
+    *reinterpret_cast<__nv_bfloat16 *>(sp + kOffW2T + (i >> 6) * kBlk +
+                                       bf16_at(o, i & 63)) = v;
+    *reinterpret_cast<__nv_bfloat16 *>(sp + kOffW2 + (o >> 6) * kBlk +
+                                       bf16_at(i, o & 63)) = v;
+  }
+  for (int e = tid; e < kHid; e += blockDim.x) {
+    sb1[e] = b1[e];
+    sb2[e] = b2[e];
+    sw3[e] = w3[e];
+  }
+  if (tid == 0) {
+    mbar_init(base + kOffBar2, 1);
+    mbar_init(base + kOffBar2 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+        ::"r"(smem_addr(slot_p)), "r"(512)
+        : "memory");
+    asm volatile(
+        "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::
+            : "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem0 = *slot_p;
+  const uint32_t tm = tmem0 + 256u * (uint32_t)s;
+  const uint32_t lane_base = (uint32_t)(32 * q) << 16;
+  const float bias3 = b3[0];
+  const int n_tiles = (n_atoms + kRows - 1) / kRows;
+  uint32_t phase = 0, n_done = 0;
+
+  auto product = [&](uint32_t d, int a_off, int b_off, int b_blk, int n_k,
+                     uint32_t idesc) {
+    tc_fence_after();
+    for (int k = 0; k < n_k; ++k) {
+      const int kb = k >> 2, j = k & 3;
+      const uint64_t da = sdesc(base + a_off + kb * kBlk + 32 * j);
+      const uint64_t db = sdesc(base + b_off + kb * b_blk + 32 * j);
+      mma_f16(d, da, db, idesc, k != 0);
+    }
+    mma_commit(bar);
+  };
+  auto wait_product = [&]() {
+    const bool ok = mbar_wait(bar, phase & 1);
+    ++phase;
+    const bool bad = slot_sync_or(bar_id, !ok);
+    tc_fence_after();
+    return !bad;
+  };
+  auto to_product = [&]() {
+    fence_proxy_async();
+    tc_fence_before();
+    slot_sync(bar_id);
+  };
+
+  for (int t = 2 * (int)blockIdx.x + s; t < n_tiles; t += 2 * (int)gridDim.x) {
+    const int row = t * kRows + r;
+    const bool have = row < n_atoms;
+    {
+      // half h stages chunks 2h, 2h + 1 of the X row
+      const uint4 *xr = reinterpret_cast<const uint4 *>(X + (size_t)row * kIn);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int cc = 2 * h + c;
+        const uint4 w = have ? xr[cc] : make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(sp + xo + chunk_at(r, cc)) = w;
+      }
+    }
+    to_product();
+    if (issuer) product(tm, xo, kOffW1T, 0, kIn / 16, idesc_bf16(kRows, kHid));
+    if (!wait_product()) break;
+
+    // h1 = silu(z1 + b1), columns 64 h .. 64 h + 63
+#pragma unroll 1
+    for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 32) {
+      float v[32];
+      tmem_ld32(tm + lane_base + (uint32_t)c0, v);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) v[k] = silu(v[k] + sb1[c0 + k]);
+      store_row32(act, r, c0, v);
+    }
+    to_product();
+    if (issuer)
+      product(tm + 128, ao, kOffW2T, kBlk, kHid / 16, idesc_bf16(kRows, kHid));
+    if (!wait_product()) break;
+
+    // partial y and g2 = w3 * silu'(z2 + b2)
+    float yp = h ? 0.f : bias3;
+#pragma unroll 1
+    for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 32) {
+      float v[32];
+      tmem_ld32(tm + 128 + lane_base + (uint32_t)c0, v);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const float u = v[k] + sb2[c0 + k];
+        yp = fmaf(silu(u), sw3[c0 + k], yp);
+        v[k] = sw3[c0 + k] * dsilu(u);
+      }
+      store_row32(act, r, c0, v);
+    }
+    sy[(2 * s + h) * kRows + r] = yp;
+    to_product();
+    if (issuer)
+      product(tm + 128, ao, kOffW2, kBlk, kHid / 16, idesc_bf16(kRows, kHid));
+    if (!wait_product()) break;
+
+    // g1 = gh1 * silu'(z1 + b1)
+#pragma unroll 1
+    for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 32) {
+      float v[32], z[32];
+      tmem_ld32(tm + 128 + lane_base + (uint32_t)c0, v);
+      tmem_ld32(tm + lane_base + (uint32_t)c0, z);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) v[k] *= dsilu(z[k] + sb1[c0 + k]);
+      store_row32(act, r, c0, v);
+    }
+    to_product();
+    if (issuer)
+      product(tm, ao, kOffW1, 32 * 128, kHid / 16, idesc_bf16(kRows, kIn));
+    if (!wait_product()) break;
+
+    if (h == 0) {
+      // gX -> FP16 row
+      float v[32];
+      tmem_ld32(tm + lane_base, v);
+      if (have) {
+        uint4 *gr = reinterpret_cast<uint4 *>(gout + (size_t)row * kIn);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          uint4 w;
+          const __half2 h0 = __floats2half2_rn(v[8 * c + 0], v[8 * c + 1]);
+          const __half2 h1 = __floats2half2_rn(v[8 * c + 2], v[8 * c + 3]);
+          const __half2 h2 = __floats2half2_rn(v[8 * c + 4], v[8 * c + 5]);
+          const __half2 h3 = __floats2half2_rn(v[8 * c + 6], v[8 * c + 7]);
+          w.x = *reinterpret_cast<const uint32_t *>(&h0);
+          w.y = *reinterpret_cast<const uint32_t *>(&h1);
+          w.z = *reinterpret_cast<const uint32_t *>(&h2);
+          w.w = *reinterpret_cast<const uint32_t *>(&h3);
+          gr[c] = w;
+        }
+      }
+    } else if (have) {
+      y[row] = sy[(2 * s) * kRows + r] + sy[(2 * s + 1) * kRows + r];
+    }
+    ++n_done;
+    // the next tile's products overwrite z1 / gX, X and the partial sums
+    tc_fence_before();
+    slot_sync(bar_id);
+  }
+  if (issuer && phase != 4u * n_done) {
+    atomicCAS(err, 0, kErrAccumWait);
+    // a product that timed out may still be writing tensor memory: one more
+    // bounded wait for its commit before the columns are freed
+    mbar_wait(bar, (phase - 1u) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(
+                     tmem0),
+                 "r"(512)
                  : "memory");
   }
 }

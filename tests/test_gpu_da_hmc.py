@@ -80,13 +80,13 @@ def _weights(sur, seed):
 
 
 @pytest.mark.parametrize('centres,hidden,mlp', [(32, 128, 0), (32, 128, 1),
-                                               (16, 64, 0)],
+                                               (32, 128, 2), (16, 64, 0)],
                          ids=['fused-32-128-mma.sync', 'fused-32-128-tcgen05',
-                              'gemm-16-64'])
+                              'fused-32-128-tcgen05-two-tiles', 'gemm-16-64'])
 def test_surrogate_energy_and_forces_match_oracle(centres, hidden, mlp):
     """The 32-128-128 net runs one fused kernel (register-resident mma.sync
-    variant 0, tensor-memory tcgen05 variant 1), other sizes the GEMM
-    chain; all against the oracle."""
+    variant 0, tensor-memory tcgen05 variants 1 and 2), other sizes the
+    GEMM chain; all against the oracle."""
     import torch
     from pyiid_gb300._native import context
     from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
