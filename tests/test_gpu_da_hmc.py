@@ -99,35 +99,70 @@ def test_surrogate_energy_and_forces_match_oracle(centres, hidden, mlp):
         ctx.set_variant('mlp', old_mlp)
 
 
-def _check_surrogate(centres, hidden):
+def _surrogate_call(sur, pos, off, max_nb=256):
+    """Energies and forces through the sampler's call path, on a stand-in
+    holding only what it reads; returns (e, f, da)."""
     import torch
-    from pyiid_gb300.surrogate import DelayedAcceptanceHMC, RBFMLPSurrogate
-    sur = RBFMLPSurrogate(n_centres=centres, n_hidden=hidden, seed=5)
-    _weights(sur, 6)
-    pos, off = _batch()
+    from pyiid_gb300.surrogate import DelayedAcceptanceHMC
     pt = torch.as_tensor(pos, device='cuda')
-    nbr, cnt = _lists(sur, pt, off, sur.rc + 1.0, 256)
-    # the sampler's call path, on a stand-in holding only what it reads
+    nbr, cnt = _lists(sur, pt, off, sur.rc + 1.0, max_nb)
     da = DelayedAcceptanceHMC.__new__(DelayedAcceptanceHMC)
-    da.sur, da.B = sur, 2
+    da.sur, da.B = sur, len(off) - 1
     da.off, da._offp = off, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
-    da.nbr, da.cnt, da.max_nb = nbr, cnt, 256
+    da.nbr, da.cnt, da.max_nb = nbr, cnt, max_nb
     da.feat = torch.empty((len(pos), sur.C), dtype=torch.bfloat16,
                           device='cuda')
-    da.es = torch.empty(2, dtype=torch.float64, device='cuda')
+    da.es = torch.empty(len(off) - 1, dtype=torch.float64, device='cuda')
     da.fs = torch.empty((len(pos), 3), dtype=torch.float32, device='cuda')
 
     class _P:
         conv = 3.0
     da.pot = _P()
-    da.w = {'w1b': None, 'b1': None, 'w2b': None, 'b2': None, 'w3': None,
-            'b3': None}
     w1b, b1, w2b = sur._effective()
     p = sur.params
-    da.w.update({'w1b': w1b, 'b1': b1, 'w2b': w2b, 'b2': p['b2'],
-                 'w3': p['w3'], 'b3': p['b3']})
+    da.w = {'w1b': w1b, 'b1': b1, 'w2b': w2b, 'b2': p['b2'], 'w3': p['w3'],
+            'b3': p['b3']}
     e, f = da.surrogate(pt)
     torch.cuda.synchronize()
+    return e, f, da
+
+
+def test_tensor_memory_mlps_equal_mma_sync_over_many_tiles():
+    """48 x 1,000-atom configurations (375 tiles of 128 atoms, more than the
+    304 tile slots of the two-tile kernel on 152 SMs, so slots take several
+    tiles and some a partial one): both tcgen05 forms against the mma.sync
+    form, which the oracle test pins at small size.  Same BF16 roundings of
+    the activations; the per-atom output sums differ in order only."""
+    from pyiid_gb300._native import context
+    from pyiid_gb300.surrogate import RBFMLPSurrogate
+    sur = RBFMLPSurrogate(seed=5)
+    _weights(sur, 6)
+    ref = S.fcc_nearest(4.08, 1000)
+    pos = np.concatenate([S.displaced(ref, 0.05, 100 + c)
+                          for c in range(48)]).astype(np.float32)
+    off = (np.arange(49) * 1000).astype(np.int32)
+    ctx = context()
+    old = ctx.get_variant('mlp')
+    out = {}
+    try:
+        for v in (0, 1, 2):
+            ctx.set_variant('mlp', v)
+            e, f, _ = _surrogate_call(sur, pos, off)
+            out[v] = (e.cpu().numpy(), f.cpu().numpy())
+    finally:
+        ctx.set_variant('mlp', old)
+    for v in (1, 2):
+        assert rel(out[v][0], out[0][0]) < 1e-6, (v, rel(out[v][0], out[0][0]))
+        assert rel(out[v][1], out[0][1]) < 1e-5, (v, rel(out[v][1], out[0][1]))
+
+
+def _check_surrogate(centres, hidden):
+    from pyiid_gb300.surrogate import RBFMLPSurrogate
+    sur = RBFMLPSurrogate(n_centres=centres, n_hidden=hidden, seed=5)
+    _weights(sur, 6)
+    pos, off = _batch()
+    e, f, da = _surrogate_call(sur, pos, off)
+    p = sur.params
     # descriptors from the lists are the all-pairs kernel's (summed in
     # another order, so equal to BF16 rounding)
     want = M.rbf_features(pos, off, sur.C, sur.rc, sur.sigma)
