@@ -523,7 +523,8 @@ int pyiid_surrogate_forces(pyiid_ctx *ctx, const float *positions,
  *   per CTA}; pairs per thread <= 0 marks the packed (FP32x2) even/odd
  *   kernels (0: one pair per thread at a time, -2: two interleaved, -3/-4:
  *   the per-tile-pair group reduction at 3/4 CTAs per SM).  A new context
- *   starts on F(Q) variant 23 ({56, -3, 256}), variant 0 of the others. */
+ *   starts on F(Q) variant 23 ({56, -3, 256}), MLP variant 2 and variant 0
+ *   of the others. */
 enum {
   PYIID_KERNEL_FQ = 0,
   PYIID_KERNEL_GRAD_FQ = 1,
