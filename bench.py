@@ -811,13 +811,19 @@ def fq_noalloc(pos_t, sp, tab, qbin, kb, out):
     return out
 
 
-def measured_hbm_gbs():
-    """HBM copy bandwidth measured on this part (MEASURED_PEAKS.json)."""
+def measured_peak(key):
+    """A peak measured on this part (MEASURED_PEAKS.json: hbm_gbs,
+    bf16_tflops, ...), or None."""
     try:
         with open(os.path.join(REPO, 'MEASURED_PEAKS.json')) as f:
-            return float(json.load(f)['hbm_gbs'])
+            return float(json.load(f)[key])
     except (OSError, ValueError, KeyError):
         return None
+
+
+def measured_hbm_gbs():
+    """HBM copy bandwidth measured on this part (MEASURED_PEAKS.json)."""
+    return measured_peak('hbm_gbs')
 
 
 def run_pdf_transforms(torch, reps=50):
@@ -859,6 +865,7 @@ def run_pdf_transforms(torch, reps=50):
     g_flops = 2 * 3 * n * nb * n_r
     g_bytes = 4 * 3 * n * nb + 8 * 3 * n * n_r + 4 * nb * n_r
     peak = fp32_peak_tflops(torch, torch.device('cuda'))
+    bf16 = measured_peak('bf16_tflops')
     fwd_gbs = fwd_bytes / (ms_f * 1e-3) / 1e9
     return {
         'workload': 'G(r) transforms, 1000-atom Au grids (K\' 330, R 4000)',
@@ -873,9 +880,22 @@ def run_pdf_transforms(torch, reps=50):
                      'achieved_tflops': g_flops / (ms_g * 1e-3) / 1e12,
                      'fp32_peak_tflops': peak,
                      'frac': g_flops / (ms_g * 1e-3) / 1e12 / peak,
+                     'frac_of': 'live FP32 SGEMM (the accuracy the result '
+                                'keeps)',
+                     # three FP16 products per multiply-add on tcgen05
+                     'tensor': {
+                         'achieved_tflops': 3 * g_flops / (ms_g * 1e-3)
+                         / 1e12,
+                         'peak_tflops': bf16,
+                         'frac': (3 * g_flops / (ms_g * 1e-3) / 1e12 / bf16
+                                  if bf16 else None),
+                         'peak_source': 'MEASURED_PEAKS.json bf16_tflops '
+                                        '(cuBLAS bf16, burst)'},
                      'algorithmic_bytes': g_bytes,
                      'achieved_gbs': g_bytes / (ms_g * 1e-3) / 1e9,
-                     'hbm_peak_gbs': hbm},
+                     'hbm_peak_gbs': hbm,
+                     'hbm_frac': (g_bytes / (ms_g * 1e-3) / 1e9 / hbm
+                                  if hbm else None)},
     }
 
 
