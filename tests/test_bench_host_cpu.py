@@ -137,3 +137,18 @@ def test_ess_estimator_on_known_processes():
     want = T * 0.1 / 1.9
     assert 0.7 * want < bench.ess_sum(x) / B < 1.3 * want
     assert bench.ess_sum(np.ones((10, 2))) == 0.0
+
+
+def test_variant_option_rejects_unknown_kernels_before_device_work():
+    """--variant KERNEL=INDEX names a launch-variant slot of the library;
+    anything else ends with a usage error (exit 2) before a context is
+    created, so no device is touched."""
+    import subprocess
+    import sys
+    for bad in ('nosuch=1', 'mlp', 'mlp=x'):
+        r = subprocess.run([sys.executable, os.path.join(REPO, 'bench.py'),
+                            '--only-workload', 'surrogate_forces_au1000x64',
+                            '--variant', bad],
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 2, (bad, r.returncode, r.stderr[-400:])
+        assert '--variant' in r.stderr
