@@ -156,6 +156,34 @@ def test_tensor_memory_mlps_equal_mma_sync_over_many_tiles():
         assert rel(out[v][1], out[0][1]) < 1e-5, (v, rel(out[v][1], out[0][1]))
 
 
+@pytest.mark.parametrize('mlp', [2, 0], ids=['tcgen05-two-tiles', 'mma.sync'])
+def test_surrogate_matches_oracle_at_1000_atoms(mlp):
+    """The delayed-acceptance configuration's size: two displaced 1,000-atom
+    fcc Au particles, energies and forces of the 32-128-128 network against
+    the FP64 oracle with the GPU's BF16 roundings mirrored."""
+    from pyiid_gb300._native import context
+    from pyiid_gb300.surrogate import RBFMLPSurrogate
+    sur = RBFMLPSurrogate(seed=5)
+    _weights(sur, 6)
+    ref = S.fcc_nearest(4.08, 1000)
+    pos = np.concatenate([S.displaced(ref, 0.05, 7 + c)
+                          for c in range(2)]).astype(np.float32)
+    off = np.array([0, 1000, 2000], np.int32)
+    ctx = context()
+    old = ctx.get_variant('mlp')
+    ctx.set_variant('mlp', mlp)
+    try:
+        e, f, _ = _surrogate_call(sur, pos, off)
+    finally:
+        ctx.set_variant('mlp', old)
+    pc = {k: v.cpu().numpy().astype(np.float64) for k, v in sur.params.items()}
+    eo, fo = M.surrogate_energy_forces(pos, off, sur.C, sur.rc, sur.sigma,
+                                       pc['w1'], pc['b1'], pc['w2'], pc['b2'],
+                                       pc['w3'], pc['b3'], scale=3.0)
+    assert rel(e.cpu().numpy(), 3.0 * eo) < 1e-3
+    assert rel(f.cpu().numpy(), fo) < 3e-2, rel(f.cpu().numpy(), fo)
+
+
 def _check_surrogate(centres, hidden):
     from pyiid_gb300.surrogate import RBFMLPSurrogate
     sur = RBFMLPSurrogate(n_centres=centres, n_hidden=hidden, seed=5)
