@@ -75,6 +75,10 @@ def test_variant_tables_are_described_without_a_gpu():
     for _, info in variants('fq_grad'):
         assert info['pairs_per_thread'] == 0          # packed kernels only
         assert info['threads'] % 32 == 0 and 32 % (info['threads'] // 32) == 0
+    # the surrogate MLP: mma.sync, tcgen05 one tile, tcgen05 two tiles
+    mlp = [(i['bins_per_thread'], i['pairs_per_thread'], i['threads'])
+           for _, i in variants('mlp')]
+    assert mlp == [(16, 0, 256), (128, 1, 128), (256, 1, 512)]
 
 
 def header_prototypes():
